@@ -1,0 +1,292 @@
+"""Benchmark: single-complex pose-scoring throughput on one GB300.
+
+Workload (the single-complex scoring configuration): a seeded synthetic
+receptor of 300 residues (~2,470 atoms) and ligand of 150 residues (~1,220
+atoms) with 12 restraints; 65,536 poses with rotations uniform on SO(3)
+(unit quaternions, expressed as gdock's Euler genes) and centroid
+translations uniform in a 40 A cube.  One step = scoring all 65,536 poses
+(pose transform, soft-core LJ, Coulomb, desolvation, AIR) in the batched
+FP32 form.
+
+Reported: ``value`` = poses/s with poses resident in HBM (CUDA events on the
+launching stream, L2 flushed between steps); ``e2e`` = poses/s through
+gd_score_poses with host genes and host results (host frames, H2D, kernel,
+D2H inside the timed region); the plain FP64 form on a pose sample; the
+per-component error of FP32 against FP64; the roofline of the scoring
+kernel; and the CPU oracle timed on a bounded sample on the host cores.
+
+``--impl reference`` times the CPU restatement of gdock's scoring (the
+reference itself is Rust and cannot be built here) on all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_REC_RES, N_LIG_RES, N_RESTRAINTS, N_POSES, SEED = 300, 150, 12, 65536, 2026
+FLOP_PER_PAIR = 37  # convention: d2 8, LJ 18, Coulomb 4, cutoff tests 5, burial 2
+METRIC = "poses/s (batched FP32 scoring, single complex)"
+
+
+def workload():
+    from gdock_gb300 import position_ligand, synth
+    c = synth.make_complex(N_REC_RES, N_LIG_RES, N_RESTRAINTS, seed=SEED)
+    lig = position_ligand(c.receptor, c.ligand)
+    genes = synth.quaternion_genes(np.random.default_rng(SEED + 1), N_POSES, half_box=20.0)
+    return c, lig, genes
+
+
+def config(c, lig, extra=None):
+    d = {"workload": "single-complex scoring: synthetic 300-residue receptor x 150-residue ligand, "
+                     "65,536 SO(3)-uniform poses",
+         "receptor_atoms": len(c.receptor), "ligand_atoms": len(lig), "restraints": N_RESTRAINTS,
+         "poses_per_step": N_POSES, "seed": SEED, "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.strip()]
+            sm = [float(r[0]) for r in rows]
+            mx = [float(r[1]) for r in rows]
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[3 + k]})
+            return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": reasons,
+                    "samples": len(rows), "power_w_max": max(float(r[2]) for r in rows)}
+        except Exception as e:  # noqa: BLE001
+            return {"error": str(e)}
+
+
+def measured_peaks(torch):
+    """FP32 and FP64 peaks measured on this GPU: cuBLAS SGEMM (TF32 off) and
+    DGEMM, best of 5 at 8192^3 / 4096^3."""
+    out = {}
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n in (("fp32", torch.float32, 8192), ("fp64", torch.float64, 4096)):
+        a = torch.randn(n, n, device="cuda", dtype=dt)
+        b = torch.randn(n, n, device="cuda", dtype=dt)
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        out[name] = 2.0 * n ** 3 / best / 1e12
+        del a, b
+    return out
+
+
+def cpu_sample(c, lig, genes, n_sample, threads):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    g = genes[:n_sample]
+    t0 = time.perf_counter()
+    oracle.score_poses(c.receptor, lig, c.restraint_pairs, g, nthreads=threads)
+    return n_sample / (time.perf_counter() - t0)
+
+
+def run_reference(args):
+    import torch.distributed as dist  # noqa: F401  (imported for parity with the GPU arm)
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    c, lig, genes = workload()
+    threads = os.cpu_count() or 1
+    n_sample = max(4, int(os.environ.get("GD_REF_SAMPLE", "32")))
+    for _ in range(args.warmup):
+        cpu_sample(c, lig, genes, min(n_sample, 8), threads)
+    vals = [cpu_sample(c, lig, genes[i * n_sample:], n_sample, threads) for i in range(args.steps)]
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "poses/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": N_POSES / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(c, lig, {"sample_poses_per_step": n_sample}),
+            "cpu_baseline": {"value": v, "unit": "poses/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_sample} poses of the workload per step, extrapolated per pose"},
+            "e2e": {"value": v, "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "gdock is Rust and cargo is not available: the CPU oracle (C restatement of its FP64 "
+                    "scoring, threaded per pose like its rayon map) stands in for it"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-sample", type=int, default=2048)
+    ap.add_argument("--cpu-sample", type=int, default=32)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    import gdock_gb300 as gd
+    from gdock_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    c, lig, genes = workload()
+    ctx = gd.Context(local)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    lib = ctx.lib
+    frames_h = _lib.make_frames(genes)
+    frames = torch.from_numpy(frames_h).to(f"cuda:{local}")
+    out = torch.zeros((N_POSES, 6), dtype=torch.float64, device=f"cuda:{local}")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MiB > L2
+    max_disp = float(np.abs(genes[:, 3:]).max())
+    stream = torch.cuda.current_stream()
+
+    def launch(prec, n=N_POSES):
+        ctx.check(lib.gd_score_frames_device(cx.h, frames.data_ptr(), n, prec, max_disp, out.data_ptr(),
+                                             stream.cuda_stream))
+
+    # --- device-resident throughput (value) ---
+    for _ in range(args.warmup):
+        launch(gd.GD_PREC_F32)
+    torch.cuda.synchronize()
+    ctx.sync()
+    if world > 1:
+        dist.barrier()
+    times = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch(gd.GD_PREC_F32)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize()
+    ctx.sync()
+    t_step = float(np.sum(times)) / args.steps
+    if world > 1:
+        t = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+        dist.barrier()
+    value = world * N_POSES / t_step
+    res32 = out.cpu().numpy().copy()
+
+    # --- end to end through the C ABI with host buffers (e2e) ---
+    cx.score_poses(genes, gd.GD_PREC_F32)  # warm
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        cx.score_poses(genes, gd.GD_PREC_F32)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = N_POSES / float(np.median(e2e_t))
+
+    # --- plain FP64 form on a sample; FP32-vs-FP64 error per component ---
+    ns = min(args.fp64_sample, N_POSES)
+    launch(gd.GD_PREC_F64, ns)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(1.0)
+    e0.record(stream)
+    launch(gd.GD_PREC_F64, ns)
+    e1.record(stream)
+    e1.synchronize()
+    ctx.sync()
+    t64 = e0.elapsed_time(e1) / 1e3
+    res64 = out[:ns].cpu().numpy()
+    names = ("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")
+    err = {n: float(np.max(np.abs(res32[:ns, k] - res64[:, k]) / np.maximum(np.abs(res64[:, k]), 1.0)))
+           for k, n in enumerate(names)}
+    plain = ns / t64
+
+    line = {}
+    if rank == 0:
+        pairs = len(c.receptor) * len(lig)
+        peaks = measured_peaks(torch)
+        achieved = FLOP_PER_PAIR * pairs * N_POSES / t_step / 1e12
+        cpu_threads = os.cpu_count() or 1
+        cpu_v = cpu_sample(c, lig, genes, args.cpu_sample, cpu_threads)
+        line = {
+            "metric": METRIC, "value": value, "unit": "poses/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(c, lig, {"parallelism": "replicas" if world > 1 else "single GPU"}),
+            "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": N_POSES * _lib.POSE_FRAME_BYTES,
+                    "d2h_bytes_per_step": N_POSES * 48},
+            "gpu_launches": args.steps,
+            "pair_evals_per_s": pairs * value,
+            "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,
+                           "tflops": FLOP_PER_PAIR * pairs * plain / 1e12,
+                           "frac_of_fp64_peak": FLOP_PER_PAIR * pairs * plain / 1e12 / peaks["fp64"]},
+            "f32_over_f64_speedup": value / plain,
+            "f32_rel_error_vs_f64": err,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32"], "unit": "TFLOP/s",
+                         "frac": achieved / peaks["fp32"], "traffic": None,
+                         "peak_source": "cuBLAS SGEMM (TF32 off) measured in this run; "
+                                        "37 flop per receptor-ligand pair convention"},
+            "cpu_baseline": {"value": cpu_v, "unit": "poses/s", "cores": cpu_threads, "kind": "port",
+                             "sample": f"{args.cpu_sample} poses of the workload"},
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    cx.close()
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+"""gdock_gb300: GB300-native population fitness evaluation and FCC clustering
+for the gdock protein-protein docker.
+
+The compute runs in ``libgdock_gb300.so`` (CUDA, sm_103a) behind the C ABI of
+``include/gdock_gb300.h``; this package is the thin Python view of that ABI
+used by the tests and the benchmark, with the reference's names:
+
+* ``Complex.score_poses``  -> Population::eval_fitness (src/population.rs:48-61)
+* ``Complex.score_models`` -> commands::score::score (src/commands/score.rs:32-79)
+* ``vdw_energy`` / ``elec_energy`` / ``desolv_energy`` / ``air_energy`` /
+  ``satisfaction_ratio`` -> src/fitness.rs
+* ``Complex.pose_contacts`` -> clustering::calculate_contacts (src/clustering.rs:62-115)
+* ``Complex.cluster`` / ``cluster_sets`` -> clustering::cluster_structures
+  (src/clustering.rs:265-293)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms, make_frames, ptr
+from .pdb import Molecule, combine_molecules, position_ligand, read_pdb, read_pdb_text
+
+__all__ = [
+    "Context", "Complex", "GdError", "GD_PREC_F32", "GD_PREC_F64", "EnergyWeights", "ClusteringConfig",
+    "ClusterResult", "vdw_energy", "elec_energy", "desolv_energy", "air_energy", "satisfaction_ratio",
+    "cluster_sets", "make_frames", "Molecule", "read_pdb", "read_pdb_text", "position_ligand",
+    "combine_molecules", "default_context",
+]
+
+
+@dataclass
+class EnergyWeights:
+    """src/constants.rs:28-56"""
+    vdw: float = 0.4
+    elec: float = 0.05
+    desolv: float = 3.4
+    air: float = 1.0
+
+
+@dataclass
+class ClusteringConfig:
+    """src/clustering.rs:14-35"""
+    contact_distance: float = 5.0
+    fcc_cutoff: float = 0.60
+    strictness: float = 0.75
+    min_cluster_size: int = 4
+
+    def c(self):
+        return _lib.GdClusterCfg(self.contact_distance, self.fcc_cutoff, self.strictness, self.min_cluster_size)
+
+
+@dataclass
+class ClusterResult:
+    """src/clustering.rs:38-46"""
+    center_idx: int
+    members: List[int]
+    size: int
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _prec(p) -> int:
+    if p in (GD_PREC_F32, "f32", "fp32", "float32"):
+        return GD_PREC_F32
+    if p in (GD_PREC_F64, "f64", "fp64", "float64"):
+        return GD_PREC_F64
+    raise ValueError(f"unknown precision {p!r}")
+
+
+class Complex:
+    """A receptor + positioned ligand resident on the GPU (gd_complex)."""
+
+    def __init__(self, receptor: Molecule, ligand: Molecule, restraint_pairs: Sequence[Tuple[int, int]] = (),
+                 weights: EnergyWeights = EnergyWeights(), ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        self.receptor, self.ligand = receptor, ligand
+        self._r, self._l = PackedAtoms(receptor), PackedAtoms(ligand)
+        pairs = np.ascontiguousarray(np.asarray(list(restraint_pairs), dtype=np.int32).reshape(-1, 2))
+        w = _lib.GdWeights(weights.vdw, weights.elec, weights.desolv, weights.air)
+        h = C.c_void_p()
+        self.ctx.check(self.lib.gd_complex_create(self.ctx.h, C.byref(self._r.s), C.byref(self._l.s),
+                                                  ptr(pairs) if pairs.size else None, pairs.shape[0],
+                                                  C.byref(w), C.byref(h)))
+        self.h = h
+
+    @property
+    def num_restraints(self) -> int:
+        return int(self.lib.gd_complex_num_restraints(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gd_complex_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def score_poses(self, genes, precision=GD_PREC_F64) -> np.ndarray:
+        """Energies of n poses (genes n x 6) as a structured array with the
+        fields fitness, vdw, elec, desolv, air, restraint_penalty."""
+        g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+        out = np.zeros(g.shape[0], dtype=POSE_ENERGY_DTYPE)
+        self.ctx.check(self.lib.gd_score_poses(self.h, ptr(g), g.shape[0], _prec(precision), ptr(out)))
+        return out
+
+    def score_models(self, xyz, precision=GD_PREC_F64) -> np.ndarray:
+        """Energies of ligand coordinate sets given as is (n x n_lig x 3)."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, len(self.ligand), 3)
+        out = np.zeros(x.shape[0], dtype=POSE_ENERGY_DTYPE)
+        self.ctx.check(self.lib.gd_score_models(self.h, ptr(x), x.shape[0], _prec(precision), ptr(out)))
+        return out
+
+    def pose_contacts(self, genes) -> List[np.ndarray]:
+        g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+        n = g.shape[0]
+        offs = np.zeros(n + 1, dtype=np.int64)
+        cap = 1 << 16
+        for _ in range(2):
+            keys = np.zeros(cap, dtype=np.int64)
+            st = self.lib.gd_pose_contacts(self.h, ptr(g), n, ptr(keys), cap, ptr(offs))
+            if st == _lib.GD_ERR_CAPACITY:
+                cap = int(offs[n])
+                continue
+            self.ctx.check(st)
+            break
+        return [keys[offs[i]:offs[i + 1]].copy() for i in range(n)]
+
+    def cluster(self, genes, config: ClusteringConfig = ClusteringConfig()) -> List[ClusterResult]:
+        g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+        n = g.shape[0]
+        centers, sizes, members = (np.zeros(max(n, 1), np.int32) for _ in range(3))
+        k = C.c_int32(0)
+        cfg = config.c()
+        self.ctx.check(self.lib.gd_cluster(self.h, ptr(g), n, C.byref(cfg), C.byref(k), ptr(centers), ptr(sizes),
+                                           ptr(members)))
+        return _results(k.value, centers, sizes, members)
+
+
+def _results(k, centers, sizes, members) -> List[ClusterResult]:
+    out, m = [], 0
+    for c in range(k):
+        s = int(sizes[c])
+        out.append(ClusterResult(int(centers[c]), members[m:m + s].tolist(), s))
+        m += s
+    return out
+
+
+def cluster_sets(sets: Sequence[np.ndarray], config: ClusteringConfig = ClusteringConfig(),
+                 ctx: Optional[Context] = None) -> List[ClusterResult]:
+    """cluster_structures on precomputed contact-key sets (FCC on the GPU)."""
+    ctx = ctx or default_context()
+    n = len(sets)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    for i, s in enumerate(sets):
+        offs[i + 1] = offs[i] + len(s)
+    keys = np.ascontiguousarray(np.concatenate([np.asarray(s, np.int64) for s in sets]) if n else np.zeros(1, np.int64))
+    if keys.size == 0:
+        keys = np.zeros(1, np.int64)
+    centers, sizes, members = (np.zeros(max(n, 1), np.int32) for _ in range(3))
+    k = C.c_int32(0)
+    cfg = config.c()
+    ctx.check(ctx.lib.gd_cluster_sets(ctx.h, ptr(keys), ptr(offs), n, C.byref(cfg), C.byref(k), ptr(centers),
+                                      ptr(sizes), ptr(members)))
+    return _results(k.value, centers, sizes, members)
+
+
+# -- reference-named energy functions (src/fitness.rs) -------------------------
+
+def _one_shot(receptor, ligand, pairs=(), precision=GD_PREC_F64):
+    cx = Complex(receptor, ligand, pairs)
+    try:
+        return cx.score_models(ligand.xyz()[None], precision)[0], cx.num_restraints
+    finally:
+        cx.close()
+
+
+def vdw_energy(receptor: Molecule, ligand: Molecule) -> float:
+    return float(_one_shot(receptor, ligand)[0]["vdw"])
+
+
+def elec_energy(receptor: Molecule, ligand: Molecule) -> float:
+    return float(_one_shot(receptor, ligand)[0]["elec"])
+
+
+def desolv_energy(receptor: Molecule, ligand: Molecule) -> float:
+    return float(_one_shot(receptor, ligand)[0]["desolv"])
+
+
+def air_energy(restraint_pairs, receptor: Molecule, ligand: Molecule) -> float:
+    return float(_one_shot(receptor, ligand, restraint_pairs)[0]["air"])
+
+
+def satisfaction_ratio(restraint_pairs, receptor: Molecule, ligand: Molecule) -> float:
+    e, k = _one_shot(receptor, ligand, restraint_pairs)
+    return 0.0 if k == 0 else 1.0 - float(e["restraint_penalty"]) / k

@@ -1,0 +1,160 @@
+"""ctypes bindings of libgdock_gb300.so (the C ABI in include/gdock_gb300.h).
+
+The shared library is built in-tree (``gdock_gb300/_build``); loading fails
+loudly when it is missing or when no CUDA device is present — there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libgdock_gb300.so"
+
+GD_OK, GD_ERR_INVALID_ARG, GD_ERR_OOM, GD_ERR_CUDA, GD_ERR_TIMEOUT, GD_ERR_CAPACITY, GD_ERR_STATE = range(7)
+GD_PREC_F64, GD_PREC_F32 = 0, 1
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTS = (
+    "gd_abi_version", "gd_status_string", "gd_context_create", "gd_context_destroy", "gd_last_error",
+    "gd_context_bytes_in_use", "gd_complex_create", "gd_complex_destroy", "gd_complex_num_restraints",
+    "gd_complex_set_weights", "gd_make_frames", "gd_score_poses", "gd_score_frames_device", "gd_sync",
+    "gd_score_models", "gd_pose_contacts", "gd_cluster", "gd_cluster_sets",
+)
+
+
+class GdAtoms(C.Structure):
+    _fields_ = [("n", C.c_int32), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("epsilon", C.c_void_p), ("rmin2", C.c_void_p), ("charge", C.c_void_p),
+                ("vdw_radius", C.c_void_p), ("serial", C.c_void_p), ("resseq", C.c_void_p),
+                ("chain", C.c_void_p), ("element", C.c_void_p), ("is_ca", C.c_void_p)]
+
+
+class GdWeights(C.Structure):
+    _fields_ = [("vdw", C.c_double), ("elec", C.c_double), ("desolv", C.c_double), ("air", C.c_double)]
+
+
+class GdClusterCfg(C.Structure):
+    _fields_ = [("contact_distance", C.c_double), ("fcc_cutoff", C.c_double), ("strictness", C.c_double),
+                ("min_cluster_size", C.c_int32)]
+
+
+POSE_ENERGY_DTYPE = np.dtype([(k, np.float64) for k in
+                              ("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")])
+POSE_FRAME_BYTES = 16 * 8
+
+_lib = None
+
+
+class GdError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"gdock_gb300 error {status}: {msg}")
+        self.status = status
+
+
+def load(path: Path = LIB_PATH):
+    """Load the library (building it first if the build is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build as _build
+    _build.build()
+    lib = C.CDLL(str(path))
+    vp, i32, i64, d = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    sigs = {
+        "gd_abi_version": ([], i32),
+        "gd_status_string": ([C.c_int], C.c_char_p),
+        "gd_context_create": ([i32, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "gd_context_destroy": ([vp], C.c_int),
+        "gd_last_error": ([vp], C.c_char_p),
+        "gd_context_bytes_in_use": ([vp], C.c_uint64),
+        "gd_complex_create": ([vp, C.POINTER(GdAtoms), C.POINTER(GdAtoms), vp, i32, C.POINTER(GdWeights),
+                               C.POINTER(vp)], C.c_int),
+        "gd_complex_destroy": ([vp], C.c_int),
+        "gd_complex_num_restraints": ([vp], i32),
+        "gd_complex_set_weights": ([vp, C.POINTER(GdWeights)], C.c_int),
+        "gd_make_frames": ([vp, i32, vp], C.c_int),
+        "gd_score_poses": ([vp, vp, i32, C.c_int, vp], C.c_int),
+        "gd_score_frames_device": ([vp, vp, i32, C.c_int, d, vp, vp], C.c_int),
+        "gd_sync": ([vp], C.c_int),
+        "gd_score_models": ([vp, vp, i32, C.c_int, vp], C.c_int),
+        "gd_pose_contacts": ([vp, vp, i32, vp, i64, vp], C.c_int),
+        "gd_cluster": ([vp, vp, i32, C.POINTER(GdClusterCfg), C.POINTER(i32), vp, vp, vp], C.c_int),
+        "gd_cluster_sets": ([vp, vp, vp, i32, C.POINTER(GdClusterCfg), C.POINTER(i32), vp, vp, vp], C.c_int),
+    }
+    for name, (args, res) in sigs.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Context:
+    """One CUDA device context of the library."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.gd_context_create(device, hbm_budget_bytes, C.byref(h))
+        if st != GD_OK:
+            raise GdError(st, f"gd_context_create failed ({self.lib.gd_status_string(st).decode()}); "
+                              "a CUDA device is required")
+        self.h = h
+
+    def check(self, st: int):
+        if st != GD_OK:
+            raise GdError(st, self.lib.gd_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.gd_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def sync(self):
+        self.check(self.lib.gd_sync(self.h))
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(self.lib.gd_context_bytes_in_use(self.h))
+
+
+class PackedAtoms:
+    """gd_atoms view of a pdb.Molecule; keeps the numpy buffers alive."""
+
+    def __init__(self, mol):
+        c = np.ascontiguousarray
+        self.bufs = [c(mol.x, np.float64), c(mol.y, np.float64), c(mol.z, np.float64),
+                     c(mol.epsilon, np.float64), c(mol.rmin2, np.float64), c(mol.charge, np.float64),
+                     c(mol.vdw_radius, np.float64), c(mol.serial, np.int32), c(mol.resseq, np.int16),
+                     c(mol.chain_code, np.uint8), c(mol.element_class, np.uint8), c(mol.is_ca, np.uint8)]
+        self.s = GdAtoms(len(mol), *[ptr(b) for b in self.bufs])
+
+
+def make_frames(genes: np.ndarray) -> np.ndarray:
+    """Pose frames (n x 16 doubles) of n x 6 genes, computed by the library."""
+    lib = load()
+    g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+    out = np.zeros((g.shape[0], 16))
+    st = lib.gd_make_frames(ptr(g), g.shape[0], ptr(out))
+    if st != GD_OK:
+        raise GdError(st, "gd_make_frames")
+    return out

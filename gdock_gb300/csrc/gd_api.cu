@@ -1,0 +1,556 @@
+// C ABI of gdock_gb300: contexts, complex upload (host-side packing of the
+// receptor/ligand into the device layout), pose frames, and the scoring
+// entry points.  No call throws across the ABI; every failure becomes a
+// gd_status with a message in gd_last_error().
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <new>
+#include <thread>
+#include <unordered_set>
+#include <utility>
+
+#include "gd_internal.cuh"
+
+namespace gd {
+
+gd_status fail(gd_context *ctx, gd_status s, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  return s;
+}
+
+gd_status cuda_fail(gd_context *ctx, cudaError_t e, const char *what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return fail(ctx, e == cudaErrorMemoryAllocation ? GD_ERR_OOM : GD_ERR_CUDA, m);
+}
+
+gd_status dev_alloc(gd_context *ctx, uint64_t bytes, void **p) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  if (ctx->budget && ctx->in_use + bytes > ctx->budget)
+    return fail(ctx, GD_ERR_OOM, "HBM budget exceeded: " + std::to_string(ctx->in_use + bytes) + " > " +
+                                     std::to_string(ctx->budget) + " bytes");
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_fail(ctx, e, "cudaMalloc");
+  }
+  ctx->in_use += bytes;
+  return GD_OK;
+}
+
+void dev_free(gd_context *ctx, void *p, uint64_t bytes) {
+  if (!p) return;
+  if (bytes == 0) bytes = 16;
+  cudaFree(p);
+  ctx->in_use -= std::min<uint64_t>(ctx->in_use, bytes);
+}
+
+gd_status ensure_scratch(gd_context *ctx, size_t dev_bytes, size_t pinned_bytes) {
+  if (dev_bytes > ctx->d_scratch_bytes) {
+    if (ctx->d_scratch) dev_free(ctx, ctx->d_scratch, ctx->d_scratch_bytes);
+    ctx->d_scratch = nullptr;
+    ctx->d_scratch_bytes = 0;
+    size_t want = std::max(dev_bytes, static_cast<size_t>(1) << 20);
+    gd_status s = dev_alloc(ctx, want, &ctx->d_scratch);
+    if (s != GD_OK) return s;
+    ctx->d_scratch_bytes = want;
+  }
+  if (pinned_bytes > ctx->h_pinned_bytes) {
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    ctx->h_pinned = nullptr;
+    ctx->h_pinned_bytes = 0;
+    size_t want = std::max(pinned_bytes, static_cast<size_t>(1) << 20);
+    cudaError_t e = cudaMallocHost(&ctx->h_pinned, want);
+    if (e != cudaSuccess) {
+      ctx->h_pinned = nullptr;
+      return cuda_fail(ctx, e, "cudaMallocHost");
+    }
+    ctx->h_pinned_bytes = want;
+  }
+  return GD_OK;
+}
+
+gd_status check_device_error(gd_context *ctx) {
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "reading the device error word");
+  if (h == kDevOk) return GD_OK;
+  cudaMemset(ctx->d_err, 0, sizeof(int));
+  if (h == kDevTimeout) return fail(ctx, GD_ERR_TIMEOUT, "a device-side wait exceeded its spin limit");
+  if (h == kDevCapacity) return fail(ctx, GD_ERR_CAPACITY, "a device-side buffer was too small");
+  return fail(ctx, GD_ERR_CUDA, "device error code " + std::to_string(h));
+}
+
+// Smallest double x with sqrt(x) >= c: then sqrt(d2) < c  <=>  d2 < x.
+static double thr_lt(double c) {
+  double x = c * c;
+  while (std::sqrt(x) >= c) x = std::nextafter(x, 0.0);
+  while (!(std::sqrt(x) >= c)) x = std::nextafter(x, INFINITY);
+  return x;
+}
+// Largest double x with sqrt(x) <= c: then sqrt(d2) <= c <=> d2 <= x, and
+// sqrt(d2) > c <=> d2 > x.
+static double thr_le(double c) {
+  double x = c * c;
+  while (std::sqrt(x) <= c) x = std::nextafter(x, INFINITY);
+  while (std::sqrt(x) > c) x = std::nextafter(x, 0.0);
+  return x;
+}
+
+// Cutoffs of src/constants.rs:59-63 and the clustering contact distance.
+Thresholds make_thresholds(double contact_cutoff) {
+  Thresholds t;
+  t.vdw_lt = thr_lt(12.0);
+  t.elec_gt = thr_le(1.0);
+  t.elec_lt = thr_lt(15.0);
+  t.desolv_lt = thr_lt(8.0);
+  t.contact_le = thr_le(contact_cutoff);
+  return t;
+}
+
+// Frame of one pose: the cosines/sines the reference evaluates per atom, and
+// the composite matrix entries in its operation order (src/structure.rs:96-103).
+void make_frame(const double *g, gd_pose_frame *f) {
+  const double ca = std::cos(g[0]), sa = std::sin(g[0]);
+  const double cb = std::cos(g[1]), sb = std::sin(g[1]);
+  const double cg = std::cos(g[2]), sg = std::sin(g[2]);
+  f->ca = ca;
+  f->sa = sa;
+  f->cb = cb;
+  f->sb = sb;
+  f->cg = cg;
+  f->sg = sg;
+  f->m01 = -sa * cg + ca * sb * sg;
+  f->m02 = sa * sg + ca * sb * cg;
+  f->m11 = ca * cg + sa * sb * sg;
+  f->m12 = -ca * sg + sa * sb * cg;
+  f->dx = g[3];
+  f->dy = g[4];
+  f->dz = g[5];
+  f->pad[0] = f->pad[1] = f->pad[2] = 0.0;
+}
+
+// Half-widths of the FP32 guard bands on d2.  The FP32 coordinates carry at
+// most M*2^-24 rounding (M bounds |x - O|); for a pair at distance c the
+// computed d2 is then off by at most ~2c*sqrt(3)*(2M*2^-24 + c*2^-24) +
+// 4c^2*2^-24.  Four times that is the band.
+void guard_widths(const gd_complex *cx, double max_disp, float *gv, float *ge, float *gdd) {
+  const double u = std::ldexp(1.0, -24);
+  const double lig = std::max({std::fabs(cx->cx - cx->ox), std::fabs(cx->cy - cx->oy), std::fabs(cx->cz - cx->oz)}) +
+                     cx->lig_radius + max_disp;
+  const double M = std::max(cx->rec_extent, lig) + 1.0;
+  auto band = [&](double c) {
+    const double err = 2.0 * c * std::sqrt(3.0) * (2.0 * M * u + c * u) + 4.0 * c * c * u;
+    return static_cast<float>(4.0 * err + 1e-6);
+  };
+  *gv = band(12.0);
+  *ge = band(15.0);
+  *gdd = band(8.0);
+}
+
+static double asp_of(uint8_t e) {  // src/fitness.rs:129-138
+  switch (e) {
+    case GD_ELEM_C: return 0.012;
+    case GD_ELEM_N: return -0.160;
+    case GD_ELEM_O: return -0.160;
+    case GD_ELEM_S: return 0.012;
+    default: return 0.0;
+  }
+}
+
+// Energy contribution of one atom at burial counts 0..10: the reference's
+// `energy -= asp * burial * r * r * 4.0 * PI` (src/fitness.rs:141-181).
+static void desolv_row(uint8_t elem, double r, double *row) {
+  const double asp = asp_of(elem);
+  for (int c = 0; c <= 10; ++c) {
+    if (std::fabs(asp) < 0.001) {
+      row[c] = 0.0;
+      continue;
+    }
+    double burial = static_cast<double>(c) / 10.0;
+    if (!(burial < 1.0)) burial = 1.0;
+    const double term = asp * burial * r * r * 4.0 * 3.141592653589793;
+    row[c] = -term;
+  }
+}
+
+static double powi6(double x) {
+  const double x2 = x * x;
+  const double x4 = x2 * x2;
+  return x2 * x4;
+}
+
+static bool atoms_ok(const gd_atoms *a) {
+  if (!a || a->n < 0) return false;
+  if (a->n == 0) return true;
+  return a->x && a->y && a->z && a->epsilon && a->rmin2 && a->charge && a->vdw_radius && a->serial && a->resseq &&
+         a->chain && a->element && a->is_ca;
+}
+
+template <typename T>
+static gd_status upload(gd_complex *cx, const std::vector<T> &h, T **d) {
+  void *p = nullptr;
+  gd_status s = dev_alloc(cx->ctx, sizeof(T) * std::max<size_t>(h.size(), 1), &p);
+  if (s != GD_OK) return s;
+  cx->allocs.push_back(p);
+  cx->bytes += sizeof(T) * std::max<size_t>(h.size(), 1);
+  *d = static_cast<T *>(p);
+  if (!h.empty()) {
+    cudaError_t e = cudaMemcpy(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(cx->ctx, e, "cudaMemcpy (complex upload)");
+  }
+  return GD_OK;
+}
+
+static void centroid(const double *x, const double *y, const double *z, int n, double *c) {
+  double sx = -0.0, sy = -0.0, sz = -0.0;  // left folds, as Molecule::center_of_mass
+  for (int i = 0; i < n; ++i) sx += x[i];
+  for (int i = 0; i < n; ++i) sy += y[i];
+  for (int i = 0; i < n; ++i) sz += z[i];
+  c[0] = sx / n;
+  c[1] = sy / n;
+  c[2] = sz / n;
+}
+
+}  // namespace gd
+
+using namespace gd;
+
+extern "C" {
+
+int32_t gd_abi_version(void) { return GD_ABI_VERSION; }
+
+const char *gd_status_string(gd_status s) {
+  switch (s) {
+    case GD_OK: return "ok";
+    case GD_ERR_INVALID_ARG: return "invalid argument";
+    case GD_ERR_OOM: return "out of device memory";
+    case GD_ERR_CUDA: return "CUDA error";
+    case GD_ERR_TIMEOUT: return "device wait timed out";
+    case GD_ERR_CAPACITY: return "output capacity too small";
+    case GD_ERR_STATE: return "invalid state";
+  }
+  return "unknown status";
+}
+
+gd_status gd_context_create(int32_t device, uint64_t hbm_budget_bytes, gd_context **out) {
+  if (!out) return GD_ERR_INVALID_ARG;
+  *out = nullptr;
+  gd_context *ctx = new (std::nothrow) gd_context();
+  if (!ctx) return GD_ERR_OOM;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || device < 0 || device >= ndev) {
+    delete ctx;
+    return e != cudaSuccess ? GD_ERR_CUDA : GD_ERR_INVALID_ARG;
+  }
+  ctx->device = device;
+  ctx->budget = hbm_budget_bytes;
+  if ((e = cudaSetDevice(device)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&ctx->ev0)) != cudaSuccess || (e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) {
+    delete ctx;
+    return GD_ERR_CUDA;
+  }
+  void *p = nullptr;
+  if (dev_alloc(ctx, sizeof(int), &p) != GD_OK) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GD_ERR_OOM;
+  }
+  ctx->d_err = static_cast<int *>(p);
+  cudaMemset(ctx->d_err, 0, sizeof(int));
+  *out = ctx;
+  return GD_OK;
+}
+
+gd_status gd_context_destroy(gd_context *ctx) {
+  if (!ctx) return GD_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GD_OK;
+}
+
+const char *gd_last_error(const gd_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+uint64_t gd_context_bytes_in_use(const gd_context *ctx) { return ctx ? ctx->in_use : 0; }
+
+gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms *lig, const int32_t *restraint_pairs,
+                            int32_t n_pairs, const gd_weights *w, gd_complex **out) {
+  if (!ctx || !out) return GD_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (!atoms_ok(rec) || !atoms_ok(lig)) return fail(ctx, GD_ERR_INVALID_ARG, "receptor/ligand arrays incomplete");
+  if (n_pairs < 0 || (n_pairs > 0 && !restraint_pairs)) return fail(ctx, GD_ERR_INVALID_ARG, "bad restraint pairs");
+  cudaSetDevice(ctx->device);
+  gd_complex *cx = new (std::nothrow) gd_complex();
+  if (!cx) return fail(ctx, GD_ERR_OOM, "host allocation");
+  cx->ctx = ctx;
+  cx->nr = rec->n;
+  cx->nl = lig->n;
+  cx->w = w ? *w : gd_weights{0.4, 0.05, 3.4, 1.0};
+
+  // atom types: distinct (epsilon, Rmin/2) pairs over both molecules
+  std::map<std::pair<uint64_t, uint64_t>, int> types;
+  std::vector<double> t_eps, t_rmin;
+  auto type_of = [&](double e, double r) {
+    uint64_t be, br;
+    std::memcpy(&be, &e, 8);
+    std::memcpy(&br, &r, 8);
+    auto it = types.find({be, br});
+    if (it != types.end()) return it->second;
+    const int id = static_cast<int>(t_eps.size());
+    types[{be, br}] = id;
+    t_eps.push_back(e);
+    t_rmin.push_back(r);
+    return id;
+  };
+  std::vector<int> rtype(rec->n), ltype(lig->n);
+  for (int i = 0; i < rec->n; ++i) rtype[i] = type_of(rec->epsilon[i], rec->rmin2[i]);
+  for (int j = 0; j < lig->n; ++j) ltype[j] = type_of(lig->epsilon[j], lig->rmin2[j]);
+  if (t_eps.empty()) type_of(0.0, 0.0);
+  const int nt = static_cast<int>(t_eps.size());
+  if (nt > kMaxTypes) {
+    delete cx;
+    return fail(ctx, GD_ERR_INVALID_ARG, "more than 64 distinct (epsilon, rmin2) atom types");
+  }
+  cx->nt = nt;
+  std::vector<TypePair32> tab32(static_cast<size_t>(nt) * nt);
+  std::vector<TypePair64> tab64(static_cast<size_t>(nt) * nt);
+  for (int a = 0; a < nt; ++a)
+    for (int b = 0; b < nt; ++b) {
+      // softcore_lj_potential's per-pair constants (src/fitness.rs:58-63)
+      const double eps = std::sqrt(t_eps[a] * t_eps[b]);
+      const double r6 = powi6(t_rmin[a] + t_rmin[b]);
+      tab64[a * nt + b] = TypePair64{r6, 0.5 * r6, eps, 0.0};
+      tab32[a * nt + b] = TypePair32{static_cast<float>(r6), static_cast<float>(eps), static_cast<float>(-2.0 * eps), 0.f};
+      if (eps > 50.0) cx->need_clamp = true;
+    }
+
+  double c[3] = {0, 0, 0};
+  if (lig->n > 0) centroid(lig->x, lig->y, lig->z, lig->n, c);
+  cx->cx = c[0];
+  cx->cy = c[1];
+  cx->cz = c[2];
+  double o[3] = {c[0], c[1], c[2]};
+  if (rec->n > 0) centroid(rec->x, rec->y, rec->z, rec->n, o);
+  cx->ox = o[0];
+  cx->oy = o[1];
+  cx->oz = o[2];
+
+  // receptor, padded to whole tiles
+  cx->nr_pad = ((rec->n + kTile - 1) / kTile) * kTile;
+  std::vector<float4> rp32(cx->nr_pad, make_float4(1e9f, 1e9f, 1e9f, 0.f));
+  std::vector<D4> rp64(cx->nr_pad, D4{1e30, 1e30, 1e30, 0.0});
+  std::vector<int2> rmeta(cx->nr_pad, make_int2(0, 0));
+  std::vector<double> rdes(static_cast<size_t>(std::max(rec->n, 1)) * 11, 0.0);
+  double ext = 0.0;
+  for (int i = 0; i < rec->n; ++i) {
+    rp32[i] = make_float4(static_cast<float>(rec->x[i] - o[0]), static_cast<float>(rec->y[i] - o[1]),
+                          static_cast<float>(rec->z[i] - o[2]), static_cast<float>(332.0636 * rec->charge[i]));
+    rp64[i] = D4{rec->x[i], rec->y[i], rec->z[i], rec->charge[i]};
+    rmeta[i] = make_int2(rtype[i] * nt, rec->serial[i]);
+    desolv_row(rec->element[i], rec->vdw_radius[i], &rdes[static_cast<size_t>(i) * 11]);
+    ext = std::max({ext, std::fabs(rec->x[i] - o[0]), std::fabs(rec->y[i] - o[1]), std::fabs(rec->z[i] - o[2])});
+  }
+  cx->rec_extent = ext;
+  std::vector<double> lx(lig->x, lig->x + lig->n), ly(lig->y, lig->y + lig->n), lz(lig->z, lig->z + lig->n);
+  std::vector<double> lq(lig->charge, lig->charge + lig->n);
+  std::vector<int> lser(lig->serial, lig->serial + lig->n);
+  std::vector<double> ldes(static_cast<size_t>(std::max(lig->n, 1)) * 11, 0.0);
+  double rad = 0.0;
+  for (int j = 0; j < lig->n; ++j) {
+    desolv_row(lig->element[j], lig->vdw_radius[j], &ldes[static_cast<size_t>(j) * 11]);
+    const double dx = lig->x[j] - c[0], dy = lig->y[j] - c[1], dz = lig->z[j] - c[2];
+    rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+  }
+  cx->lig_radius = rad;
+  {
+    std::unordered_set<int32_t> rs(rec->serial, rec->serial + rec->n);
+    for (int j = 0; j < lig->n && !cx->serial_overlap; ++j) cx->serial_overlap = rs.count(lig->serial[j]) > 0;
+  }
+
+  // restraints: first CA with each residue number (src/restraints.rs:44-77)
+  std::vector<D4> rr;
+  std::vector<int> rl;
+  auto first_ca = [](const gd_atoms *m, int32_t res) {
+    for (int i = 0; i < m->n; ++i)
+      if (m->is_ca[i] && static_cast<int32_t>(m->resseq[i]) == res) return i;
+    return -1;
+  };
+  for (int k = 0; k < n_pairs; ++k) {
+    const int a = first_ca(rec, restraint_pairs[2 * k]);
+    const int b = first_ca(lig, restraint_pairs[2 * k + 1]);
+    if (a >= 0 && b >= 0) {
+      rr.push_back(D4{rec->x[a], rec->y[a], rec->z[a], 0.0});
+      rl.push_back(b);
+    }
+  }
+  cx->K = static_cast<int>(rl.size());
+
+  gd_status s;
+  if ((s = upload(cx, rp32, &cx->rec_pos32)) != GD_OK || (s = upload(cx, rp64, &cx->rec_pos64)) != GD_OK ||
+      (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
+      (s = upload(cx, lx, &cx->lig_x)) != GD_OK || (s = upload(cx, ly, &cx->lig_y)) != GD_OK ||
+      (s = upload(cx, lz, &cx->lig_z)) != GD_OK || (s = upload(cx, lq, &cx->lig_q)) != GD_OK ||
+      (s = upload(cx, ltype, &cx->lig_type)) != GD_OK || (s = upload(cx, lser, &cx->lig_serial)) != GD_OK ||
+      (s = upload(cx, ldes, &cx->lig_desolv)) != GD_OK || (s = upload(cx, tab32, &cx->tab32)) != GD_OK ||
+      (s = upload(cx, tab64, &cx->tab64)) != GD_OK || (s = upload(cx, rr, &cx->restr_rec)) != GD_OK ||
+      (s = upload(cx, rl, &cx->restr_lig)) != GD_OK) {
+    gd_complex_destroy(cx);
+    return s;
+  }
+  // host copies for clustering
+  cx->h_rx.assign(rec->x, rec->x + rec->n);
+  cx->h_ry.assign(rec->y, rec->y + rec->n);
+  cx->h_rz.assign(rec->z, rec->z + rec->n);
+  cx->h_lx = lx;
+  cx->h_ly = ly;
+  cx->h_lz = lz;
+  cx->h_rchain.assign(rec->chain, rec->chain + rec->n);
+  cx->h_lchain.assign(lig->chain, lig->chain + lig->n);
+  cx->h_relem.assign(rec->element, rec->element + rec->n);
+  cx->h_lelem.assign(lig->element, lig->element + lig->n);
+  cx->h_rres.assign(rec->resseq, rec->resseq + rec->n);
+  cx->h_lres.assign(lig->resseq, lig->resseq + lig->n);
+  *out = cx;
+  return GD_OK;
+}
+
+gd_status gd_complex_destroy(gd_complex *cx) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_cluster_cache(cx);
+  for (void *p : cx->allocs) cudaFree(p);
+  ctx->in_use -= std::min<uint64_t>(ctx->in_use, cx->bytes);
+  delete cx;
+  return GD_OK;
+}
+
+int32_t gd_complex_num_restraints(const gd_complex *cx) { return cx ? cx->K : -1; }
+
+gd_status gd_complex_set_weights(gd_complex *cx, const gd_weights *w) {
+  if (!cx || !w) return GD_ERR_INVALID_ARG;
+  cx->w = *w;
+  return GD_OK;
+}
+
+gd_status gd_make_frames(const double *genes, int32_t n, gd_pose_frame *frames) {
+  if (n < 0 || (n > 0 && (!genes || !frames))) return GD_ERR_INVALID_ARG;
+  const int nth = n >= 4096 ? std::max(1u, std::min(16u, std::thread::hardware_concurrency())) : 1;
+  if (nth <= 1) {
+    for (int i = 0; i < n; ++i) make_frame(genes + 6 * static_cast<size_t>(i), frames + i);
+    return GD_OK;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nth; ++t)
+    th.emplace_back([=]() {
+      for (int i = t; i < n; i += nth) make_frame(genes + 6 * static_cast<size_t>(i), frames + i);
+    });
+  for (auto &x : th) x.join();
+  return GD_OK;
+}
+
+static double max_abs_disp(const double *genes, int n) {
+  double m = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int k = 3; k < 6; ++k) m = std::max(m, std::fabs(genes[6 * static_cast<size_t>(i) + k]));
+  return m;
+}
+
+gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_precision prec, gd_pose_energy *out) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n < 0 || (n > 0 && (!genes || !out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad genes/out");
+  if (prec != GD_PREC_F32 && prec != GD_PREC_F64) return fail(ctx, GD_ERR_INVALID_ARG, "bad precision");
+  if (n == 0) return GD_OK;
+  cudaSetDevice(ctx->device);
+  const size_t fb = sizeof(gd_pose_frame) * n, ob = sizeof(gd_pose_energy) * n;
+  gd_status s = ensure_scratch(ctx, fb + ob + 256, fb + ob + 256);
+  if (s != GD_OK) return s;
+  gd_pose_frame *h_frames = static_cast<gd_pose_frame *>(ctx->h_pinned);
+  gd_pose_energy *h_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->h_pinned) + ((fb + 255) / 256) * 256);
+  gd_pose_frame *d_frames = static_cast<gd_pose_frame *>(ctx->d_scratch);
+  gd_pose_energy *d_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->d_scratch) + ((fb + 255) / 256) * 256);
+  gd_make_frames(genes, n, h_frames);
+  cudaError_t e = cudaMemcpyAsync(d_frames, h_frames, fb, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "H2D frames");
+  s = launch_score(cx, d_frames, nullptr, n, prec, d_out, ctx->stream, max_abs_disp(genes, n));
+  if (s != GD_OK) return s;
+  e = cudaMemcpyAsync(h_out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "D2H energies");
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "score kernel");
+  s = check_device_error(ctx);
+  if (s != GD_OK) return s;
+  std::memcpy(out, h_out, ob);
+  return GD_OK;
+}
+
+gd_status gd_score_frames_device(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n, gd_precision prec,
+                                 double max_displacement, gd_pose_energy *d_out, void *stream) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n < 0 || (n > 0 && (!d_frames || !d_out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad frames/out");
+  if (prec != GD_PREC_F32 && prec != GD_PREC_F64) return fail(ctx, GD_ERR_INVALID_ARG, "bad precision");
+  if (!(max_displacement >= 0.0)) return fail(ctx, GD_ERR_INVALID_ARG, "bad max_displacement");
+  cudaSetDevice(ctx->device);
+  return launch_score(cx, d_frames, nullptr, n, prec, d_out, stream ? static_cast<cudaStream_t>(stream) : ctx->stream,
+                      max_displacement);
+}
+
+gd_status gd_sync(gd_context *ctx) {
+  if (!ctx) return GD_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "device synchronize");
+  return check_device_error(ctx);
+}
+
+gd_status gd_score_models(gd_complex *cx, const double *lig_xyz, int32_t n_models, gd_precision prec,
+                          gd_pose_energy *out) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n_models < 0 || (n_models > 0 && (!lig_xyz || !out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad models/out");
+  if (prec != GD_PREC_F32 && prec != GD_PREC_F64) return fail(ctx, GD_ERR_INVALID_ARG, "bad precision");
+  if (n_models == 0) return GD_OK;
+  cudaSetDevice(ctx->device);
+  const size_t mb = sizeof(double) * 3 * static_cast<size_t>(cx->nl) * n_models;
+  const size_t ob = sizeof(gd_pose_energy) * n_models;
+  const size_t mb_al = ((mb + 255) / 256) * 256;
+  gd_status s = ensure_scratch(ctx, mb_al + ob, ob);
+  if (s != GD_OK) return s;
+  double *d_models = static_cast<double *>(ctx->d_scratch);
+  gd_pose_energy *d_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->d_scratch) + mb_al);
+  // displacement bound: furthest model coordinate from the ligand centroid
+  double m = 0.0;
+  for (size_t i = 0; i < 3 * static_cast<size_t>(cx->nl) * n_models; i += 3)
+    m = std::max({m, std::fabs(lig_xyz[i] - cx->cx), std::fabs(lig_xyz[i + 1] - cx->cy),
+                  std::fabs(lig_xyz[i + 2] - cx->cz)});
+  cudaError_t e = cudaMemcpyAsync(d_models, lig_xyz, mb, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "H2D models");
+  s = launch_score(cx, nullptr, d_models, n_models, prec, d_out, ctx->stream, m);
+  if (s != GD_OK) return s;
+  gd_pose_energy *h_out = static_cast<gd_pose_energy *>(ctx->h_pinned);
+  e = cudaMemcpyAsync(h_out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "D2H energies");
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "score kernel");
+  s = check_device_error(ctx);
+  if (s != GD_OK) return s;
+  std::memcpy(out, h_out, ob);
+  return GD_OK;
+}
+
+}  // extern "C"

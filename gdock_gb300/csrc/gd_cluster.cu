@@ -1,0 +1,694 @@
+// FCC clustering: residue contacts per pose, all-pairs fraction of common
+// contacts by popcount, neighbour graph, greedy clustering.
+//
+// Reference: src/clustering.rs:62-293.  Residues are keyed by (chain,
+// resseq) over non-hydrogen atoms of the receptor+ligand complex; a contact
+// is a pair of residues on different chains with an atom pair at distance
+// <= cutoff; FCC(i,j) = |Xi & Xj| / |Xi| (and / |Xj|), an edge i->j when
+// FCC >= c and FCC_v >= c * strictness; greedy clustering picks the element
+// with most unused neighbours (ties: lower index).
+//
+// GPU pieces:
+//   k_contacts_rl  one warp per (pose, ligand residue): transforms the residue's
+//                  atoms exactly (FP64, reference operation order), culls
+//                  receptor residues by bounding spheres, and decides atom
+//                  pairs on exact d2 against the exact threshold; each contact
+//                  is appended to the pose's list.
+//   k_fcc          64x64 tiles of pose pairs; contact bitsets over the
+//                  compacted contact universe staged in shared memory; AND +
+//                  popcount; FP64 ratios and threshold tests exactly as the
+//                  reference; edges written to an adjacency bit matrix.
+// Host pieces: key canonicalisation (smaller chain first), receptor-only and
+// ligand-only inter-chain contacts of multi-chain molecules, the universe
+// compaction, and the greedy clustering over the adjacency bit matrix.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "gd_internal.cuh"
+
+namespace gd {
+
+struct ClusterTopo {
+  // receptor heavy atoms grouped by residue (canonical ids), ligand likewise
+  int GR = 0, GL = 0;
+  std::vector<int64_t> rg_key, lg_key;  // (chain << 16) | uint16(resseq)
+  std::vector<int> rg_off, lg_off;      // atom ranges
+  std::vector<int> r_atoms, l_atoms;    // original atom indices, grouped
+  bool multi_chain_rec = false, multi_chain_lig = false;
+  std::vector<int64_t> rr_keys;         // receptor-only inter-chain contacts (pose independent)
+  double rr_cutoff = -1.0;
+  // device
+  double *d_rx = nullptr, *d_ry = nullptr, *d_rz = nullptr;
+  double *d_lx = nullptr, *d_ly = nullptr, *d_lz = nullptr;
+  int *d_rg_off = nullptr, *d_lg_off = nullptr;
+  float4 *d_rg_sph = nullptr;   // (centre - O, radius) FP32
+  D4 *d_lg_sph = nullptr;  // (centre in the positioned frame, radius)
+  uint8_t *d_rg_chain = nullptr, *d_lg_chain = nullptr;
+  std::vector<void *> allocs;
+  uint64_t bytes = 0;
+};
+
+namespace {
+
+constexpr int kMaxGroupAtoms = 64;
+
+__device__ __forceinline__ void xform(const gd_pose_frame &f, double cx, double cy, double cz, double xo, double yo,
+                                      double zo, double &X, double &Y, double &Z) {
+  const double x = __dsub_rn(xo, cx), y = __dsub_rn(yo, cy), z = __dsub_rn(zo, cz);
+  const double nx = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(x, f.ca), f.cb), __dmul_rn(y, f.m01)),
+                              __dmul_rn(z, f.m02));
+  const double ny = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(x, f.sa), f.cb), __dmul_rn(y, f.m11)),
+                              __dmul_rn(z, f.m12));
+  const double nz = __dadd_rn(__dadd_rn(__dmul_rn(-x, f.sb), __dmul_rn(__dmul_rn(y, f.cb), f.sg)),
+                              __dmul_rn(__dmul_rn(z, f.cb), f.cg));
+  X = __dadd_rn(__dadd_rn(nx, cx), f.dx);
+  Y = __dadd_rn(__dadd_rn(ny, cy), f.dy);
+  Z = __dadd_rn(__dadd_rn(nz, cz), f.dz);
+}
+
+// ((dx)^2 + (dy)^2) + (dz)^2 as src/clustering.rs:98 forms it
+__device__ __forceinline__ double d2_exact(double ax, double ay, double az, double bx, double by, double bz) {
+  const double dx = __dsub_rn(ax, bx), dy = __dsub_rn(ay, by), dz = __dsub_rn(az, bz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+struct ContactParams {
+  const double *rx, *ry, *rz;
+  const int *rg_off;
+  const float4 *rg_sph;
+  const uint8_t *rg_chain;
+  const double *lx, *ly, *lz;
+  const int *lg_off;
+  const D4 *lg_sph;
+  const uint8_t *lg_chain;
+  int GR, GL;
+  double cx, cy, cz, ox, oy, oz;
+  const gd_pose_frame *frames;
+  int n;
+  double t_le;     // contact decision: d2 <= t_le
+  float reach;     // cutoff + culling margin
+  int *counts;     // [n]
+  uint32_t *lists; // [n * cap]
+  int cap;
+};
+
+constexpr int kContactWarps = 8;
+
+__global__ void __launch_bounds__(kContactWarps * 32) k_contacts_rl(const ContactParams p) {
+  __shared__ double s_xyz[kContactWarps][3][kMaxGroupAtoms];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long items = static_cast<long long>(p.n) * p.GL;
+  for (long long it = static_cast<long long>(blockIdx.x) * kContactWarps + wib; it < items;
+       it += static_cast<long long>(gridDim.x) * kContactWarps) {
+    const int pose = static_cast<int>(it / p.GL), lg = static_cast<int>(it % p.GL);
+    const gd_pose_frame f = p.frames[pose];
+    const int a0 = p.lg_off[lg], na = p.lg_off[lg + 1] - a0;
+    const bool staged = na <= kMaxGroupAtoms;
+    if (staged) {
+      for (int a = lane; a < na; a += 32) {
+        double X, Y, Z;
+        xform(f, p.cx, p.cy, p.cz, p.lx[a0 + a], p.ly[a0 + a], p.lz[a0 + a], X, Y, Z);
+        s_xyz[wib][0][a] = X;
+        s_xyz[wib][1][a] = Y;
+        s_xyz[wib][2][a] = Z;
+      }
+    }
+    __syncwarp();
+    // culling sphere of the ligand residue after the transform
+    const D4 ls = p.lg_sph[lg];
+    double CX, CY, CZ;
+    xform(f, p.cx, p.cy, p.cz, ls.x, ls.y, ls.z, CX, CY, CZ);
+    const float lcx = static_cast<float>(CX - p.ox), lcy = static_cast<float>(CY - p.oy),
+                lcz = static_cast<float>(CZ - p.oz);
+    const float lrad = static_cast<float>(ls.w);
+    const uint8_t lchain = p.lg_chain[lg];
+    for (int rg = lane; rg < p.GR; rg += 32) {
+      if (p.rg_chain[rg] == lchain) continue;
+      const float4 rs = p.rg_sph[rg];
+      const float dx = rs.x - lcx, dy = rs.y - lcy, dz = rs.z - lcz;
+      const float lim = rs.w + lrad + p.reach;
+      if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+      bool found = false;
+      for (int b = p.rg_off[rg]; b < p.rg_off[rg + 1] && !found; ++b) {
+        const double bx = p.rx[b], by = p.ry[b], bz = p.rz[b];
+        for (int a = 0; a < na; ++a) {
+          double X, Y, Z;
+          if (staged) {
+            X = s_xyz[wib][0][a];
+            Y = s_xyz[wib][1][a];
+            Z = s_xyz[wib][2][a];
+          } else {
+            xform(f, p.cx, p.cy, p.cz, p.lx[a0 + a], p.ly[a0 + a], p.lz[a0 + a], X, Y, Z);
+          }
+          if (d2_exact(bx, by, bz, X, Y, Z) <= p.t_le) {
+            found = true;
+            break;
+          }
+        }
+      }
+      if (found) {
+        const int slot = atomicAdd(&p.counts[pose], 1);
+        if (slot < p.cap) p.lists[static_cast<size_t>(pose) * p.cap + slot] = static_cast<uint32_t>(rg) * p.GL + lg;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// pose bitsets over the compacted contact universe: n rows of W 64-bit words
+struct FccParams {
+  const unsigned long long *bits;
+  const int *sizes;
+  int n, W;
+  double c, cs;  // fcc_cutoff and fcc_cutoff * strictness
+  uint32_t *adj; // n rows of ceil(n/32) words; bit j of row i: edge i -> j
+  int adj_words;
+};
+
+constexpr int kFT = 64;   // pose tile
+constexpr int kFW = 16;   // words per staged chunk
+
+__global__ void __launch_bounds__(256) k_fcc(const FccParams p) {
+  __shared__ unsigned long long sa[kFT][kFW + 1];
+  __shared__ unsigned long long sb[kFT][kFW + 1];
+  const int i0 = blockIdx.y * kFT, j0 = blockIdx.x * kFT;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 pairs each
+  int cnt[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) cnt[a][b] = 0;
+  for (int w0 = 0; w0 < p.W; w0 += kFW) {
+    for (int e = threadIdx.x; e < kFT * kFW; e += 256) {
+      const int r = e / kFW, w = e % kFW;
+      const int gi = i0 + r, gj = j0 + r, gw = w0 + w;
+      sa[r][w] = (gi < p.n && gw < p.W) ? p.bits[static_cast<size_t>(gi) * p.W + gw] : 0ull;
+      sb[r][w] = (gj < p.n && gw < p.W) ? p.bits[static_cast<size_t>(gj) * p.W + gw] : 0ull;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int w = 0; w < kFW; ++w) {
+      unsigned long long av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = sa[ty + 16 * a][w];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = sb[tx + 16 * b][w];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cnt[a][b] += __popcll(av[a] & bv[b]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + ty + 16 * a;
+    if (i >= p.n) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + tx + 16 * b;
+      if (j >= p.n) continue;
+      const int si = p.sizes[i], sj = p.sizes[j];
+      // calculate_fcc (src/clustering.rs:122-132) and the first test of
+      // create_elements (src/clustering.rs:171); the second test for the
+      // pair (j, i) is the same condition, evaluated in that pair's thread.
+      bool edge = false;
+      if (si > 0 && sj > 0) {
+        const double common = static_cast<double>(cnt[a][b]);
+        const double fcc = common / static_cast<double>(si);
+        const double fcc_v = common / static_cast<double>(sj);
+        edge = fcc >= p.c && fcc_v >= p.cs;
+      }
+      if (edge) atomicOr(&p.adj[static_cast<size_t>(i) * p.adj_words + (j >> 5)], 1u << (j & 31));
+    }
+  }
+}
+
+__global__ void k_compact_lists(const uint32_t *lists, const int *counts, const long long *offs, int n, int cap,
+                                uint32_t *out) {
+  for (long long pose = blockIdx.x; pose < n; pose += gridDim.x) {
+    const int c = min(counts[pose], cap);
+    for (int k = threadIdx.x; k < c; k += blockDim.x) out[offs[pose] + k] = lists[pose * cap + k];
+  }
+}
+
+// host mirror of the device transform (same operation order, no fused ops)
+void xform_host(const gd_pose_frame &f, double cx, double cy, double cz, double xo, double yo, double zo, double &X,
+                double &Y, double &Z) {
+  const double x = xo - cx, y = yo - cy, z = zo - cz;
+  const double nx = x * f.ca * f.cb + y * f.m01 + z * f.m02;
+  const double ny = x * f.sa * f.cb + y * f.m11 + z * f.m12;
+  const double nz = -x * f.sb + y * f.cb * f.sg + z * f.cb * f.cg;
+  X = nx + cx + f.dx;
+  Y = ny + cy + f.dy;
+  Z = nz + cz + f.dz;
+}
+
+inline int64_t canon(int64_t ka, int64_t kb) {
+  // "cA rA cB rB" with the smaller chain first (src/clustering.rs:100-105)
+  const int64_t ca = ka >> 16, cb = kb >> 16;
+  if (ca > cb) std::swap(ka, kb);
+  return ((ka >> 16) << 48) | ((ka & 0xffff) << 32) | ((kb >> 16) << 16) | (kb & 0xffff);
+}
+
+// inter-chain contacts among the residues of one molecule (host; used for
+// multi-chain receptors once and multi-chain ligands per pose)
+void intra_contacts(const std::vector<int64_t> &gkey, const std::vector<int> &goff, const std::vector<int> &atoms,
+                    const double *x, const double *y, const double *z, double t_le, std::vector<int64_t> &out) {
+  const int G = static_cast<int>(gkey.size());
+  for (int g = 0; g < G; ++g)
+    for (int h = g + 1; h < G; ++h) {
+      if ((gkey[g] >> 16) == (gkey[h] >> 16)) continue;
+      bool found = false;
+      for (int a = goff[g]; a < goff[g + 1] && !found; ++a)
+        for (int b = goff[h]; b < goff[h + 1]; ++b) {
+          const int ia = atoms[a], ib = atoms[b];
+          const double dx = x[ia] - x[ib], dy = y[ia] - y[ib], dz = z[ia] - z[ib];
+          if (dx * dx + dy * dy + dz * dz <= t_le) {
+            found = true;
+            break;
+          }
+        }
+      if (found) out.push_back(canon(gkey[g], gkey[h]));
+    }
+}
+
+template <typename T>
+gd_status topo_upload(gd_context *ctx, ClusterTopo *t, const std::vector<T> &h, T **d) {
+  void *p = nullptr;
+  const size_t bytes = sizeof(T) * std::max<size_t>(h.size(), 1);
+  gd_status s = dev_alloc(ctx, bytes, &p);
+  if (s != GD_OK) return s;
+  t->allocs.push_back(p);
+  t->bytes += bytes;
+  *d = static_cast<T *>(p);
+  if (!h.empty()) {
+    cudaError_t e = cudaMemcpy(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy (contact topology)");
+  }
+  return GD_OK;
+}
+
+void group_atoms(const std::vector<uint8_t> &chain, const std::vector<int16_t> &res, const std::vector<uint8_t> &elem,
+                 std::vector<int64_t> &gkey, std::vector<int> &goff, std::vector<int> &atoms) {
+  std::map<int64_t, std::vector<int>> g;
+  for (size_t i = 0; i < chain.size(); ++i) {
+    if (elem[i] == GD_ELEM_H) continue;  // src/clustering.rs:67-70
+    g[(static_cast<int64_t>(chain[i]) << 16) | static_cast<uint16_t>(res[i])].push_back(static_cast<int>(i));
+  }
+  goff.assign(1, 0);
+  for (auto &kv : g) {
+    gkey.push_back(kv.first);
+    atoms.insert(atoms.end(), kv.second.begin(), kv.second.end());
+    goff.push_back(static_cast<int>(atoms.size()));
+  }
+}
+
+gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
+  gd_context *ctx = cx->ctx;
+  ClusterTopo *t = new ClusterTopo();
+  group_atoms(cx->h_rchain, cx->h_rres, cx->h_relem, t->rg_key, t->rg_off, t->r_atoms);
+  group_atoms(cx->h_lchain, cx->h_lres, cx->h_lelem, t->lg_key, t->lg_off, t->l_atoms);
+  t->GR = static_cast<int>(t->rg_key.size());
+  t->GL = static_cast<int>(t->lg_key.size());
+  for (int g = 1; g < t->GR; ++g) t->multi_chain_rec |= (t->rg_key[g] >> 16) != (t->rg_key[0] >> 16);
+  for (int g = 1; g < t->GL; ++g) t->multi_chain_lig |= (t->lg_key[g] >> 16) != (t->lg_key[0] >> 16);
+  std::vector<double> rx, ry, rz, lx, ly, lz;
+  for (int i : t->r_atoms) {
+    rx.push_back(cx->h_rx[i]);
+    ry.push_back(cx->h_ry[i]);
+    rz.push_back(cx->h_rz[i]);
+  }
+  for (int i : t->l_atoms) {
+    lx.push_back(cx->h_lx[i]);
+    ly.push_back(cx->h_ly[i]);
+    lz.push_back(cx->h_lz[i]);
+  }
+  std::vector<float4> rsph(t->GR);
+  std::vector<uint8_t> rch(t->GR), lch(t->GL);
+  for (int g = 0; g < t->GR; ++g) {
+    double c[3] = {0, 0, 0};
+    const int a0 = t->rg_off[g], a1 = t->rg_off[g + 1];
+    for (int a = a0; a < a1; ++a) {
+      c[0] += rx[a];
+      c[1] += ry[a];
+      c[2] += rz[a];
+    }
+    for (double &v : c) v /= (a1 - a0);
+    double r = 0;
+    for (int a = a0; a < a1; ++a)
+      r = std::max(r, std::sqrt((rx[a] - c[0]) * (rx[a] - c[0]) + (ry[a] - c[1]) * (ry[a] - c[1]) +
+                                (rz[a] - c[2]) * (rz[a] - c[2])));
+    rsph[g] = make_float4(static_cast<float>(c[0] - cx->ox), static_cast<float>(c[1] - cx->oy),
+                          static_cast<float>(c[2] - cx->oz), static_cast<float>(r * (1 + 1e-6) + 1e-3));
+    rch[g] = static_cast<uint8_t>(t->rg_key[g] >> 16);
+  }
+  std::vector<D4> lsph(t->GL);
+  for (int g = 0; g < t->GL; ++g) {
+    double c[3] = {0, 0, 0};
+    const int a0 = t->lg_off[g], a1 = t->lg_off[g + 1];
+    for (int a = a0; a < a1; ++a) {
+      c[0] += lx[a];
+      c[1] += ly[a];
+      c[2] += lz[a];
+    }
+    for (double &v : c) v /= (a1 - a0);
+    double r = 0;
+    for (int a = a0; a < a1; ++a)
+      r = std::max(r, std::sqrt((lx[a] - c[0]) * (lx[a] - c[0]) + (ly[a] - c[1]) * (ly[a] - c[1]) +
+                                (lz[a] - c[2]) * (lz[a] - c[2])));
+    lsph[g] = D4{c[0], c[1], c[2], r * (1 + 1e-6) + 1e-3};
+    lch[g] = static_cast<uint8_t>(t->lg_key[g] >> 16);
+  }
+  gd_status s;
+  if ((s = topo_upload(ctx, t, rx, &t->d_rx)) != GD_OK || (s = topo_upload(ctx, t, ry, &t->d_ry)) != GD_OK ||
+      (s = topo_upload(ctx, t, rz, &t->d_rz)) != GD_OK || (s = topo_upload(ctx, t, lx, &t->d_lx)) != GD_OK ||
+      (s = topo_upload(ctx, t, ly, &t->d_ly)) != GD_OK || (s = topo_upload(ctx, t, lz, &t->d_lz)) != GD_OK ||
+      (s = topo_upload(ctx, t, t->rg_off, &t->d_rg_off)) != GD_OK ||
+      (s = topo_upload(ctx, t, t->lg_off, &t->d_lg_off)) != GD_OK || (s = topo_upload(ctx, t, rsph, &t->d_rg_sph)) != GD_OK ||
+      (s = topo_upload(ctx, t, lsph, &t->d_lg_sph)) != GD_OK || (s = topo_upload(ctx, t, rch, &t->d_rg_chain)) != GD_OK ||
+      (s = topo_upload(ctx, t, lch, &t->d_lg_chain)) != GD_OK) {
+    for (void *p : t->allocs) cudaFree(p);
+    ctx->in_use -= std::min<uint64_t>(ctx->in_use, t->bytes);
+    delete t;
+    return s;
+  }
+  *out = t;
+  return GD_OK;
+}
+
+gd_status get_topo(gd_complex *cx, ClusterTopo **t) {
+  if (!cx->cluster_cache) {
+    ClusterTopo *nt = nullptr;
+    gd_status s = build_topo(cx, &nt);
+    if (s != GD_OK) return s;
+    cx->cluster_cache = nt;
+  }
+  *t = static_cast<ClusterTopo *>(cx->cluster_cache);
+  return GD_OK;
+}
+
+// Greedy clustering of cluster_elements (src/clustering.rs:183-254) over an
+// adjacency bit matrix, then the size filter (src/clustering.rs:289-292).
+int greedy_clusters(const std::vector<uint32_t> &adj, int n, int words, int min_size, int32_t *centers, int32_t *sizes,
+                    int32_t *members) {
+  std::vector<int> count(n, 0);
+  std::vector<std::vector<int>> in_edges(n);  // e with edge e -> m
+  for (int e = 0; e < n; ++e)
+    for (int w = 0; w < words; ++w) {
+      uint32_t v = adj[static_cast<size_t>(e) * words + w];
+      count[e] += __builtin_popcount(v);
+      while (v) {
+        const int b = __builtin_ctz(v);
+        v &= v - 1;
+        in_edges[w * 32 + b].push_back(e);
+      }
+    }
+  std::vector<char> used(n, 0);
+  struct Cl { int center, first, size; };
+  std::vector<Cl> cls;
+  std::vector<int> mem;
+  auto mark = [&](int m) {
+    used[m] = 1;
+    for (int e : in_edges[m]) --count[e];
+  };
+  for (;;) {
+    int center = -1, best = -1;
+    for (int e = 0; e < n; ++e)
+      if (!used[e] && count[e] > best) {
+        best = count[e];
+        center = e;
+      }
+    if (center < 0) break;
+    const int first = static_cast<int>(mem.size());
+    mem.push_back(center);
+    std::vector<int> nb;
+    for (int w = 0; w < words; ++w) {
+      uint32_t v = adj[static_cast<size_t>(center) * words + w];
+      while (v) {
+        const int b = __builtin_ctz(v);
+        v &= v - 1;
+        const int m = w * 32 + b;
+        if (m != center && !used[m]) nb.push_back(m);
+      }
+    }
+    for (int m : nb) {
+      mem.push_back(m);
+      mark(m);
+    }
+    mark(center);
+    std::sort(mem.begin() + first, mem.end());
+    cls.push_back(Cl{center, first, static_cast<int>(mem.size()) - first});
+  }
+  std::stable_sort(cls.begin(), cls.end(), [](const Cl &a, const Cl &b) { return a.size > b.size; });
+  int k = 0, mo = 0;
+  for (const Cl &c : cls) {
+    if (c.size < min_size) continue;
+    centers[k] = c.center;
+    sizes[k] = c.size;
+    std::memcpy(members + mo, mem.data() + c.first, sizeof(int32_t) * c.size);
+    mo += c.size;
+    ++k;
+  }
+  return k;
+}
+
+}  // namespace
+
+void free_cluster_cache(gd_complex *cx) {
+  if (!cx->cluster_cache) return;
+  ClusterTopo *t = static_cast<ClusterTopo *>(cx->cluster_cache);
+  for (void *p : t->allocs) cudaFree(p);
+  cx->ctx->in_use -= std::min<uint64_t>(cx->ctx->in_use, t->bytes);
+  delete t;
+  cx->cluster_cache = nullptr;
+}
+
+// Contact keys of n poses (sorted per pose) into a host vector + offsets.
+gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double cutoff, std::vector<int64_t> &keys,
+                             std::vector<int64_t> &offs) {
+  gd_context *ctx = cx->ctx;
+  ClusterTopo *t = nullptr;
+  gd_status s = get_topo(cx, &t);
+  if (s != GD_OK) return s;
+  const Thresholds thr = make_thresholds(cutoff);
+  if (t->multi_chain_rec && t->rr_cutoff != cutoff) {
+    t->rr_keys.clear();
+    intra_contacts(t->rg_key, t->rg_off, t->r_atoms, cx->h_rx.data(), cx->h_ry.data(), cx->h_rz.data(),
+                   thr.contact_le, t->rr_keys);
+    t->rr_cutoff = cutoff;
+  }
+  std::vector<gd_pose_frame> frames(n);
+  gd_make_frames(genes, n, frames.data());
+  const long long pairs = static_cast<long long>(t->GR) * t->GL;
+  int cap = static_cast<int>(std::min<long long>(std::max<long long>(pairs, 1), 2048));
+  std::vector<int> counts(n);
+  std::vector<uint32_t> flat;
+  std::vector<long long> loffs(n + 1, 0);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const size_t fb = sizeof(gd_pose_frame) * n, cb = sizeof(int) * n,
+                 lb = sizeof(uint32_t) * static_cast<size_t>(n) * cap, ob = sizeof(long long) * (n + 1);
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    s = ensure_scratch(ctx, al(fb) + al(cb) + al(lb) + al(ob) + al(lb), 0);
+    if (s != GD_OK) return s;
+    char *base = static_cast<char *>(ctx->d_scratch);
+    gd_pose_frame *d_frames = reinterpret_cast<gd_pose_frame *>(base);
+    int *d_counts = reinterpret_cast<int *>(base + al(fb));
+    uint32_t *d_lists = reinterpret_cast<uint32_t *>(base + al(fb) + al(cb));
+    long long *d_offs = reinterpret_cast<long long *>(base + al(fb) + al(cb) + al(lb));
+    uint32_t *d_flat = reinterpret_cast<uint32_t *>(base + al(fb) + al(cb) + al(lb) + al(ob));
+    cudaError_t e = cudaMemcpyAsync(d_frames, frames.data(), fb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_counts, 0, cb, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "contacts setup");
+    if (pairs > 0) {
+      ContactParams p{};
+      p.rx = t->d_rx;
+      p.ry = t->d_ry;
+      p.rz = t->d_rz;
+      p.rg_off = t->d_rg_off;
+      p.rg_sph = t->d_rg_sph;
+      p.rg_chain = t->d_rg_chain;
+      p.lx = t->d_lx;
+      p.ly = t->d_ly;
+      p.lz = t->d_lz;
+      p.lg_off = t->d_lg_off;
+      p.lg_sph = t->d_lg_sph;
+      p.lg_chain = t->d_lg_chain;
+      p.GR = t->GR;
+      p.GL = t->GL;
+      p.cx = cx->cx;
+      p.cy = cx->cy;
+      p.cz = cx->cz;
+      p.ox = cx->ox;
+      p.oy = cx->oy;
+      p.oz = cx->oz;
+      p.frames = d_frames;
+      p.n = n;
+      p.t_le = thr.contact_le;
+      p.reach = static_cast<float>(cutoff) + 0.05f;
+      p.counts = d_counts;
+      p.lists = d_lists;
+      p.cap = cap;
+      const long long items = static_cast<long long>(n) * t->GL;
+      const int grid = static_cast<int>(std::min<long long>((items + kContactWarps - 1) / kContactWarps,
+                                                            static_cast<long long>(ctx->sm_count) * 16));
+      k_contacts_rl<<<grid, kContactWarps * 32, 0, ctx->stream>>>(p);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "contacts kernel launch");
+    }
+    e = cudaMemcpyAsync(counts.data(), d_counts, cb, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "contacts kernel");
+    const int maxc = n > 0 ? *std::max_element(counts.begin(), counts.end()) : 0;
+    if (maxc > cap) {  // rerun once with room for the largest pose
+      cap = maxc;
+      continue;
+    }
+    for (int i = 0; i < n; ++i) loffs[i + 1] = loffs[i] + counts[i];
+    flat.resize(static_cast<size_t>(loffs[n]));
+    if (loffs[n] > 0) {
+      e = cudaMemcpyAsync(d_offs, loffs.data(), ob, cudaMemcpyHostToDevice, ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "H2D offsets");
+      k_compact_lists<<<std::min(n, ctx->sm_count * 8), 128, 0, ctx->stream>>>(d_lists, d_counts, d_offs, n, cap,
+                                                                                 d_flat);
+      e = cudaMemcpyAsync(flat.data(), d_flat, sizeof(uint32_t) * flat.size(), cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "contact list gather");
+    }
+    break;
+  }
+  keys.clear();
+  offs.assign(1, 0);
+  std::vector<int64_t> pk;
+  std::vector<double> tx, ty, tz;
+  for (int i = 0; i < n; ++i) {
+    pk.clear();
+    for (long long k = loffs[i]; k < loffs[i + 1]; ++k) {
+      const uint32_t v = flat[k];
+      pk.push_back(canon(t->rg_key[v / t->GL], t->lg_key[v % t->GL]));
+    }
+    pk.insert(pk.end(), t->rr_keys.begin(), t->rr_keys.end());
+    if (t->multi_chain_lig) {
+      tx.resize(cx->nl);
+      ty.resize(cx->nl);
+      tz.resize(cx->nl);
+      for (int a : t->l_atoms)
+        xform_host(frames[i], cx->cx, cx->cy, cx->cz, cx->h_lx[a], cx->h_ly[a], cx->h_lz[a], tx[a], ty[a], tz[a]);
+      intra_contacts(t->lg_key, t->lg_off, t->l_atoms, tx.data(), ty.data(), tz.data(), thr.contact_le, pk);
+    }
+    std::sort(pk.begin(), pk.end());
+    pk.erase(std::unique(pk.begin(), pk.end()), pk.end());
+    keys.insert(keys.end(), pk.begin(), pk.end());
+    offs.push_back(static_cast<int64_t>(keys.size()));
+  }
+  return GD_OK;
+}
+
+gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs, int n, const gd_cluster_cfg &cfg,
+                       int32_t *n_clusters, int32_t *centers, int32_t *sizes, int32_t *members) {
+  *n_clusters = 0;
+  if (n <= 0) return GD_OK;
+  // compacted contact universe
+  std::vector<int64_t> uni(keys, keys + offs[n]);
+  std::sort(uni.begin(), uni.end());
+  uni.erase(std::unique(uni.begin(), uni.end()), uni.end());
+  const int W = std::max(1, static_cast<int>((uni.size() + 63) / 64));
+  std::vector<unsigned long long> bits(static_cast<size_t>(n) * W, 0ull);
+  std::vector<int> sz(n);
+  for (int i = 0; i < n; ++i) {
+    sz[i] = static_cast<int>(offs[i + 1] - offs[i]);
+    for (int64_t k = offs[i]; k < offs[i + 1]; ++k) {
+      const size_t u = std::lower_bound(uni.begin(), uni.end(), keys[k]) - uni.begin();
+      bits[static_cast<size_t>(i) * W + u / 64] |= 1ull << (u % 64);
+    }
+  }
+  const int aw = (n + 31) / 32;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t bb = sizeof(unsigned long long) * bits.size(), sb = sizeof(int) * n,
+               ab = sizeof(uint32_t) * static_cast<size_t>(n) * aw;
+  gd_status s = ensure_scratch(ctx, al(bb) + al(sb) + al(ab), 0);
+  if (s != GD_OK) return s;
+  char *base = static_cast<char *>(ctx->d_scratch);
+  unsigned long long *d_bits = reinterpret_cast<unsigned long long *>(base);
+  int *d_sz = reinterpret_cast<int *>(base + al(bb));
+  uint32_t *d_adj = reinterpret_cast<uint32_t *>(base + al(bb) + al(sb));
+  cudaError_t e = cudaMemcpyAsync(d_bits, bits.data(), bb, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_sz, sz.data(), sb, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_adj, 0, ab, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC setup");
+  FccParams p{};
+  p.bits = d_bits;
+  p.sizes = d_sz;
+  p.n = n;
+  p.W = W;
+  p.c = cfg.fcc_cutoff;
+  p.cs = cfg.fcc_cutoff * cfg.strictness;
+  p.adj = d_adj;
+  p.adj_words = aw;
+  dim3 grid((n + kFT - 1) / kFT, (n + kFT - 1) / kFT);
+  k_fcc<<<grid, 256, 0, ctx->stream>>>(p);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel launch");
+  std::vector<uint32_t> adj(static_cast<size_t>(n) * aw);
+  e = cudaMemcpyAsync(adj.data(), d_adj, ab, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel");
+  *n_clusters = greedy_clusters(adj, n, aw, cfg.min_cluster_size, centers, sizes, members);
+  return GD_OK;
+}
+
+}  // namespace gd
+
+using namespace gd;
+
+static gd_cluster_cfg default_cfg() { return gd_cluster_cfg{5.0, 0.60, 0.75, 4}; }
+
+extern "C" {
+
+gd_status gd_pose_contacts(gd_complex *cx, const double *genes, int32_t n, int64_t *keys, int64_t cap,
+                           int64_t *offsets) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n < 0 || (n > 0 && (!genes || !offsets)) || cap < 0 || (cap > 0 && !keys))
+    return fail(ctx, GD_ERR_INVALID_ARG, "bad genes/keys/offsets");
+  cudaSetDevice(ctx->device);
+  std::vector<int64_t> k, o;
+  gd_status s = pose_contacts_host(cx, genes, n, 5.0, k, o);
+  if (s != GD_OK) return s;
+  std::memcpy(offsets, o.data(), sizeof(int64_t) * (n + 1));
+  if (static_cast<int64_t>(k.size()) > cap) return fail(ctx, GD_ERR_CAPACITY, "contact key buffer too small");
+  if (!k.empty()) std::memcpy(keys, k.data(), sizeof(int64_t) * k.size());
+  return GD_OK;
+}
+
+gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cluster_cfg *cfg, int32_t *n_clusters,
+                     int32_t *centers, int32_t *sizes, int32_t *members) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n < 0 || (n > 0 && (!genes || !centers || !sizes || !members)) || !n_clusters)
+    return fail(ctx, GD_ERR_INVALID_ARG, "bad cluster arguments");
+  const gd_cluster_cfg c = cfg ? *cfg : default_cfg();
+  *n_clusters = 0;
+  if (n == 0) return GD_OK;  // cluster_structures on no structures
+  cudaSetDevice(ctx->device);
+  std::vector<int64_t> k, o;
+  gd_status s = pose_contacts_host(cx, genes, n, c.contact_distance, k, o);
+  if (s != GD_OK) return s;
+  return cluster_sets(ctx, k.data(), o.data(), n, c, n_clusters, centers, sizes, members);
+}
+
+gd_status gd_cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offsets, int32_t n,
+                          const gd_cluster_cfg *cfg, int32_t *n_clusters, int32_t *centers, int32_t *sizes,
+                          int32_t *members) {
+  if (!ctx) return GD_ERR_INVALID_ARG;
+  if (n < 0 || (n > 0 && (!offsets || !centers || !sizes || !members)) || !n_clusters)
+    return fail(ctx, GD_ERR_INVALID_ARG, "bad cluster arguments");
+  if (n > 0 && offsets[n] > 0 && !keys) return fail(ctx, GD_ERR_INVALID_ARG, "null keys");
+  cudaSetDevice(ctx->device);
+  const gd_cluster_cfg c = cfg ? *cfg : default_cfg();
+  return cluster_sets(ctx, keys, offsets, n, c, n_clusters, centers, sizes, members);
+}
+
+}  // extern "C"

@@ -1,0 +1,145 @@
+// Internal declarations shared by the gdock_gb300 CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "gdock_gb300.h"
+
+namespace gd {
+
+// Four doubles, 32-byte aligned (one receptor atom of the FP64 tiles).
+struct alignas(32) D4 {
+  double x, y, z, w;
+};
+
+// Receptor atoms per tile staged in shared memory by one bulk (TMA) copy.
+constexpr int kTile = 256;
+constexpr int kStages = 3;
+// Upper bounds of a device-side wait before it gives up: polls and wall time.
+constexpr uint32_t kSpinLimit = 1u << 26;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+// Distinct (epsilon, Rmin/2) atom types a complex may hold.
+constexpr int kMaxTypes = 64;
+
+// device error codes written to the context's error word
+enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };
+
+// Per-pair parameters of one type pair, FP32 form: R6 = (Rmin_i + Rmin_j)^6,
+// eps = sqrt(eps_i eps_j), m2eps = -2 eps.
+struct TypePair32 { float r6, eps, m2eps, pad; };
+// FP64 form: R6, alpha*R6 (alpha = 0.5), eps.
+struct TypePair64 { double r6, hr6, eps, pad; };
+
+// Exact FP64 thresholds on the squared distance d2 = dx*dx + dy*dy + dz*dz,
+// so that d2-comparisons make the same decisions as the reference's
+// comparisons of sqrt(d2) against its cutoffs.
+struct Thresholds {
+  double vdw_lt;    // dist < 12   <=>  d2 < vdw_lt
+  double elec_gt;   // dist > 1    <=>  d2 > elec_gt
+  double elec_lt;   // dist < 15   <=>  d2 < elec_lt
+  double desolv_lt; // dist < 8    <=>  d2 < desolv_lt
+  double contact_le;// dist <= 5   <=>  d2 <= contact_le (per call's cutoff)
+};
+
+struct ScoreParams {
+  // receptor, sorted by atom type, padded to a multiple of kTile
+  const float4 *rec_pos32;  // (x-O, y-O, z-O, 332.0636*q) FP32
+  const D4 *rec_pos64; // (x, y, z, q) FP64
+  const int2 *rec_meta;     // (type, serial)
+  const double *rec_desolv; // [nr * 11] energy contribution at burial count 0..10
+  int nr, n_tiles;
+  // ligand, original order
+  const double *lig_x, *lig_y, *lig_z;
+  const double *lig_q;
+  const int *lig_type, *lig_serial;
+  const double *lig_desolv; // [nl * 11]
+  int nl;
+  double cx, cy, cz;        // rotation centre (centroid of the positioned ligand)
+  double ox, oy, oz;        // FP32 coordinate origin
+  const TypePair32 *tab32;
+  const TypePair64 *tab64;
+  int nt;
+  int need_clamp;           // some |eps_ij| may exceed the [-50, 500] clamp
+  // restraints: receptor CA coordinates and ligand CA atom index
+  const D4 *restr_rec; // (x, y, z, -) of the receptor CA
+  const int *restr_lig;     // ligand CA index
+  int K;
+  double wv, we, wd, wa;
+  Thresholds thr;
+  float guard_v, guard_e, guard_d; // FP32 guard half-widths on d2
+  // poses
+  const gd_pose_frame *frames;
+  const double *models;     // explicit ligand coordinates (n x nl x 3) or null
+  int n_poses;
+  gd_pose_energy *out;
+  int *err;
+};
+
+}  // namespace gd
+
+using gd::D4;
+
+struct gd_context {
+  int device = 0;
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  int *d_err = nullptr;
+  std::string last_error;
+  // grow-only scratch: device and pinned host staging
+  void *d_scratch = nullptr;
+  size_t d_scratch_bytes = 0;
+  void *h_pinned = nullptr;
+  size_t h_pinned_bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+struct gd_complex {
+  gd_context *ctx = nullptr;
+  int nr = 0, nl = 0, nr_pad = 0, nt = 0, K = 0;
+  gd_weights w{};
+  bool serial_overlap = false;
+  bool need_clamp = false;
+  double cx = 0, cy = 0, cz = 0, ox = 0, oy = 0, oz = 0;
+  double rec_extent = 0;  // max |x - O| over receptor atoms (inf-norm)
+  double lig_radius = 0;  // max |x - c| over ligand atoms (Euclidean)
+  // device arrays
+  float4 *rec_pos32 = nullptr;
+  D4 *rec_pos64 = nullptr;
+  int2 *rec_meta = nullptr;
+  double *rec_desolv = nullptr;
+  double *lig_x = nullptr, *lig_y = nullptr, *lig_z = nullptr, *lig_q = nullptr;
+  int *lig_type = nullptr, *lig_serial = nullptr;
+  double *lig_desolv = nullptr;
+  gd::TypePair32 *tab32 = nullptr;
+  gd::TypePair64 *tab64 = nullptr;
+  D4 *restr_rec = nullptr;
+  int *restr_lig = nullptr;
+  std::vector<void *> allocs;
+  uint64_t bytes = 0;
+  // host copies used by clustering
+  std::vector<double> h_rx, h_ry, h_rz, h_lx, h_ly, h_lz;
+  std::vector<uint8_t> h_rchain, h_lchain, h_relem, h_lelem;
+  std::vector<int16_t> h_rres, h_lres;
+  void *cluster_cache = nullptr;  // gd::ClusterTopo*, built on first use
+};
+
+namespace gd {
+gd_status fail(gd_context *ctx, gd_status s, const std::string &msg);
+gd_status cuda_fail(gd_context *ctx, cudaError_t e, const char *what);
+gd_status dev_alloc(gd_context *ctx, uint64_t bytes, void **p);
+void dev_free(gd_context *ctx, void *p, uint64_t bytes);
+gd_status ensure_scratch(gd_context *ctx, size_t dev_bytes, size_t pinned_bytes);
+gd_status check_device_error(gd_context *ctx);
+Thresholds make_thresholds(double contact_cutoff);
+void make_frame(const double *g, gd_pose_frame *f);
+void guard_widths(const gd_complex *cx, double max_disp, float *gv, float *ge, float *gd);
+gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const double *d_models, int n,
+                       gd_precision prec, gd_pose_energy *d_out, cudaStream_t stream, double max_disp);
+void free_cluster_cache(gd_complex *cx);
+}  // namespace gd

@@ -1,0 +1,170 @@
+/* gdock_gb300 — GB300 (sm_103a) engine for gdock's population fitness
+ * evaluation and FCC clustering, behind a plain C ABI.
+ *
+ * The entry points replace these functions of the gdock (Rust) reference, so
+ * that its host code can call one GPU through a thin FFI crate:
+ *
+ *   Population::eval_fitness          src/population.rs:48-61   -> gd_score_poses
+ *   Chromosome::fitness (one pose)    src/chromosome.rs:85-128  -> gd_score_poses (n = 1)
+ *   Chromosome::apply_genes           src/chromosome.rs:79-83   -> inside gd_score_poses / gd_cluster
+ *   fitness::{vdw,elec,desolv}_energy src/fitness.rs:86-184,284-302 -> gd_score_models
+ *   fitness::air_energy, satisfaction_ratio src/fitness.rs:205-267 -> gd_score_* (air, restraint_penalty)
+ *   commands::score::score loop       src/commands/score.rs:32-79 -> gd_score_models
+ *   restraints::create_restraints_from_pairs src/restraints.rs:44-77 -> gd_complex_create
+ *   clustering::calculate_contacts    src/clustering.rs:62-115  -> gd_pose_contacts
+ *   clustering::cluster_structures    src/clustering.rs:265-293 -> gd_cluster
+ *
+ * Conventions: every call returns a gd_status; nothing throws or aborts
+ * across the ABI.  The library copies all inputs; callers keep ownership of
+ * their buffers.  A context belongs to one host thread at a time (serialise
+ * externally to share one).  All floating-point outputs are FP64.
+ */
+#ifndef GDOCK_GB300_H
+#define GDOCK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GD_ABI_VERSION 1
+
+typedef enum gd_status {
+  GD_OK = 0,
+  GD_ERR_INVALID_ARG = 1, /* bad pointer, size or value */
+  GD_ERR_OOM = 2,         /* device allocation failed or HBM budget exceeded */
+  GD_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  GD_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  GD_ERR_CAPACITY = 5,    /* an output buffer is too small */
+  GD_ERR_STATE = 6        /* call not valid in the object's current state */
+} gd_status;
+
+typedef enum gd_precision {
+  GD_PREC_F64 = 0, /* plain form: FP64 throughout (the correctness reference) */
+  GD_PREC_F32 = 1  /* FP32 pair terms, compensated partials, FP64 per-pose reduction,
+                      FP64 recheck of every pair near a cutoff */
+} gd_precision;
+
+/* element classes, from the trimmed PDB element column (src/structure.rs:241-256) */
+enum { GD_ELEM_OTHER = 0, GD_ELEM_H = 1, GD_ELEM_C = 2, GD_ELEM_N = 3, GD_ELEM_O = 4, GD_ELEM_S = 5 };
+
+/* One molecule as structure-of-arrays; the fields of gdock's Atom that the
+ * scoring and clustering read (src/structure.rs:27-49). */
+typedef struct gd_atoms {
+  int32_t n;
+  const double *x, *y, *z;
+  const double *epsilon;    /* toppar epsilon (kcal/mol, <= 0 for OPLS types) */
+  const double *rmin2;      /* toppar Rmin/2 (A) */
+  const double *charge;     /* partial charge (e) */
+  const double *vdw_radius; /* radius by element (A) */
+  const int32_t *serial;    /* PDB serial: equal receptor/ligand serials skip the vdW pair */
+  const int16_t *resseq;    /* residue number */
+  const uint8_t *chain;     /* chain id character */
+  const uint8_t *element;   /* GD_ELEM_* */
+  const uint8_t *is_ca;     /* 1 when the atom name is "CA" */
+} gd_atoms;
+
+/* EnergyWeights, src/constants.rs:28-56 (defaults 0.4, 0.05, 3.4, 1.0) */
+typedef struct gd_weights { double vdw, elec, desolv, air; } gd_weights;
+
+/* The six fields Chromosome::fitness writes (src/chromosome.rs:111-127). */
+typedef struct gd_pose_energy {
+  double fitness, vdw, elec, desolv, air, restraint_penalty;
+} gd_pose_energy;
+
+/* ClusteringConfig, src/clustering.rs:14-35 (defaults 5.0, 0.60, 0.75, 4) */
+typedef struct gd_cluster_cfg {
+  double contact_distance, fcc_cutoff, strictness;
+  int32_t min_cluster_size;
+} gd_cluster_cfg;
+
+/* Rotation/translation of one pose as the host precomputes it from its genes
+ * (cosines and sines of the three angles with the host's libm, the composite
+ * matrix entries in the reference's operation order, the displacement). */
+typedef struct gd_pose_frame {
+  double ca, sa, cb, sb, cg, sg;
+  double m01, m02, m11, m12;
+  double dx, dy, dz;
+  double pad[3];
+} gd_pose_frame;
+
+typedef struct gd_context gd_context;
+typedef struct gd_complex gd_complex;
+
+int32_t gd_abi_version(void);
+const char *gd_status_string(gd_status s);
+
+/* Context on one CUDA device.  hbm_budget_bytes = 0 means "no limit beyond
+ * the device's memory". */
+gd_status gd_context_create(int32_t device, uint64_t hbm_budget_bytes, gd_context **out);
+gd_status gd_context_destroy(gd_context *ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char *gd_last_error(const gd_context *ctx);
+/* Bytes of device memory the context's objects hold. */
+uint64_t gd_context_bytes_in_use(const gd_context *ctx);
+
+/* Upload a receptor and a ligand that is already centred on the receptor
+ * (utils::position_ligand, src/utils.rs:77-95).  restraint_pairs holds
+ * n_pairs (receptor resseq, ligand resseq) pairs; as in
+ * create_restraints_from_pairs, a pair is kept when both molecules contain
+ * an atom named CA with that residue number (the first such atom is used)
+ * and dropped otherwise.  w may be NULL for the default weights. */
+gd_status gd_complex_create(gd_context *ctx, const gd_atoms *receptor, const gd_atoms *ligand,
+                            const int32_t *restraint_pairs, int32_t n_pairs, const gd_weights *w,
+                            gd_complex **out);
+gd_status gd_complex_destroy(gd_complex *cx);
+/* number of restraints kept at upload */
+int32_t gd_complex_num_restraints(const gd_complex *cx);
+gd_status gd_complex_set_weights(gd_complex *cx, const gd_weights *w);
+
+/* Host-side frame of each pose from its 6 genes (alpha, beta, gamma, dx, dy, dz). */
+gd_status gd_make_frames(const double *genes, int32_t n, gd_pose_frame *frames);
+
+/* Population::eval_fitness: score n poses given as genes (n x 6, host
+ * memory); writes n gd_pose_energy records (host memory).  Synchronous. */
+gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_precision prec,
+                         gd_pose_energy *out);
+
+/* Same, on device-resident frames and outputs, enqueued on `stream`
+ * (a cudaStream_t; NULL = the context's stream).  max_displacement bounds
+ * |dx|, |dy|, |dz| over the frames (it sizes the FP32 guard bands).  Returns
+ * after the launch; errors of the device run are reported by gd_sync. */
+gd_status gd_score_frames_device(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n,
+                                 gd_precision prec, double max_displacement, gd_pose_energy *d_out,
+                                 void *stream);
+/* Wait for the context's work and report any device-side error. */
+gd_status gd_sync(gd_context *ctx);
+
+/* The `score` command: score n_models ligand coordinate sets as given
+ * (lig_xyz: n_models x n_lig x 3, host memory); no transform is applied. */
+gd_status gd_score_models(gd_complex *cx, const double *lig_xyz, int32_t n_models, gd_precision prec,
+                          gd_pose_energy *out);
+
+/* calculate_contacts for the complex receptor + ligand moved by each pose's
+ * genes.  Contact keys are (chainA<<48)|(uint16(resA)<<32)|(chainB<<16)|uint16(resB)
+ * with chainA < chainB, ascending per pose.  offsets has n+1 entries; keys
+ * holds up to cap keys.  GD_ERR_CAPACITY (with offsets[n] = keys needed) if
+ * cap is too small. */
+gd_status gd_pose_contacts(gd_complex *cx, const double *genes, int32_t n, int64_t *keys, int64_t cap,
+                           int64_t *offsets);
+
+/* cluster_structures over the n poses given as genes: contacts, all-pairs
+ * FCC, neighbour graph and greedy clustering, clusters of at least
+ * min_cluster_size in gdock's output order.  centers/sizes hold up to n
+ * entries, members up to n; *n_clusters receives the count. cfg may be NULL
+ * for the defaults. */
+gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cluster_cfg *cfg,
+                     int32_t *n_clusters, int32_t *centers, int32_t *sizes, int32_t *members);
+
+/* cluster_structures on caller-supplied contact sets (keys/offsets as
+ * gd_pose_contacts writes them); the FCC and neighbour graph run on the GPU. */
+gd_status gd_cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offsets, int32_t n,
+                          const gd_cluster_cfg *cfg, int32_t *n_clusters, int32_t *centers,
+                          int32_t *sizes, int32_t *members);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GDOCK_GB300_H */

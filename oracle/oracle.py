@@ -1,0 +1,213 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+load this module to check or time against; the GPU product path never
+imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+_LIB_PATH = _HERE / "_build" / "libgd_oracle.so"
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    src = [_HERE / "gd_oracle.c", _HERE / "gd_oracle.h"]
+    if force or not _LIB_PATH.exists() or any(s.stat().st_mtime > _LIB_PATH.stat().st_mtime for s in src):
+        subprocess.run(["make", "-s", "-C", str(_HERE)], check=True)
+    return _LIB_PATH
+
+
+class OrcMol(C.Structure):
+    _fields_ = [("n", C.c_int32),
+                ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("epsilon", C.c_void_p), ("rmin2", C.c_void_p), ("charge", C.c_void_p),
+                ("vdw_radius", C.c_void_p), ("serial", C.c_void_p), ("resseq", C.c_void_p),
+                ("chain", C.c_void_p), ("element", C.c_void_p), ("is_ca", C.c_void_p)]
+
+
+class OrcWeights(C.Structure):
+    _fields_ = [("vdw", C.c_double), ("elec", C.c_double), ("desolv", C.c_double), ("air", C.c_double)]
+
+
+ENERGY_FIELDS = ("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")
+DEFAULT_WEIGHTS = (0.4, 0.05, 3.4, 1.0)  # src/constants.rs:22-25
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(_LIB_PATH))
+        P = C.POINTER
+        _lib.orc_vdw_energy.restype = C.c_double
+        _lib.orc_elec_energy.restype = C.c_double
+        _lib.orc_desolv_energy.restype = C.c_double
+        _lib.orc_air_energy.restype = C.c_double
+        _lib.orc_satisfaction_ratio.restype = C.c_double
+        _lib.orc_count_restraints.restype = C.c_int32
+        _lib.orc_contacts.restype = C.c_int32
+        _lib.orc_pose_contacts.restype = C.c_int32
+        _lib.orc_cluster.restype = C.c_int32
+        for f in ("orc_vdw_energy", "orc_elec_energy", "orc_desolv_energy"):
+            getattr(_lib, f).argtypes = [P(OrcMol), P(OrcMol)]
+    return _lib
+
+
+class _Packed:
+    """Keeps the numpy buffers of an OrcMol alive."""
+
+    def __init__(self, mol, x=None, y=None, z=None):
+        c = np.ascontiguousarray
+        self.bufs = [
+            c(mol.x if x is None else x, dtype=np.float64), c(mol.y if y is None else y, dtype=np.float64),
+            c(mol.z if z is None else z, dtype=np.float64), c(mol.epsilon, dtype=np.float64),
+            c(mol.rmin2, dtype=np.float64), c(mol.charge, dtype=np.float64),
+            c(mol.vdw_radius, dtype=np.float64), c(mol.serial, dtype=np.int32),
+            c(mol.resseq, dtype=np.int16), c(mol.chain_code, dtype=np.uint8),
+            c(mol.element_class, dtype=np.uint8), c(mol.is_ca, dtype=np.uint8)]
+        self.s = OrcMol(len(mol), *[b.ctypes.data for b in self.bufs])
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+
+def pack(mol, x=None, y=None, z=None) -> _Packed:
+    return _Packed(mol, x, y, z)
+
+
+def _pairs(pairs):
+    a = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+    return a, a.shape[0]
+
+
+def vdw_energy(rec, lig) -> float:
+    return lib().orc_vdw_energy(pack(rec).ref, pack(lig).ref)
+
+
+def elec_energy(rec, lig) -> float:
+    return lib().orc_elec_energy(pack(rec).ref, pack(lig).ref)
+
+
+def desolv_energy(rec, lig) -> float:
+    return lib().orc_desolv_energy(pack(rec).ref, pack(lig).ref)
+
+
+def air_energy(pairs, rec, lig) -> float:
+    a, k = _pairs(pairs)
+    return lib().orc_air_energy(a.ctypes.data_as(C.c_void_p), C.c_int32(k), pack(rec).ref, pack(lig).ref)
+
+
+def satisfaction_ratio(pairs, rec, lig) -> float:
+    a, k = _pairs(pairs)
+    return lib().orc_satisfaction_ratio(a.ctypes.data_as(C.c_void_p), C.c_int32(k), pack(rec).ref, pack(lig).ref)
+
+
+def kept_restraints(pairs, rec, lig) -> np.ndarray:
+    a, k = _pairs(pairs)
+    out = np.zeros_like(a)
+    m = lib().orc_count_restraints(a.ctypes.data_as(C.c_void_p), C.c_int32(k), pack(rec).ref,
+                                   pack(lig).ref, out.ctypes.data_as(C.c_void_p))
+    return out[:m].copy()
+
+
+def apply_genes(lig, genes):
+    n = len(lig)
+    x, y, z = np.empty(n), np.empty(n), np.empty(n)
+    g = np.ascontiguousarray(genes, dtype=np.float64)
+    lib().orc_apply_genes(pack(lig).ref, g.ctypes.data_as(C.c_void_p), x.ctypes.data_as(C.c_void_p),
+                          y.ctypes.data_as(C.c_void_p), z.ctypes.data_as(C.c_void_p))
+    return x, y, z
+
+
+def score_poses(rec, lig, pairs, genes, weights=DEFAULT_WEIGHTS, nthreads=None) -> np.ndarray:
+    """(n, 6) array of fitness, vdw, elec, desolv, air, restraint_penalty.
+    `pairs` are the restraint residue pairs; the ones whose CAs are missing
+    are dropped first, as gdock does when it builds restraints."""
+    kept = kept_restraints(pairs, rec, lig)
+    g = np.ascontiguousarray(np.asarray(genes, dtype=np.float64).reshape(-1, 6))
+    out = np.zeros((g.shape[0], 6))
+    w = OrcWeights(*weights)
+    pr, pl = pack(rec), pack(lig)
+    lib().orc_score_poses(pr.ref, pl.ref, kept.ctypes.data_as(C.c_void_p), C.c_int32(kept.shape[0]),
+                          C.byref(w), g.ctypes.data_as(C.c_void_p), C.c_int32(g.shape[0]),
+                          out.ctypes.data_as(C.c_void_p), C.c_int32(nthreads or os.cpu_count() or 1))
+    return out
+
+
+def score_models(rec, lig, pairs, xyz, weights=DEFAULT_WEIGHTS, nthreads=None) -> np.ndarray:
+    kept = kept_restraints(pairs, rec, lig)
+    x = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1, len(lig), 3))
+    out = np.zeros((x.shape[0], 6))
+    w = OrcWeights(*weights)
+    pr, pl = pack(rec), pack(lig)
+    lib().orc_score_models(pr.ref, pl.ref, kept.ctypes.data_as(C.c_void_p), C.c_int32(kept.shape[0]),
+                           C.byref(w), x.ctypes.data_as(C.c_void_p), C.c_int32(x.shape[0]),
+                           out.ctypes.data_as(C.c_void_p), C.c_int32(nthreads or os.cpu_count() or 1))
+    return out
+
+
+def contacts(mol, cutoff=5.0) -> np.ndarray:
+    cap = 1 << 20
+    keys = np.zeros(cap, dtype=np.int64)
+    n = lib().orc_contacts(pack(mol).ref, C.c_double(cutoff), keys.ctypes.data_as(C.c_void_p), C.c_int32(cap))
+    return keys[: min(n, cap)].copy()
+
+
+def pose_contacts(rec, lig, genes, cutoff=5.0) -> np.ndarray:
+    cap = 1 << 20
+    keys = np.zeros(cap, dtype=np.int64)
+    g = np.ascontiguousarray(genes, dtype=np.float64)
+    n = lib().orc_pose_contacts(pack(rec).ref, pack(lig).ref, g.ctypes.data_as(C.c_void_p), C.c_double(cutoff),
+                                keys.ctypes.data_as(C.c_void_p), C.c_int32(cap))
+    return keys[: min(n, cap)].copy()
+
+
+def _flatten_sets(sets):
+    offs = np.zeros(len(sets) + 1, dtype=np.int64)
+    for i, s in enumerate(sets):
+        offs[i + 1] = offs[i] + len(s)
+    keys = np.concatenate([np.asarray(s, dtype=np.int64) for s in sets]) if sets else np.zeros(0, np.int64)
+    return np.ascontiguousarray(keys), offs
+
+
+def pairwise_fcc(sets):
+    keys, offs = _flatten_sets(sets)
+    n = len(sets)
+    f, fv = np.zeros((n, n)), np.zeros((n, n))
+    lib().orc_pairwise_fcc(keys.ctypes.data_as(C.c_void_p), offs.ctypes.data_as(C.c_void_p), C.c_int32(n),
+                           f.ctypes.data_as(C.c_void_p), fv.ctypes.data_as(C.c_void_p))
+    return f, fv
+
+
+def cluster(sets, fcc_cutoff=0.60, strictness=0.75, min_size=4):
+    """[(center, [members...]), ...] in gdock's output order."""
+    keys, offs = _flatten_sets(sets)
+    n = len(sets)
+    centers = np.zeros(max(n, 1), np.int32)
+    sizes = np.zeros(max(n, 1), np.int32)
+    members = np.zeros(max(n, 1), np.int32)
+    k = lib().orc_cluster(keys.ctypes.data_as(C.c_void_p), offs.ctypes.data_as(C.c_void_p), C.c_int32(n),
+                          C.c_double(fcc_cutoff), C.c_double(strictness), C.c_int32(min_size),
+                          centers.ctypes.data_as(C.c_void_p), sizes.ctypes.data_as(C.c_void_p),
+                          members.ctypes.data_as(C.c_void_p))
+    out, m = [], 0
+    for c in range(k):
+        out.append((int(centers[c]), members[m:m + sizes[c]].tolist()))
+        m += int(sizes[c])
+    return out
+
+
+def contact_key(chain_a: str, res_a: int, chain_b: str, res_b: int) -> int:
+    """Key of the contact string "cA rA cB rB" (smaller chain first)."""
+    if chain_a > chain_b:
+        chain_a, res_a, chain_b, res_b = chain_b, res_b, chain_a, res_a
+    return (ord(chain_a) << 48) | ((res_a & 0xffff) << 32) | (ord(chain_b) << 16) | (res_b & 0xffff)

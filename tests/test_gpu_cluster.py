@@ -1,0 +1,85 @@
+"""GPU parity of contacts and FCC clustering: bit-exact against the oracle."""
+import numpy as np
+import pytest
+
+import gdock_gb300 as gd
+from gdock_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    c = synth.make_complex(50, 76, 6, seed=21)
+    lig = gd.position_ligand(c.receptor, c.ligand)
+    return c, lig
+
+
+def near_genes(rng, n, spread):
+    """Poses around a few seeds so that clusters exist."""
+    base = synth.random_genes(rng, 4, max_displacement=12.0)
+    g = base[rng.integers(0, 4, n)].copy()
+    g[:, :3] = np.mod(g[:, :3] + rng.normal(0, 0.05 * spread, (n, 3)), 2 * np.pi)
+    g[:, 3:] += rng.normal(0, 0.5 * spread, (n, 3))
+    return g
+
+
+def test_contacts_bit_exact(oracle, setup):
+    c, lig = setup
+    genes = near_genes(np.random.default_rng(0), 24, 1.0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    got = cx.pose_contacts(genes)
+    n_nonempty = 0
+    for g, keys in zip(genes, got):
+        ref = oracle.pose_contacts(c.receptor, lig, g)
+        np.testing.assert_array_equal(keys, ref)
+        n_nonempty += len(ref) > 0
+    assert n_nonempty > 0
+
+
+def test_cluster_matches_oracle(oracle, setup):
+    c, lig = setup
+    rng = np.random.default_rng(1)
+    genes = near_genes(rng, 60, 1.0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    sets = [oracle.pose_contacts(c.receptor, lig, g) for g in genes]
+    want = oracle.cluster(sets)
+    got = cx.cluster(genes)
+    assert [(r.center_idx, r.members) for r in got] == want
+    assert all(r.size == len(r.members) for r in got)
+    got2 = gd.cluster_sets(sets)
+    assert [(r.center_idx, r.members) for r in got2] == want
+    for ms in (1, 2):
+        cfg = gd.ClusteringConfig(min_cluster_size=ms)
+        assert [(r.center_idx, r.members) for r in gd.cluster_sets(sets, cfg)] == oracle.cluster(sets, min_size=ms)
+
+
+def test_cluster_edge_cases(oracle):
+    assert gd.cluster_sets([]) == []
+    s = [np.array([], np.int64)] * 5
+    got = gd.cluster_sets(s, gd.ClusteringConfig(min_cluster_size=1))
+    assert [(r.center_idx, r.members) for r in got] == oracle.cluster(s, min_size=1)
+    rng = np.random.default_rng(3)
+    for trial in range(5):
+        n = int(rng.integers(2, 140))
+        u = rng.integers(1, 200)
+        sets = [np.unique(rng.integers(0, u, int(rng.integers(0, 30))).astype(np.int64)) for _ in range(n)]
+        for ms in (1, 4):
+            cfg = gd.ClusteringConfig(min_cluster_size=ms)
+            got = [(r.center_idx, r.members) for r in gd.cluster_sets(sets, cfg)]
+            assert got == oracle.cluster(sets, min_size=ms), trial
+
+
+def test_multichain_receptor_contacts(oracle):
+    """A receptor of two chains: receptor-only inter-chain contacts count in
+    every pose's set (src/clustering.rs:82-91)."""
+    c = synth.make_complex(40, 30, 3, seed=8)
+    rec = c.receptor
+    chains = ["A" if i < len(rec) // 2 else "C" for i in range(len(rec))]
+    rec = gd.Molecule(**{**rec.__dict__, "chainid": chains})
+    lig = gd.position_ligand(rec, c.ligand)
+    genes = near_genes(np.random.default_rng(4), 8, 1.0)
+    cx = gd.Complex(rec, lig, c.restraint_pairs)
+    got = cx.pose_contacts(genes)
+    for g, keys in zip(genes, got):
+        np.testing.assert_array_equal(keys, oracle.pose_contacts(rec, lig, g))

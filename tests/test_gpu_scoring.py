@@ -1,0 +1,173 @@
+"""GPU parity of the scoring path through the C ABI against the CPU oracle.
+
+FP64 (plain) form: every energy component within 1e-12 relative of the
+oracle (summation order is the only difference); AIR and the restraint
+penalty bit-identical (same restraint order, same arithmetic).
+FP32 form: every component within 1e-5 relative, measured against
+max(|E_ref|, 1 kcal/mol).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import gdock_gb300 as gd
+from gdock_gb300 import synth
+from conftest import make_mol, tatom
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("vdw", "elec", "desolv", "air", "restraint_penalty", "fitness")
+F64_TOL = 1e-12
+F32_TOL = 1e-5
+
+
+def rel_err(got, ref, floor=1.0):
+    return np.abs(got - ref) / np.maximum(np.abs(ref), floor)
+
+
+def check(e, ref, tol, exact_air=True):
+    for k, name in enumerate(("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")):
+        r = ref[:, k]
+        g = e[name]
+        if name in ("air", "restraint_penalty") and exact_air:
+            np.testing.assert_array_equal(g, r, err_msg=name)
+        else:
+            err = rel_err(g, r)
+            assert err.max() <= tol, (name, err.max(), int(err.argmax()))
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return synth.make_complex(50, 76, 6, seed=11)
+
+
+def positioned(c):
+    return gd.position_ligand(c.receptor, c.ligand)
+
+
+@pytest.mark.parametrize("prec,tol", [(gd.GD_PREC_F64, F64_TOL), (gd.GD_PREC_F32, F32_TOL)])
+def test_c1_random_genes(oracle, c1, prec, tol):
+    lig = positioned(c1)
+    rng = np.random.default_rng(5)
+    genes = synth.random_genes(rng, 48)
+    genes[:16, 3:] = rng.uniform(-8, 8, size=(16, 3))  # overlapping poses: many pairs in range
+    cx = gd.Complex(c1.receptor, lig, c1.restraint_pairs)
+    assert cx.num_restraints == len(oracle.kept_restraints(c1.restraint_pairs, c1.receptor, lig))
+    e = cx.score_poses(genes, prec)
+    ref = oracle.score_poses(c1.receptor, lig, c1.restraint_pairs, genes)
+    check(e, ref, tol)
+
+
+@pytest.mark.parametrize("nr_res,nl_res", [(3, 2), (33, 35), (40, 70), (150, 140)])
+def test_sizes_around_tiles(oracle, nr_res, nl_res):
+    """Receptor/ligand sizes around the 256-atom tile and slot boundaries."""
+    c = synth.make_complex(nr_res, nl_res, 4, seed=nr_res * 7 + nl_res)
+    lig = positioned(c)
+    rng = np.random.default_rng(nr_res)
+    genes = synth.random_genes(rng, 9, max_displacement=6.0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    ref = oracle.score_poses(c.receptor, lig, c.restraint_pairs, genes)
+    check(cx.score_poses(genes, gd.GD_PREC_F64), ref, F64_TOL)
+    check(cx.score_poses(genes, gd.GD_PREC_F32), ref, F32_TOL)
+
+
+def test_single_pose_and_no_restraints(oracle, c1):
+    lig = positioned(c1)
+    genes = np.array([[0.1, 0.2, 0.3, 1.0, -1.0, 2.0]])
+    cx = gd.Complex(c1.receptor, lig, [])
+    assert cx.num_restraints == 0
+    e = cx.score_poses(genes)
+    ref = oracle.score_poses(c1.receptor, lig, [], genes)
+    check(e, ref, F64_TOL)
+    assert e["air"][0] == 0.0 and e["restraint_penalty"][0] == 0.0
+
+
+def test_missing_restraint_pairs_dropped(oracle, c1):
+    lig = positioned(c1)
+    pairs = list(c1.restraint_pairs) + [(9999, 1), (1, 9999)]
+    cx = gd.Complex(c1.receptor, lig, pairs)
+    assert cx.num_restraints == len(c1.restraint_pairs)
+
+
+def test_equal_serials_skip_vdw_pairs(oracle):
+    """Receptor and ligand numbered from 1: equal serials drop the vdW pair
+    (src/fitness.rs:92)."""
+    c = synth.make_complex(30, 25, 3, seed=3, overlap_serials=True)
+    lig = positioned(c)
+    genes = synth.random_genes(np.random.default_rng(1), 12, max_displacement=5.0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    ref = oracle.score_poses(c.receptor, lig, c.restraint_pairs, genes)
+    check(cx.score_poses(genes, gd.GD_PREC_F64), ref, F64_TOL)
+    check(cx.score_poses(genes, gd.GD_PREC_F32), ref, F32_TOL)
+
+
+def test_models_path_matches_oracle(oracle, c1):
+    """score command: explicit model coordinates, no transform."""
+    lig = positioned(c1)
+    genes = synth.random_genes(np.random.default_rng(2), 5, max_displacement=10.0)
+    xyz = np.stack([np.stack(oracle.apply_genes(lig, g), axis=1) for g in genes])
+    cx = gd.Complex(c1.receptor, c1.ligand, c1.restraint_pairs)
+    ref = oracle.score_models(c1.receptor, c1.ligand, c1.restraint_pairs, xyz)
+    check(cx.score_models(xyz, gd.GD_PREC_F64), ref, F64_TOL)
+    check(cx.score_models(xyz, gd.GD_PREC_F32), ref, F32_TOL)
+    # genes path and models path agree
+    cx2 = gd.Complex(c1.receptor, lig, c1.restraint_pairs)
+    a = cx2.score_poses(genes)
+    ref2 = oracle.score_poses(c1.receptor, lig, c1.restraint_pairs, genes)
+    check(a, ref2, F64_TOL)
+
+
+def test_reference_kats_through_abi(oracle):
+    """The reference's fitness unit tests, re-run through the GPU path."""
+    r = make_mol([tatom(0, 0, 0, charge=1.0)])
+    l = make_mol([tatom(5, 0, 0, charge=-1.0, serial=2)])
+    assert gd.elec_energy(r, l) == pytest.approx(332.0636 * -1.0 / 25.0, rel=1e-15)
+    l20 = make_mol([tatom(20, 0, 0, serial=2)])
+    assert gd.vdw_energy(r, l20) == 0.0
+    l1 = make_mol([tatom(1, 0, 0)])  # serial 1 == receptor serial: skipped
+    assert gd.vdw_energy(r, l1) == 0.0
+    ring = make_mol([tatom(3 * math.cos(i), 3 * math.sin(i), 0, "C", serial=10 + i) for i in range(15)])
+    assert gd.desolv_energy(make_mol([tatom(0, 0, 0, "C")]), ring) < 0
+    assert gd.desolv_energy(make_mol([tatom(0, 0, 0, "O")]), ring) > 0
+    ca_r = make_mol([tatom(0, 0, 0, name="CA", resseq=1)])
+    for d, air, sat in ((5.0, 0.0, 1.0), (7.0, 0.0, 1.0), (15.0, 640.0, 0.0)):
+        ca_l = make_mol([tatom(d, 0, 0, name="CA", resseq=10, serial=2)])
+        assert gd.air_energy([(1, 10)], ca_r, ca_l) == air
+        assert gd.satisfaction_ratio([(1, 10)], ca_r, ca_l) == pytest.approx(sat)
+
+
+def test_cutoff_boundaries_f32_matches_f64(oracle):
+    """Ligand atoms placed within a few ulps of every cutoff: the FP32 form's
+    guard band must reproduce the exact FP64 decisions."""
+    rec = make_mol([tatom(0, 0, 0, "O", charge=0.8, serial=1)])
+    pts = []
+    for c in (1.0, 8.0, 12.0, 15.0):
+        for k in (-3, -1, 0, 1, 3):
+            d = c * (1 + k * 2.0 ** -52)
+            u = np.array([1.0, 2.0, 2.0]) / 3.0
+            pts.append(tatom(*(d * u), "N", charge=-0.7, serial=100 + len(pts)))
+    lig = make_mol(pts)
+    cx = gd.Complex(rec, lig, [])
+    xyz = lig.xyz()[None]
+    e64 = cx.score_models(xyz, gd.GD_PREC_F64)
+    e32 = cx.score_models(xyz, gd.GD_PREC_F32)
+    ref = oracle.score_models(rec, lig, [], xyz)
+    check(e64, ref, F64_TOL)
+    for name in ("vdw", "elec", "desolv"):
+        assert abs(e32[name][0] - e64[name][0]) <= 1e-5 * max(1.0, abs(e64[name][0])), name
+
+
+def test_deterministic(c1):
+    lig = positioned(c1)
+    genes = synth.random_genes(np.random.default_rng(9), 20)
+    cx = gd.Complex(c1.receptor, lig, c1.restraint_pairs)
+    for prec in (gd.GD_PREC_F64, gd.GD_PREC_F32):
+        a, b = cx.score_poses(genes, prec), cx.score_poses(genes, prec)
+        assert a.tobytes() == b.tobytes()
+
+
+def test_invalid_arguments_raise(c1):
+    cx = gd.Complex(c1.receptor, positioned(c1), c1.restraint_pairs)
+    with pytest.raises(gd.GdError):
+        cx.score_poses(np.zeros((1, 6)), 7)

@@ -38,11 +38,11 @@ FLOP_PER_PAIR = 37  # convention: d2 8, LJ 18, Coulomb 4, cutoff tests 5, burial
 METRIC = "poses/s (batched FP32 scoring, single complex)"
 
 
-def workload():
+def workload(n_poses=N_POSES):
     from gdock_gb300 import position_ligand, synth
     c = synth.make_complex(N_REC_RES, N_LIG_RES, N_RESTRAINTS, seed=SEED)
     lig = position_ligand(c.receptor, c.ligand)
-    genes = synth.quaternion_genes(np.random.default_rng(SEED + 1), N_POSES, half_box=20.0)
+    genes = synth.quaternion_genes(np.random.default_rng(SEED + 1), n_poses, half_box=20.0)
     return c, lig, genes
 
 
@@ -166,7 +166,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-sample", type=int, default=2048)
     ap.add_argument("--cpu-sample", type=int, default=32)
+    ap.add_argument("--poses", type=int, default=N_POSES,
+                    help="poses per step (smaller only for profiling captures)")
     args = ap.parse_args()
+    NP = args.poses
     if args.impl == "reference":
         return run_reference(args)
 
@@ -182,18 +185,23 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
 
-    c, lig, genes = workload()
+    c, lig, genes = workload(NP)
     ctx = gd.Context(local)
     cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
     lib = ctx.lib
     frames_h = _lib.make_frames(genes)
     frames = torch.from_numpy(frames_h).to(f"cuda:{local}")
-    out = torch.zeros((N_POSES, 6), dtype=torch.float64, device=f"cuda:{local}")
+    out = torch.zeros((NP, 6), dtype=torch.float64, device=f"cuda:{local}")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MiB > L2
     max_disp = float(np.abs(genes[:, 3:]).max())
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library launches on it and the events are
+    # recorded on it (the legacy default stream's handle is 0, which the ABI
+    # reads as "the context's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
 
-    def launch(prec, n=N_POSES):
+    def launch(prec, n=NP):
         ctx.check(lib.gd_score_frames_device(cx.h, frames.data_ptr(), n, prec, max_disp, out.data_ptr(),
                                              stream.cuda_stream))
 
@@ -206,6 +214,7 @@ def main():
         dist.barrier()
     times = []
     with Clocks(local) as clk:
+        time.sleep(0.5)  # let the sampler start
         for _ in range(args.steps):
             flush.fill_(1.0)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -222,7 +231,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_step = float(t.item())
         dist.barrier()
-    value = world * N_POSES / t_step
+    value = world * NP / t_step
     res32 = out.cpu().numpy().copy()
 
     # --- end to end through the C ABI with host buffers (e2e) ---
@@ -232,10 +241,10 @@ def main():
         t0 = time.perf_counter()
         cx.score_poses(genes, gd.GD_PREC_F32)
         e2e_t.append(time.perf_counter() - t0)
-    e2e = N_POSES / float(np.median(e2e_t))
+    e2e = NP / float(np.median(e2e_t))
 
     # --- plain FP64 form on a sample; FP32-vs-FP64 error per component ---
-    ns = min(args.fp64_sample, N_POSES)
+    ns = min(args.fp64_sample, NP)
     launch(gd.GD_PREC_F64, ns)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -256,16 +265,16 @@ def main():
     if rank == 0:
         pairs = len(c.receptor) * len(lig)
         peaks = measured_peaks(torch)
-        achieved = FLOP_PER_PAIR * pairs * N_POSES / t_step / 1e12
+        achieved = FLOP_PER_PAIR * pairs * NP / t_step / 1e12
         cpu_threads = os.cpu_count() or 1
         cpu_v = cpu_sample(c, lig, genes, args.cpu_sample, cpu_threads)
         line = {
             "metric": METRIC, "value": value, "unit": "poses/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(c, lig, {"parallelism": "replicas" if world > 1 else "single GPU"}),
-            "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": N_POSES * _lib.POSE_FRAME_BYTES,
-                    "d2h_bytes_per_step": N_POSES * 48},
+            "config": config(c, lig, {"parallelism": "replicas" if world > 1 else "single GPU", "poses_per_step": NP}),
+            "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES,
+                    "d2h_bytes_per_step": NP * 48},
             "gpu_launches": args.steps,
             "pair_evals_per_s": pairs * value,
             "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,

@@ -147,6 +147,7 @@ class PackedAtoms:
                      c(mol.vdw_radius, np.float64), c(mol.serial, np.int32), c(mol.resseq, np.int16),
                      c(mol.chain_code, np.uint8), c(mol.element_class, np.uint8), c(mol.is_ca, np.uint8)]
         self.s = GdAtoms(len(mol), *[ptr(b) for b in self.bufs])
+        self.s._keep = self.bufs  # the struct holds raw addresses: keep the buffers alive with it
 
 
 def make_frames(genes: np.ndarray) -> np.ndarray:

@@ -74,6 +74,9 @@ class _Packed:
             c(mol.resseq, dtype=np.int16), c(mol.chain_code, dtype=np.uint8),
             c(mol.element_class, dtype=np.uint8), c(mol.is_ca, dtype=np.uint8)]
         self.s = OrcMol(len(mol), *[b.ctypes.data for b in self.bufs])
+        # the struct holds raw addresses only: tie the buffers' lifetime to it,
+        # so that a byref() of a temporary keeps them alive for the call
+        self.s._keep = self.bufs
 
     @property
     def ref(self):

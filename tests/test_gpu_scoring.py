@@ -167,7 +167,26 @@ def test_deterministic(c1):
         assert a.tobytes() == b.tobytes()
 
 
-def test_invalid_arguments_raise(c1):
+def test_invalid_arguments_rejected(c1):
+    from gdock_gb300 import _lib
     cx = gd.Complex(c1.receptor, positioned(c1), c1.restraint_pairs)
-    with pytest.raises(gd.GdError):
-        cx.score_poses(np.zeros((1, 6)), 7)
+    g = np.zeros((1, 6))
+    out = np.zeros(1, dtype=_lib.POSE_ENERGY_DTYPE)
+    lib = cx.lib
+    assert lib.gd_score_poses(cx.h, _lib.ptr(g), 1, 7, _lib.ptr(out)) == _lib.GD_ERR_INVALID_ARG
+    assert lib.gd_score_poses(cx.h, None, 1, 0, _lib.ptr(out)) == _lib.GD_ERR_INVALID_ARG
+    assert lib.gd_score_poses(cx.h, _lib.ptr(g), -1, 0, _lib.ptr(out)) == _lib.GD_ERR_INVALID_ARG
+    assert lib.gd_score_poses(None, _lib.ptr(g), 1, 0, _lib.ptr(out)) == _lib.GD_ERR_INVALID_ARG
+    assert b"precision" in lib.gd_last_error(cx.ctx.h) or lib.gd_last_error(cx.ctx.h)
+    with pytest.raises(ValueError):
+        cx.score_poses(g, 7)
+    # nothing was corrupted: a valid call still works
+    assert np.isfinite(cx.score_poses(g)["fitness"]).all()
+
+
+def test_hbm_budget_enforced(c1):
+    ctx = gd.Context(0, hbm_budget_bytes=1 << 16)
+    with pytest.raises(gd.GdError) as ei:
+        gd.Complex(c1.receptor, positioned(c1), c1.restraint_pairs, ctx=ctx)
+    assert ei.value.status == 2  # GD_ERR_OOM
+    ctx.close()

@@ -93,7 +93,7 @@ class Clocks:
             sm = [float(r[0]) for r in rows]
             mx = [float(r[1]) for r in rows]
             names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-            reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[3 + k]})
+            reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k].strip() == "Active"})
             return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": reasons,
                     "samples": len(rows), "power_w_max": max(float(r[2]) for r in rows)}
         except Exception as e:  # noqa: BLE001

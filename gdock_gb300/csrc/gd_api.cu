@@ -363,6 +363,27 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
     ext = std::max({ext, std::fabs(rec->x[i] - o[0]), std::fabs(rec->y[i] - o[1]), std::fabs(rec->z[i] - o[2])});
   }
   cx->rec_extent = ext;
+  // culling spheres of 8-atom receptor blocks: centre (FP32 frame) and
+  // radius + 15 A + margin, so that a block further than this from a ligand
+  // atom holds no pair with any nonzero term
+  std::vector<float4> rsph(std::max(cx->nr_pad / 8, 1), make_float4(0.f, 0.f, 0.f, -1.0e30f));
+  for (int b = 0; b * 8 < rec->n; ++b) {
+    const int a0 = b * 8, a1 = std::min(rec->n, a0 + 8);
+    double c3[3] = {0, 0, 0};
+    for (int i = a0; i < a1; ++i) {
+      c3[0] += rec->x[i] - o[0];
+      c3[1] += rec->y[i] - o[1];
+      c3[2] += rec->z[i] - o[2];
+    }
+    for (double &v : c3) v /= (a1 - a0);
+    double r = 0.0;
+    for (int i = a0; i < a1; ++i) {
+      const double dx = rec->x[i] - o[0] - c3[0], dy = rec->y[i] - o[1] - c3[1], dz = rec->z[i] - o[2] - c3[2];
+      r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    rsph[b] = make_float4(static_cast<float>(c3[0]), static_cast<float>(c3[1]), static_cast<float>(c3[2]),
+                          static_cast<float>(r * 1.0001 + 0.01 + 15.0));
+  }
   std::vector<double> lx(lig->x, lig->x + lig->n), ly(lig->y, lig->y + lig->n), lz(lig->z, lig->z + lig->n);
   std::vector<double> lq(lig->charge, lig->charge + lig->n);
   std::vector<int> lser(lig->serial, lig->serial + lig->n);
@@ -399,7 +420,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
 
   gd_status s;
   if ((s = upload(cx, rp32, &cx->rec_pos32)) != GD_OK || (s = upload(cx, rp64, &cx->rec_pos64)) != GD_OK ||
-      (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
+      (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rsph, &cx->rec_sph32)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
       (s = upload(cx, lx, &cx->lig_x)) != GD_OK || (s = upload(cx, ly, &cx->lig_y)) != GD_OK ||
       (s = upload(cx, lz, &cx->lig_z)) != GD_OK || (s = upload(cx, lq, &cx->lig_q)) != GD_OK ||
       (s = upload(cx, ltype, &cx->lig_type)) != GD_OK || (s = upload(cx, lser, &cx->lig_serial)) != GD_OK ||

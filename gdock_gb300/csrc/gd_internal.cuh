@@ -49,6 +49,7 @@ struct ScoreParams {
   // receptor, sorted by atom type, padded to a multiple of kTile
   const float4 *rec_pos32;  // (x-O, y-O, z-O, 332.0636*q) FP32
   const D4 *rec_pos64; // (x, y, z, q) FP64
+  const float4 *rec_sph32;  // per 8-atom block: (centre - O, radius + 15 A reach)
   const int2 *rec_meta;     // (type, serial)
   const double *rec_desolv; // [nr * 11] energy contribution at burial count 0..10
   int nr, n_tiles;
@@ -111,6 +112,7 @@ struct gd_complex {
   // device arrays
   float4 *rec_pos32 = nullptr;
   D4 *rec_pos64 = nullptr;
+  float4 *rec_sph32 = nullptr;
   int2 *rec_meta = nullptr;
   double *rec_desolv = nullptr;
   double *lig_x = nullptr, *lig_y = nullptr, *lig_z = nullptr, *lig_q = nullptr;

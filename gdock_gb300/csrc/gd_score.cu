@@ -252,43 +252,115 @@ __device__ void drain(uint64_t *s_full, long long q_from, long long q_to) {
 
 // --------------------------------------------------------------- FP32 ----
 
+// Receptor atoms per culling block: each block of kBlk consecutive receptor
+// atoms carries a bounding sphere; a (block, warp slot) pair is skipped when
+// the spheres are further apart than the 15 A electrostatics cutoff (every
+// term and count is exactly zero there, and no pair is near a cutoff).
+constexpr int kBlk = 8;
+
+struct SmemLayout32 {
+  size_t pos, meta, sph, bars, tab, frame, red, blob, rcnt, total;
+};
+
+__host__ __device__ inline SmemLayout32 smem_layout32(int nt, int nr, int nthreads) {
+  SmemLayout32 L;
+  size_t o = 0;
+  auto al = [&](size_t a) { o = (o + a - 1) / a * a; };
+  L.pos = o;
+  o += sizeof(float4) * kStages * kTile;
+  L.meta = o;
+  o += sizeof(int2) * kStages * kTile;
+  L.sph = o;
+  o += sizeof(float4) * kStages * (kTile / kBlk);
+  L.bars = o;
+  o += 8 * 8;
+  al(16);
+  L.tab = o;
+  o += sizeof(float2) * nt * nt;
+  al(16);
+  L.frame = o;
+  o += sizeof(gd_pose_frame);
+  al(16);
+  L.red = o;
+  o += sizeof(double) * 3 * (nthreads / 32);
+  al(16);
+  L.blob = o;
+  o += sizeof(float4) * 8 * (nthreads / 32);
+  al(16);
+  L.rcnt = o;
+  o += sizeof(uint32_t) * nr;
+  al(16);
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ void issue_tile32(long long q, int n_tiles, const ScoreParams &p, float4 *s_pos,
+                                             int2 *s_meta, float4 *s_sph, uint64_t *s_full) {
+  const int st = static_cast<int>(q % kStages);
+  const int t = static_cast<int>(q % n_tiles);
+  constexpr uint32_t kBytes = kTile * (sizeof(float4) + sizeof(int2)) + (kTile / kBlk) * sizeof(float4);
+  mbar_expect_tx(&s_full[st], kBytes);
+  bulk_g2s(&s_pos[st * kTile], p.rec_pos32 + static_cast<size_t>(t) * kTile, kTile * sizeof(float4), &s_full[st]);
+  bulk_g2s(&s_meta[st * kTile], p.rec_meta + static_cast<size_t>(t) * kTile, kTile * sizeof(int2), &s_full[st]);
+  bulk_g2s(&s_sph[st * (kTile / kBlk)], p.rec_sph32 + static_cast<size_t>(t) * (kTile / kBlk),
+           (kTile / kBlk) * sizeof(float4), &s_full[st]);
+}
+
+// acc += v when |t| < lim (predicated add, no select)
+__device__ __forceinline__ void add_if_abs_lt(float &acc, float t, float lim, float v) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, %2;\n\t@p add.f32 %0, %0, %3;\n\t}" : "+f"(acc)
+      : "f"(fabsf(t)), "f"(lim), "f"(v));
+}
+// both counters += 1 when d2 < 64
+__device__ __forceinline__ void count_if_lt64(int &a, int &b, float d2) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %2, 0f42800000;\n\t@p add.s32 %0, %0, 1;\n\t@p add.s32 %1, %1, 1;\n\t}"
+      : "+r"(a), "+r"(b)
+      : "f"(d2));
+}
+
 template <bool SERIAL, bool CLAMP>
 struct Pair32 {
-  // One receptor x ligand pair; accumulates into the per-tile partials.
-  static __device__ __forceinline__ void run(const float4 &r, int rtrow, int rser, const float2 *s_tab, float lx,
-                                             float ly, float lz, float lq, int lt, int lser, const ScoreParams &p,
-                                             float &av, float &ae, int &lc, int &rc, bool &amb) {
+  static __device__ __forceinline__ float d2f(const float4 &r, float lx, float ly, float lz) {
     const float dx = __fsub_rn(r.x, lx), dy = __fsub_rn(r.y, ly), dz = __fsub_rn(r.z, lz);
-    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-    const float2 tp = s_tab[rtrow + lt];  // (R6, eps)
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+  }
+  // soft-core LJ term in FP32 (src/fitness.rs:57-70): eps*(q^2 - 2q),
+  // q = R6 / (r^6 + R6/2)
+  static __device__ __forceinline__ float vdw(float d2, float2 tp) {
     const float r6 = d2 * d2 * d2;
     const float q = tp.x * rcp_approx(__fmaf_rn(0.5f, tp.x, r6));
     float v = (q * (q - 2.0f)) * tp.y;
     if (CLAMP) v = v < -50.0f ? -50.0f : (v > 500.0f ? 500.0f : v);
-    const float tv = __fsub_rn(d2, 72.0f);
-    bool pv = fabsf(tv) < 72.0f;  // 0 < d2 < 144
-    if (SERIAL) pv = pv && (rser != lser);
-    av += pv ? v : 0.0f;
+    return v;
+  }
+  // One receptor x ligand pair; accumulates into the per-tile partials.
+  static __device__ __forceinline__ void run(const float4 &r, int rtrow, int rser, const float2 *s_tab, float lx,
+                                             float ly, float lz, float lq, int lt, int lser, const ScoreParams &p,
+                                             float &av, float &ae, int &lc, int &rc, bool &amb) {
+    const float d2 = d2f(r, lx, ly, lz);
+    const float v = vdw(d2, s_tab[rtrow + lt]);
+    const float tv = __fsub_rn(d2, 72.0f);  // 0 < d2 < 144  <=>  |tv| < 72
+    if (SERIAL) {
+      av += (fabsf(tv) < 72.0f && rser != lser) ? v : 0.0f;
+    } else {
+      add_if_abs_lt(av, tv, 72.0f, v);
+    }
     const float e = (r.w * lq) * rcp_approx(d2);
-    const float te = __fsub_rn(d2, 113.0f);
-    const bool pe = fabsf(te) < 112.0f;  // 1 < d2 < 225
-    ae += pe ? e : 0.0f;
-    const bool pd = d2 < 64.0f;
-    lc += pd;
-    rc += pd;
+    const float te = __fsub_rn(d2, 113.0f);  // 1 < d2 < 225  <=>  |te| < 112
+    add_if_abs_lt(ae, te, 112.0f, e);
+    count_if_lt64(lc, rc, d2);
     amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < p.guard_e) | (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < p.guard_v) |
           (fabsf(__fsub_rn(d2, 64.0f)) < p.guard_d);
   }
 
   // FP64 re-decision of a pair flagged by the guard band.  Recomputes the FP32
-  // decisions with the same intrinsic sequence as run() and corrects the
-  // accumulated terms where the exact decision differs.
-  static __device__ __forceinline__ void fix(const float4 &r, const D4 &r64, int rtrow, int rser,
-                                             const float2 *s_tab, float lx, float ly, float lz, float lq, int lt,
-                                             int lser, double X, double Y, double Z, const ScoreParams &p,
-                                             float &av, float &ae, int &lc, int &rfix) {
-    const float dx = __fsub_rn(r.x, lx), dy = __fsub_rn(r.y, ly), dz = __fsub_rn(r.z, lz);
-    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+  // d2 with the same intrinsic sequence as run() (bit-identical) and corrects
+  // the accumulated terms where the exact decision differs.
+  static __device__ __noinline__ void fix(const float4 r, const D4 r64, int rtrow, int rser, const float2 *s_tab,
+                                          float lx, float ly, float lz, float lq, int lt, int lser, double X,
+                                          double Y, double Z, const Thresholds thr, float *av, float *ae, int *lc,
+                                          int *rfix) {
+    const float d2 = d2f(r, lx, ly, lz);
     const float tv = __fsub_rn(d2, 72.0f);
     const float te = __fsub_rn(d2, 113.0f);
     bool pv32 = fabsf(tv) < 72.0f;
@@ -296,43 +368,41 @@ struct Pair32 {
     const bool pe32 = fabsf(te) < 112.0f;
     const bool pd32 = d2 < 64.0f;
     const double d2x = exact_d2(r64.x, r64.y, r64.z, X, Y, Z);
-    bool pv64 = d2x > 0.0 && d2x < p.thr.vdw_lt;
+    bool pv64 = d2x > 0.0 && d2x < thr.vdw_lt;
     if (SERIAL) pv64 = pv64 && (rser != lser);
-    const bool pe64 = d2x > p.thr.elec_gt && d2x < p.thr.elec_lt;
-    const bool pd64 = d2x < p.thr.desolv_lt;
+    const bool pe64 = d2x > thr.elec_gt && d2x < thr.elec_lt;
+    const bool pd64 = d2x < thr.desolv_lt;
     if (pv64 != pv32) {
-      const float2 tp = s_tab[rtrow + lt];
-      const float r6 = d2 * d2 * d2;
-      const float q = tp.x * rcp_approx(__fmaf_rn(0.5f, tp.x, r6));
-      float v = (q * (q - 2.0f)) * tp.y;
-      if (CLAMP) v = v < -50.0f ? -50.0f : (v > 500.0f ? 500.0f : v);
-      av += pv64 ? v : -v;
+      const float v = vdw(d2, s_tab[rtrow + lt]);
+      *av += pv64 ? v : -v;
     }
     if (pe64 != pe32) {
       const float e = (r.w * lq) * rcp_approx(d2);
-      ae += pe64 ? e : -e;
+      *ae += pe64 ? e : -e;
     }
     if (pd64 != pd32) {
       const int dlt = pd64 ? 1 : -1;
-      lc += dlt;
-      rfix += dlt;
+      *lc += dlt;
+      *rfix += dlt;
     }
   }
 };
 
 template <int NT, int S, bool SERIAL, bool CLAMP>
-__global__ void __launch_bounds__(NT) k_score_f32(const ScoreParams p) {
+__global__ void __launch_bounds__(NT, 2) k_score_f32(const ScoreParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const SmemLayout L = smem_layout<float4>(p.nt, p.nr, NT, sizeof(float2));
+  const SmemLayout32 L = smem_layout32(p.nt, p.nr, NT);
   float4 *s_pos = reinterpret_cast<float4 *>(smem + L.pos);
   int2 *s_meta = reinterpret_cast<int2 *>(smem + L.meta);
+  float4 *s_sph = reinterpret_cast<float4 *>(smem + L.sph);
   uint64_t *s_full = reinterpret_cast<uint64_t *>(smem + L.bars);
   float2 *s_tab = reinterpret_cast<float2 *>(smem + L.tab);
   gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(smem + L.frame);
   double *s_red = reinterpret_cast<double *>(smem + L.red);
+  float4 *s_blob = reinterpret_cast<float4 *>(smem + L.blob);
   uint32_t *s_rcnt = reinterpret_cast<uint32_t *>(smem + L.rcnt);
 
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) mbar_init(&s_full[s], 1);
     fence_mbar_init();
@@ -350,16 +420,16 @@ __global__ void __launch_bounds__(NT) k_score_f32(const ScoreParams p) {
       (static_cast<int>(blockIdx.x) < p.n_poses) ? (p.n_poses - 1 - static_cast<int>(blockIdx.x)) / gridDim.x + 1 : 0;
   const long long Q = static_cast<long long>(my_poses) * nchunks * p.n_tiles;
   if (tid == 0)
-    for (long long q = 0; q < Q && q < kStages; ++q)
-      issue_tile(q, p.n_tiles, p.rec_pos32, p.rec_meta, s_pos, s_meta, s_full);
+    for (long long q = 0; q < Q && q < kStages; ++q) issue_tile32(q, p.n_tiles, p, s_pos, s_meta, s_sph, s_full);
 
+  float4 *my_blob = s_blob + warp * 8;
   long long q = 0;
   for (int k = 0; k < my_poses; ++k) {
     const int pose = static_cast<int>(blockIdx.x) + k * static_cast<int>(gridDim.x);
     if (!p.models && tid < 16)
       reinterpret_cast<double *>(s_frame)[tid] = reinterpret_cast<const double *>(p.frames + pose)[tid];
     __syncthreads();
-    const gd_pose_frame f = *s_frame;
+    const gd_pose_frame &f = *s_frame;
     double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
 
     for (int ch = 0; ch < nchunks; ++ch) {
@@ -369,7 +439,8 @@ __global__ void __launch_bounds__(NT) k_score_f32(const ScoreParams p) {
       for (int s = 0; s < S; ++s) {
         const int j = ch * kChunk + s * NT + tid;
         lcnt[s] = 0;
-        if (j < p.nl) {
+        const bool on = j < p.nl;
+        if (on) {
           double X, Y, Z;
           ligand_atom(p, f, pose, j, X, Y, Z);
           lx[s] = static_cast<float>(X - p.ox);
@@ -384,7 +455,26 @@ __global__ void __launch_bounds__(NT) k_score_f32(const ScoreParams p) {
           lt[s] = 0;
           lser[s] = 0;
         }
+        // bounding sphere of this warp's 32 atoms of slot s (warp-uniform)
+        const unsigned on_mask = __ballot_sync(kFull, on);
+        float cx = on ? lx[s] : 0.f, cy = on ? ly[s] : 0.f, cz = on ? lz[s] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          cx += __shfl_xor_sync(kFull, cx, o);
+          cy += __shfl_xor_sync(kFull, cy, o);
+          cz += __shfl_xor_sync(kFull, cz, o);
+        }
+        const float inv = on_mask ? 1.0f / static_cast<float>(__popc(on_mask)) : 0.0f;
+        cx *= inv;
+        cy *= inv;
+        cz *= inv;
+        float rr = on ? sqrtf((lx[s] - cx) * (lx[s] - cx) + (ly[s] - cy) * (ly[s] - cy) + (lz[s] - cz) * (lz[s] - cz))
+                      : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rr = fmaxf(rr, __shfl_xor_sync(kFull, rr, o));
+        if (lane == 0) my_blob[s] = make_float4(cx, cy, cz, on_mask ? rr * 1.0001f + 0.01f : -1.0e30f);
       }
+      __syncwarp();
       float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
       for (int t = 0; t < p.n_tiles; ++t, ++q) {
         const int st = static_cast<int>(q % kStages);
@@ -393,38 +483,52 @@ __global__ void __launch_bounds__(NT) k_score_f32(const ScoreParams p) {
         const int cnt = min(kTile, p.nr - base);
         float av = 0.0f, ae = 0.0f;
         if (ok) {
-          for (int a = 0; a < cnt; ++a) {
-            const float4 r = s_pos[st * kTile + a];
-            const int2 m = s_meta[st * kTile + a];
-            int rc = 0;
-            bool amb = false;
+          for (int b0 = 0; b0 < cnt; b0 += kBlk) {
+            // which slots of this warp can reach receptor block b0 / kBlk
+            const float4 sp = s_sph[st * (kTile / kBlk) + b0 / kBlk];  // (centre, radius + cutoff reach)
+            unsigned act = 0;
 #pragma unroll
-            for (int s = 0; s < S; ++s)
-              Pair32<SERIAL, CLAMP>::run(r, m.x, m.y, s_tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], p, av, ae,
-                                         lcnt[s], rc, amb);
-            const int tot = __reduce_add_sync(kFull, rc);
-            if (lane == 0 && tot) atomicAdd(&s_rcnt[base + a], static_cast<uint32_t>(tot));
-            if (__any_sync(kFull, amb)) {
-              const D4 r64 = p.rec_pos64[base + a];
-              int rfix = 0;
+            for (int s = 0; s < S; ++s) {
+              const float4 bl = my_blob[s];
+              const float dx = sp.x - bl.x, dy = sp.y - bl.y, dz = sp.z - bl.z;
+              const float lim = sp.w + bl.w;
+              act |= (lim > 0.0f && dx * dx + dy * dy + dz * dz < lim * lim) ? (1u << s) : 0u;
+            }
+            if (act == 0) continue;
+            const int bend = min(b0 + kBlk, cnt);
+            for (int a = b0; a < bend; ++a) {
+              const float4 r = s_pos[st * kTile + a];
+              const int2 m = s_meta[st * kTile + a];
+              int rc = 0;
+              bool amb = false;
 #pragma unroll
-              for (int s = 0; s < S; ++s) {
-                const int j = ch * kChunk + s * NT + tid;
-                if (j >= p.nl) continue;
-                const float dx = __fsub_rn(r.x, lx[s]), dy = __fsub_rn(r.y, ly[s]), dz = __fsub_rn(r.z, lz[s]);
-                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                const float tv = __fsub_rn(d2, 72.0f), te = __fsub_rn(d2, 113.0f);
-                const bool near = (fabsf(__fsub_rn(fabsf(te), 112.0f)) < p.guard_e) |
-                                  (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < p.guard_v) |
-                                  (fabsf(__fsub_rn(d2, 64.0f)) < p.guard_d);
-                if (!near) continue;
-                double X, Y, Z;
-                ligand_atom(p, f, pose, j, X, Y, Z);
-                Pair32<SERIAL, CLAMP>::fix(r, r64, m.x, m.y, s_tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], X, Y,
-                                           Z, p, av, ae, lcnt[s], rfix);
+              for (int s = 0; s < S; ++s)
+                if (act & (1u << s))
+                  Pair32<SERIAL, CLAMP>::run(r, m.x, m.y, s_tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], p, av,
+                                             ae, lcnt[s], rc, amb);
+              const int tot = __reduce_add_sync(kFull, rc);
+              if (lane == 0 && tot) atomicAdd(&s_rcnt[base + a], static_cast<uint32_t>(tot));
+              if (__any_sync(kFull, amb)) {
+                const D4 r64 = p.rec_pos64[base + a];
+                int rfix = 0;
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                  const int j = ch * kChunk + s * NT + tid;
+                  if (j >= p.nl || !(act & (1u << s))) continue;
+                  const float d2 = Pair32<SERIAL, CLAMP>::d2f(r, lx[s], ly[s], lz[s]);
+                  const float tv = __fsub_rn(d2, 72.0f), te = __fsub_rn(d2, 113.0f);
+                  const bool near = (fabsf(__fsub_rn(fabsf(te), 112.0f)) < p.guard_e) |
+                                    (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < p.guard_v) |
+                                    (fabsf(__fsub_rn(d2, 64.0f)) < p.guard_d);
+                  if (!near) continue;
+                  double X, Y, Z;
+                  ligand_atom(p, f, pose, j, X, Y, Z);
+                  Pair32<SERIAL, CLAMP>::fix(r, r64, m.x, m.y, s_tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], X,
+                                             Y, Z, p.thr, &av, &ae, &lcnt[s], &rfix);
+                }
+                const int fx = __reduce_add_sync(kFull, rfix);
+                if (lane == 0 && fx) atomicAdd(&s_rcnt[base + a], static_cast<uint32_t>(fx));
               }
-              const int fx = __reduce_add_sync(kFull, rfix);
-              if (lane == 0 && fx) atomicAdd(&s_rcnt[base + a], static_cast<uint32_t>(fx));
             }
           }
         }
@@ -434,11 +538,11 @@ __global__ void __launch_bounds__(NT) k_score_f32(const ScoreParams p) {
         if (__syncthreads_or(!ok)) {
           if (tid == 0) {
             atomicExch(p.err, kDevTimeout);
-            drain(s_full, q, (q + kStages < Q ? q + kStages : Q));
+            drain(s_full, q, q + kStages < Q ? q + kStages : Q);
           }
           return;
         }
-        if (tid == 0 && q + kStages < Q) issue_tile(q + kStages, p.n_tiles, p.rec_pos32, p.rec_meta, s_pos, s_meta, s_full);
+        if (tid == 0 && q + kStages < Q) issue_tile32(q + kStages, p.n_tiles, p, s_pos, s_meta, s_sph, s_full);
       }
 #pragma unroll
       for (int s = 0; s < S; ++s) {
@@ -631,6 +735,7 @@ gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const doub
   ScoreParams p{};
   p.rec_pos32 = cx->rec_pos32;
   p.rec_pos64 = cx->rec_pos64;
+  p.rec_sph32 = cx->rec_sph32;
   p.rec_meta = cx->rec_meta;
   p.rec_desolv = cx->rec_desolv;
   p.nr = cx->nr;
@@ -673,7 +778,7 @@ gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const doub
   const bool serial = cx->serial_overlap, clamp = cx->need_clamp;
   cudaError_t e;
   if (prec == GD_PREC_F32) {
-    const size_t smem = smem_layout<float4>(p.nt, p.nr, kNT, sizeof(float2)).total;
+    const size_t smem = smem_layout32(p.nt, p.nr, kNT).total;
     const int S = std::max(1, std::min(8, (p.nl + kNT - 1) / kNT));
     switch (S) {
       case 1: e = launch_f32<1>(p, serial, clamp, smem, ctx->sm_count, stream); break;

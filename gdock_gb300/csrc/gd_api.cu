@@ -72,6 +72,21 @@ gd_status ensure_scratch(gd_context *ctx, size_t dev_bytes, size_t pinned_bytes)
   return GD_OK;
 }
 
+gd_status ensure_batch_scratch(gd_context *ctx, size_t dev_bytes) {
+  if (dev_bytes <= ctx->d_batch_bytes) return GD_OK;
+  if (ctx->d_batch) {
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, ctx->d_batch, ctx->d_batch_bytes);
+  }
+  ctx->d_batch = nullptr;
+  ctx->d_batch_bytes = 0;
+  const size_t want = std::max(dev_bytes, static_cast<size_t>(1) << 20);
+  gd_status s = dev_alloc(ctx, want, &ctx->d_batch);
+  if (s != GD_OK) return s;
+  ctx->d_batch_bytes = want;
+  return GD_OK;
+}
+
 gd_status check_device_error(gd_context *ctx) {
   int h = 0;
   cudaError_t e = cudaMemcpy(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
@@ -272,6 +287,7 @@ gd_status gd_context_destroy(gd_context *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+  if (ctx->d_batch) cudaFree(ctx->d_batch);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -332,7 +348,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
       const double eps = std::sqrt(t_eps[a] * t_eps[b]);
       const double r6 = powi6(t_rmin[a] + t_rmin[b]);
       tab64[a * nt + b] = TypePair64{r6, 0.5 * r6, eps, 0.0};
-      tab32[a * nt + b] = TypePair32{static_cast<float>(r6), static_cast<float>(eps), static_cast<float>(-2.0 * eps), 0.f};
+      tab32[a * nt + b] = TypePair32{static_cast<float>(r6), static_cast<float>(eps)};
       if (eps > 50.0) cx->need_clamp = true;
     }
 

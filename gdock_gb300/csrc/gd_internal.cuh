@@ -29,8 +29,8 @@ constexpr int kMaxTypes = 64;
 enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };
 
 // Per-pair parameters of one type pair, FP32 form: R6 = (Rmin_i + Rmin_j)^6,
-// eps = sqrt(eps_i eps_j), m2eps = -2 eps.
-struct TypePair32 { float r6, eps, m2eps, pad; };
+// eps = sqrt(eps_i eps_j).
+struct TypePair32 { float r6, eps; };
 // FP64 form: R6, alpha*R6 (alpha = 0.5), eps.
 struct TypePair64 { double r6, hr6, eps, pad; };
 
@@ -97,6 +97,9 @@ struct gd_context {
   size_t d_scratch_bytes = 0;
   void *h_pinned = nullptr;
   size_t h_pinned_bytes = 0;
+  // argument blocks of batched launches (descriptors, queue, counters)
+  void *d_batch = nullptr;
+  size_t d_batch_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -144,4 +147,9 @@ void guard_widths(const gd_complex *cx, double max_disp, float *gv, float *ge, f
 gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const double *d_models, int n,
                        gd_precision prec, gd_pose_energy *d_out, cudaStream_t stream, double max_disp);
 void free_cluster_cache(gd_complex *cx);
+gd_status ensure_batch_scratch(gd_context *ctx, size_t dev_bytes);
+ScoreParams make_params(gd_complex *cx, const gd_pose_frame *d_frames, const double *d_models, int n,
+                        gd_pose_energy *d_out, double max_disp);
+gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
+                                 int slots, cudaStream_t stream);
 }  // namespace gd

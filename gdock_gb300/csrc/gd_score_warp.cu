@@ -1,0 +1,540 @@
+// Batched FP32 scoring: a persistent kernel in which every warp owns whole
+// work items (one pose of one complex) taken from a global queue, so that
+// poses of many complexes of uneven sizes share one launch and no warp ever
+// waits for another.
+//
+// Per work item a warp
+//   1. copies the complex's descriptor and the pose frame to its shared memory;
+//   2. for each chunk of 32*S ligand atoms: transforms them exactly (FP64, the
+//      reference's operation order, src/structure.rs:80-131), keeps FP32
+//      copies in registers (S slots of 32 consecutive atoms, one per lane) and
+//      a bounding sphere per slot;
+//   3. streams the receptor through its own ring of shared-memory stages, each
+//      filled by one bulk (TMA) copy of 64 atoms + 8 culling spheres and
+//      guarded by a per-warp mbarrier;
+//   4. per 8-atom receptor block, finds the slots whose sphere is within the
+//      15 A cutoff reach (all other pairs contribute exactly nothing) and
+//      evaluates those pairs four receptor atoms at a time (independent
+//      FP32 chains for ILP): soft-core LJ, Coulomb, burial counts, guard band;
+//   5. re-decides in FP64 any pair whose FP32 d2 lies within the guard band of
+//      a cutoff (1, 8, 12, 15 A), so all decisions equal the FP64 ones;
+//   6. reduces in FP64: per-lane Kahan partials, warp sums, desolvation from
+//      the exact burial counts, AIR in restraint order (bit-identical), and
+//      writes the six-field record (src/chromosome.rs:110-127).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gd_device.cuh"
+
+namespace gd {
+namespace {
+
+constexpr int kWarps = 4;      // warps per CTA (independent)
+constexpr int kSeg = 64;       // receptor atoms per ring stage
+constexpr int kWS = 4;         // ring stages per warp
+constexpr int kBlk = 8;        // receptor atoms per culling sphere
+constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
+
+struct BatchParams {
+  const ScoreParams *descs;       // one per complex
+  const long long *item_start;    // prefix sums of poses, ncx + 1 entries
+  int ncx;
+  long long total;
+  unsigned long long *queue;      // work counter, zero at launch
+  uint8_t *gcounts;               // per-warp burial counters in global memory (when not in smem)
+  int gcount_stride;              // bytes per warp in gcounts
+  int smem_cnt;                   // bytes per warp of shared-memory counters (0: use gcounts)
+  int max_nr;                     // largest receptor of the batch
+  int warp_smem;                  // bytes of shared memory per warp
+  int *err;
+};
+
+struct WarpSmem {
+  size_t pos, meta, sph, bars, desc, frame, blob, cnt, total;
+};
+
+__host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
+  WarpSmem L;
+  size_t o = 0;
+  auto al = [&](size_t a) { o = (o + a - 1) / a * a; };
+  L.pos = o;
+  o += sizeof(float4) * kWS * kSeg;
+  L.meta = o;
+  o += sizeof(int2) * kWS * kSeg;
+  L.sph = o;
+  o += sizeof(float4) * kWS * (kSeg / kBlk);
+  L.bars = o;
+  o += 8 * kWS;
+  al(16);
+  L.desc = o;
+  o += sizeof(ScoreParams);
+  al(16);
+  L.frame = o;
+  o += sizeof(gd_pose_frame);
+  L.blob = o;
+  o += sizeof(float4) * 8;
+  L.cnt = o;
+  o += smem_cnt;
+  al(128);
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ void issue_seg(long long q, int seg, const ScoreParams &p, float4 *s_pos, int2 *s_meta,
+                                          float4 *s_sph, uint64_t *s_bar) {
+  const int st = static_cast<int>(q % kWS);
+  constexpr uint32_t kBytes = kSeg * (sizeof(float4) + sizeof(int2)) + (kSeg / kBlk) * sizeof(float4);
+  mbar_expect_tx(&s_bar[st], kBytes);
+  bulk_g2s(&s_pos[st * kSeg], p.rec_pos32 + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(float4), &s_bar[st]);
+  bulk_g2s(&s_meta[st * kSeg], p.rec_meta + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(int2), &s_bar[st]);
+  bulk_g2s(&s_sph[st * (kSeg / kBlk)], p.rec_sph32 + static_cast<size_t>(seg) * (kSeg / kBlk),
+           (kSeg / kBlk) * sizeof(float4), &s_bar[st]);
+}
+
+// acc += v when |t| < lim (one predicated add)
+__device__ __forceinline__ void add_if_abs_lt(float &acc, float t, float lim, float v) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, %2;\n\t@p add.f32 %0, %0, %3;\n\t}" : "+f"(acc)
+      : "f"(fabsf(t)), "f"(lim), "f"(v));
+}
+// a += 1 and b += 1 when d2 < 64
+__device__ __forceinline__ void count_if_lt64(int &a, int &b, float d2) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %2, 0f42800000;\n\t@p add.s32 %0, %0, 1;\n\t@p add.s32 %1, %1, 1;\n\t}"
+      : "+r"(a), "+r"(b)
+      : "f"(d2));
+}
+
+__device__ __forceinline__ float d2f(const float4 &r, float lx, float ly, float lz) {
+  const float dx = __fsub_rn(r.x, lx), dy = __fsub_rn(r.y, ly), dz = __fsub_rn(r.z, lz);
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// soft-core LJ in FP32 (src/fitness.rs:57-70): eps*(q^2 - 2q), q = R6/(r^6 + R6/2)
+template <bool CLAMP>
+__device__ __forceinline__ float vdw_term(float d2, float2 tp) {
+  const float r6 = d2 * d2 * d2;
+  const float q = tp.x * rcp_approx(__fmaf_rn(0.5f, tp.x, r6));
+  float v = (q * (q - 2.0f)) * tp.y;
+  if (CLAMP) v = v < -50.0f ? -50.0f : (v > 500.0f ? 500.0f : v);
+  return v;
+}
+
+template <bool SERIAL, bool CLAMP>
+__device__ __forceinline__ void pair32(const float4 &r, int rtrow, int rser, const float2 *tab, float lx, float ly,
+                                       float lz, float lq, int lt, int lser, float gv, float ge, float gdd, float &av,
+                                       float &ae, int &lc, int &rc, bool &amb) {
+  const float d2 = d2f(r, lx, ly, lz);
+  const float v = vdw_term<CLAMP>(d2, __ldg(&tab[rtrow + lt]));
+  const float tv = __fsub_rn(d2, 72.0f);  // 0 < d2 < 144  <=>  |tv| < 72
+  if (SERIAL) {
+    av += (fabsf(tv) < 72.0f && rser != lser) ? v : 0.0f;
+  } else {
+    add_if_abs_lt(av, tv, 72.0f, v);
+  }
+  const float e = (r.w * lq) * rcp_approx(d2);
+  const float te = __fsub_rn(d2, 113.0f);  // 1 < d2 < 225  <=>  |te| < 112
+  add_if_abs_lt(ae, te, 112.0f, e);
+  count_if_lt64(lc, rc, d2);
+  amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < gv) |
+        (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
+}
+
+__device__ __forceinline__ bool near_band(float d2, float gv, float ge, float gdd) {
+  const float tv = __fsub_rn(d2, 72.0f), te = __fsub_rn(d2, 113.0f);
+  return (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < gv) |
+         (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
+}
+
+// FP64 re-decision of one flagged pair; corrects the FP32 partials where the
+// exact decision differs from the FP32 one (recomputed bit-identically).
+template <bool SERIAL, bool CLAMP>
+__device__ __noinline__ void fix_pair(const float4 r, const D4 r64, int rtrow, int rser, const float2 *tab, float lx,
+                                      float ly, float lz, float lq, int lt, int lser, double X, double Y, double Z,
+                                      const Thresholds thr, float *av, float *ae, int *lc, int *rfix) {
+  const float d2 = d2f(r, lx, ly, lz);
+  const float tv = __fsub_rn(d2, 72.0f);
+  const float te = __fsub_rn(d2, 113.0f);
+  bool pv32 = fabsf(tv) < 72.0f;
+  if (SERIAL) pv32 = pv32 && (rser != lser);
+  const bool pe32 = fabsf(te) < 112.0f;
+  const bool pd32 = d2 < 64.0f;
+  const double d2x = exact_d2(r64.x, r64.y, r64.z, X, Y, Z);
+  bool pv64 = d2x > 0.0 && d2x < thr.vdw_lt;
+  if (SERIAL) pv64 = pv64 && (rser != lser);
+  const bool pe64 = d2x > thr.elec_gt && d2x < thr.elec_lt;
+  const bool pd64 = d2x < thr.desolv_lt;
+  if (pv64 != pv32) {
+    const float v = vdw_term<CLAMP>(d2, __ldg(&tab[rtrow + lt]));
+    *av += pv64 ? v : -v;
+  }
+  if (pe64 != pe32) {
+    const float e = (r.w * lq) * rcp_approx(d2);
+    *ae += pe64 ? e : -e;
+  }
+  if (pd64 != pd32) {
+    const int dlt = pd64 ? 1 : -1;
+    *lc += dlt;
+    *rfix += dlt;
+  }
+}
+
+__device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
+  const int c = static_cast<int>(cnt[i]) + delta;
+  cnt[i] = static_cast<uint8_t>(c > 255 ? 255 : (c < 0 ? 0 : c));
+}
+
+template <int S, bool SERIAL, bool CLAMP>
+__global__ void __launch_bounds__(kWarps * 32) k_score_f32w(const BatchParams bp) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const WarpSmem L = warp_layout(bp.smem_cnt);
+  unsigned char *base = smem + static_cast<size_t>(wib) * L.total;
+  float4 *s_pos = reinterpret_cast<float4 *>(base + L.pos);
+  int2 *s_meta = reinterpret_cast<int2 *>(base + L.meta);
+  float4 *s_sph = reinterpret_cast<float4 *>(base + L.sph);
+  uint64_t *s_bar = reinterpret_cast<uint64_t *>(base + L.bars);
+  ScoreParams *s_desc = reinterpret_cast<ScoreParams *>(base + L.desc);
+  gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(base + L.frame);
+  float4 *s_blob = reinterpret_cast<float4 *>(base + L.blob);
+  const int gwarp = static_cast<int>(blockIdx.x) * kWarps + wib;
+  uint8_t *cnt = bp.smem_cnt ? reinterpret_cast<uint8_t *>(base + L.cnt)
+                             : bp.gcounts + static_cast<size_t>(gwarp) * bp.gcount_stride;
+
+  if (lane == 0) {
+    for (int s = 0; s < kWS; ++s) mbar_init(&s_bar[s], 1);
+    fence_mbar_init();
+  }
+  for (int i = lane; i < bp.max_nr; i += 32) cnt[i] = 0;
+  __syncwarp();
+
+  constexpr int kChunk = 32 * S;
+  long long q = 0;  // ring uses of this warp so far
+  for (;;) {
+    unsigned long long item = 0;
+    if (lane == 0) item = atomicAdd(bp.queue, 1ull);
+    item = __shfl_sync(kFull, item, 0);
+    if (static_cast<long long>(item) >= bp.total) break;
+    // complex of this item: last c with item_start[c] <= item
+    int lo = 0, hi = bp.ncx - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (bp.item_start[mid] <= static_cast<long long>(item)) lo = mid;
+      else hi = mid - 1;
+    }
+    const int pose = static_cast<int>(static_cast<long long>(item) - bp.item_start[lo]);
+    __syncwarp();
+    {
+      const uint64_t *src = reinterpret_cast<const uint64_t *>(bp.descs + lo);
+      uint64_t *dst = reinterpret_cast<uint64_t *>(s_desc);
+      for (int w = lane; w < static_cast<int>(sizeof(ScoreParams) / 8); w += 32) dst[w] = src[w];
+    }
+    __syncwarp();
+    const ScoreParams &p = *s_desc;
+    if (!p.models && lane < 16)
+      reinterpret_cast<double *>(s_frame)[lane] = reinterpret_cast<const double *>(p.frames + pose)[lane];
+    __syncwarp();
+    const gd_pose_frame &f = *s_frame;
+    const int nseg = (p.nr + kSeg - 1) / kSeg;
+    const int nchunks = (p.nl + kChunk - 1) / kChunk;
+    const long long Qi = static_cast<long long>(nchunks) * nseg;
+    const long long q0 = q;
+    if (lane == 0)
+      for (long long k = 0; k < Qi && k < kWS; ++k) issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_sph, s_bar);
+    const float gv = p.guard_v, ge = p.guard_e, gdd = p.guard_d;
+    const float2 *tab = reinterpret_cast<const float2 *>(p.tab32);
+    double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
+    bool failed = false;
+
+    for (int ch = 0; ch < nchunks && !failed; ++ch) {
+      float lx[S], ly[S], lz[S], lq[S];
+      int lt[S], lser[S], lcnt[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int j = ch * kChunk + s * 32 + lane;
+        lcnt[s] = 0;
+        const bool on = j < p.nl;
+        if (on) {
+          double X, Y, Z;
+          ligand_atom(p, f, pose, j, X, Y, Z);
+          lx[s] = static_cast<float>(X - p.ox);
+          ly[s] = static_cast<float>(Y - p.oy);
+          lz[s] = static_cast<float>(Z - p.oz);
+          lq[s] = static_cast<float>(p.lig_q[j]);
+          lt[s] = p.lig_type[j];
+          lser[s] = SERIAL ? p.lig_serial[j] : 0;
+        } else {
+          lx[s] = ly[s] = lz[s] = 1.0e9f;  // far away: no term, no count, no guard hit
+          lq[s] = 0.0f;
+          lt[s] = 0;
+          lser[s] = 0;
+        }
+        // bounding sphere of the slot's 32 atoms
+        const unsigned on_mask = __ballot_sync(kFull, on);
+        float cx = on ? lx[s] : 0.f, cy = on ? ly[s] : 0.f, cz = on ? lz[s] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          cx += __shfl_xor_sync(kFull, cx, o);
+          cy += __shfl_xor_sync(kFull, cy, o);
+          cz += __shfl_xor_sync(kFull, cz, o);
+        }
+        const float inv = on_mask ? 1.0f / static_cast<float>(__popc(on_mask)) : 0.0f;
+        cx *= inv;
+        cy *= inv;
+        cz *= inv;
+        float rr = on ? sqrtf((lx[s] - cx) * (lx[s] - cx) + (ly[s] - cy) * (ly[s] - cy) + (lz[s] - cz) * (lz[s] - cz))
+                      : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rr = fmaxf(rr, __shfl_xor_sync(kFull, rr, o));
+        if (lane == 0) s_blob[s] = make_float4(cx, cy, cz, on_mask ? rr * 1.0001f + 0.01f : -1.0e30f);
+      }
+      __syncwarp();
+      float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
+      for (int g = 0; g < nseg; ++g, ++q) {
+        const int st = static_cast<int>(q % kWS);
+        const bool ok = __all_sync(kFull, mbar_wait(&s_bar[st], static_cast<uint32_t>((q / kWS) & 1)));
+        if (!ok) {
+          failed = true;
+          break;
+        }
+        const int gbase = g * kSeg;
+        const int na = min(kSeg, p.nr - gbase);
+        float av = 0.0f, ae = 0.0f;
+        for (int b0 = 0; b0 < na; b0 += kBlk) {
+          const float4 sp = s_sph[st * (kSeg / kBlk) + b0 / kBlk];  // (centre, radius + cutoff reach)
+          unsigned act = 0;
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            const float4 bl = s_blob[s];
+            const float dx = sp.x - bl.x, dy = sp.y - bl.y, dz = sp.z - bl.z;
+            const float lim = sp.w + bl.w;
+            act |= (lim > 0.0f && dx * dx + dy * dy + dz * dz < lim * lim) ? (1u << s) : 0u;
+          }
+          if (act == 0) continue;
+          const int bend = min(b0 + kBlk, na);
+#pragma unroll 1
+          for (int h = b0; h < bend; h += 4) {
+            float4 r[4];
+            int rt[4], rs[4], rc[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              rc[i] = 0;
+              if (h + i < bend) {
+                r[i] = s_pos[st * kSeg + h + i];
+                const int2 m = s_meta[st * kSeg + h + i];
+                rt[i] = m.x;
+                rs[i] = m.y;
+              } else {
+                r[i] = make_float4(-1.0e9f, -1.0e9f, -1.0e9f, 0.0f);
+                rt[i] = 0;
+                rs[i] = 0;
+              }
+            }
+            bool amb = false;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              if (!(act & (1u << s))) continue;
+#pragma unroll
+              for (int i = 0; i < 4; ++i)
+                pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], gv, ge, gdd,
+                                      av, ae, lcnt[s], rc[i], amb);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const int tot = __reduce_add_sync(kFull, rc[i]);
+              if (lane == 0 && tot) bump_count(cnt, gbase + h + i, tot);
+            }
+            if (__any_sync(kFull, amb)) {
+#pragma unroll 1
+              for (int i = 0; i < 4 && h + i < bend; ++i) {
+                const D4 r64 = p.rec_pos64[gbase + h + i];
+                int rfix = 0;
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                  const int j = ch * kChunk + s * 32 + lane;
+                  if (j >= p.nl || !(act & (1u << s))) continue;
+                  if (!near_band(d2f(r[i], lx[s], ly[s], lz[s]), gv, ge, gdd)) continue;
+                  double X, Y, Z;
+                  ligand_atom(p, f, pose, j, X, Y, Z);
+                  fix_pair<SERIAL, CLAMP>(r[i], r64, rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], X,
+                                          Y, Z, p.thr, &av, &ae, &lcnt[s], &rfix);
+                }
+                const int fx = __reduce_add_sync(kFull, rfix);
+                if (lane == 0 && fx) bump_count(cnt, gbase + h + i, fx);
+              }
+            }
+          }
+        }
+        kahan_add(sv, cv, av);
+        kahan_add(se, ce, ae);
+        __syncwarp();
+        const long long k = q - q0;  // index of this use within the item
+        if (lane == 0 && k + kWS < Qi)
+          issue_seg(q + kWS, static_cast<int>((k + kWS) % nseg), p, s_pos, s_meta, s_sph, s_bar);
+      }
+      if (failed) break;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int j = ch * kChunk + s * 32 + lane;
+        if (j < p.nl) desolv_t += p.lig_desolv[static_cast<size_t>(j) * 11 + min(lcnt[s], 10)];
+      }
+      vdw_t += static_cast<double>(sv) - static_cast<double>(cv);
+      elec_t += static_cast<double>(se) - static_cast<double>(ce);
+    }
+    if (failed) {
+      // a bulk copy did not land in time: record it, wait (bounded) for the
+      // copies this warp still has in flight, and stop this warp
+      if (lane == 0) {
+        atomicExch(bp.err, kDevTimeout);
+        const long long issued = q0 + (Qi < q - q0 + kWS ? Qi : q - q0 + kWS);
+        for (long long u = q; u < issued; ++u) mbar_wait(&s_bar[u % kWS], static_cast<uint32_t>((u / kWS) & 1));
+      }
+      __syncwarp();
+      return;
+    }
+    // receptor burial -> desolvation; reset the counters for the next item
+    for (int i = lane; i < p.nr; i += 32) {
+      const int c = cnt[i];
+      desolv_t += p.rec_desolv[static_cast<size_t>(i) * 11 + (c < 10 ? c : 10)];
+      cnt[i] = 0;
+    }
+    vdw_t = warp_sum(vdw_t);
+    elec_t = warp_sum(elec_t);
+    desolv_t = warp_sum(desolv_t);
+    // AIR: one restraint per lane, summed in restraint order
+    double air = 0.0;
+    int sat = 0;
+    for (int r0 = 0; r0 < p.K; r0 += 32) {
+      double term = 0.0;
+      int ok = 0;
+      const int r = r0 + lane;
+      if (r < p.K) {
+        const D4 a = p.restr_rec[r];
+        double X, Y, Z;
+        ligand_atom(p, f, pose, p.restr_lig[r], X, Y, Z);
+        const double dist = sqrt(exact_d2(a.x, a.y, a.z, X, Y, Z));
+        double v = 0.0;
+        if (dist < 0.0) v = __dsub_rn(0.0, dist);
+        else if (dist > 7.0) v = __dsub_rn(dist, 7.0);
+        term = __dmul_rn(__dmul_rn(10.0, v), v);
+        ok = dist <= 7.0;
+      }
+      for (int k = 0; k < 32 && r0 + k < p.K; ++k) {
+        air = __dadd_rn(air, __shfl_sync(kFull, term, k));
+        sat += __shfl_sync(kFull, ok, k);
+      }
+    }
+    if (lane == 0) {
+      const double ratio = p.K > 0 ? static_cast<double>(sat) / static_cast<double>(p.K) : 0.0;
+      gd_pose_energy o;
+      o.vdw = vdw_t;
+      o.elec = elec_t;
+      o.desolv = desolv_t;
+      o.air = air;
+      o.restraint_penalty = __dmul_rn(__dsub_rn(1.0, ratio), static_cast<double>(p.K));
+      o.fitness = __dadd_rn(
+          __dadd_rn(__dadd_rn(__dmul_rn(p.wv, vdw_t), __dmul_rn(p.we, elec_t)), __dmul_rn(p.wd, desolv_t)),
+          __dmul_rn(p.wa, air));
+      p.out[pose] = o;
+    }
+    __syncwarp();
+  }
+}
+
+template <int S>
+cudaError_t launch_w(const BatchParams &bp, bool serial, bool clamp, size_t smem, int grid, cudaStream_t st) {
+  auto go = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kWarps * 32, smem, st>>>(bp);
+    return cudaGetLastError();
+  };
+  if (!serial && !clamp) return go(k_score_f32w<S, false, false>);
+  if (serial && !clamp) return go(k_score_f32w<S, true, false>);
+  if (!serial && clamp) return go(k_score_f32w<S, false, true>);
+  return go(k_score_f32w<S, true, true>);
+}
+
+template <int S>
+cudaError_t occupancy_w(bool serial, bool clamp, size_t smem, int *per_sm) {
+  if (!serial && !clamp) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, false, false>, kWarps * 32, smem);
+  if (serial && !clamp) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, true, false>, kWarps * 32, smem);
+  if (!serial && clamp) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, false, true>, kWarps * 32, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, true, true>, kWarps * 32, smem);
+}
+
+}  // namespace
+
+// Score the poses of several complexes in one persistent launch (FP32 form).
+// descs[c] describes complex c with its frames/models, outputs and pose count.
+gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
+                                 int slots, cudaStream_t stream) {
+  const int ncx = static_cast<int>(descs.size());
+  if (ncx == 0) return GD_OK;
+  std::vector<long long> start(ncx + 1, 0);
+  int max_nr = 0;
+  for (int c = 0; c < ncx; ++c) {
+    start[c + 1] = start[c] + descs[c].n_poses;
+    max_nr = std::max(max_nr, descs[c].nr);
+  }
+  if (start[ncx] == 0) return GD_OK;
+  const int smem_cnt = max_nr <= kCntSmemMax ? ((max_nr + 15) / 16) * 16 : 0;
+  const WarpSmem L = warp_layout(smem_cnt);
+  const size_t smem = L.total * kWarps;
+  int per_sm = 0;
+  cudaError_t e;
+  const int S = slots <= 2 ? 2 : (slots <= 4 ? 4 : (slots <= 6 ? 6 : 8));
+  switch (S) {
+    case 2: e = occupancy_w<2>(serial, clamp, smem, &per_sm); break;
+    case 4: e = occupancy_w<4>(serial, clamp, smem, &per_sm); break;
+    case 6: e = occupancy_w<6>(serial, clamp, smem, &per_sm); break;
+    default: e = occupancy_w<8>(serial, clamp, smem, &per_sm); break;
+  }
+  if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
+  const long long warps_needed = start[ncx];
+  const int grid = static_cast<int>(std::max<long long>(
+      1, std::min<long long>((warps_needed + kWarps - 1) / kWarps, static_cast<long long>(per_sm) * ctx->sm_count)));
+  // device-side argument block: descriptors, prefix sums, queue counter, counters
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t db = sizeof(ScoreParams) * ncx, sb = sizeof(long long) * (ncx + 1), qb = sizeof(unsigned long long);
+  const size_t gstride = smem_cnt ? 0 : ((max_nr + 127) / 128) * 128;
+  const size_t gb = gstride * static_cast<size_t>(grid) * kWarps;
+  gd_status s = ensure_batch_scratch(ctx, al(db) + al(sb) + al(qb) + al(gb));
+  if (s != GD_OK) return s;
+  char *base = static_cast<char *>(ctx->d_batch);
+  ScoreParams *d_desc = reinterpret_cast<ScoreParams *>(base);
+  long long *d_start = reinterpret_cast<long long *>(base + al(db));
+  unsigned long long *d_queue = reinterpret_cast<unsigned long long *>(base + al(db) + al(sb));
+  uint8_t *d_gcnt = reinterpret_cast<uint8_t *>(base + al(db) + al(sb) + al(qb));
+  // staged from pageable memory: the copy has left the host buffer when the
+  // call returns, so back-to-back launches cannot race on it
+  std::vector<char> h(al(db) + sb);
+  std::memcpy(h.data(), descs.data(), db);
+  std::memcpy(h.data() + al(db), start.data(), sb);
+  e = cudaMemcpyAsync(base, h.data(), h.size(), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, qb, stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring setup");
+  BatchParams bp{};
+  bp.descs = d_desc;
+  bp.item_start = d_start;
+  bp.ncx = ncx;
+  bp.total = start[ncx];
+  bp.queue = d_queue;
+  bp.gcounts = d_gcnt;
+  bp.gcount_stride = static_cast<int>(gstride);
+  bp.smem_cnt = smem_cnt;
+  bp.max_nr = max_nr;
+  bp.warp_smem = static_cast<int>(L.total);
+  bp.err = ctx->d_err;
+  switch (S) {
+    case 2: e = launch_w<2>(bp, serial, clamp, smem, grid, stream); break;
+    case 4: e = launch_w<4>(bp, serial, clamp, smem, grid, stream); break;
+    case 6: e = launch_w<6>(bp, serial, clamp, smem, grid, stream); break;
+    default: e = launch_w<8>(bp, serial, clamp, smem, grid, stream); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
+  return GD_OK;
+}
+
+}  // namespace gd

@@ -35,6 +35,7 @@ constexpr int kWarps = 4;      // warps per CTA (independent)
 constexpr int kSeg = 64;       // receptor atoms per ring stage
 constexpr int kWS = 4;         // ring stages per warp
 constexpr int kBlk = 8;        // receptor atoms per culling sphere
+constexpr int kAtoms = 2;      // receptor atoms held in registers per inner step
 constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
 
 struct BatchParams {
@@ -146,12 +147,20 @@ __device__ __forceinline__ bool near_band(float d2, float gv, float ge, float gd
          (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
 }
 
-// FP64 re-decision of one flagged pair; corrects the FP32 partials where the
-// exact decision differs from the FP32 one (recomputed bit-identically).
+// Corrections of one pair's FP32 contributions after its FP64 re-decision.
+struct FixOut {
+  float dv, de;
+  int dl;
+};
+
+// FP64 re-decision of one flagged pair: recomputes the FP32 d2 and decisions
+// bit-identically to pair32() and returns the corrections where the exact
+// decision differs.  Out of line: it runs for a handful of pairs per pose.
 template <bool SERIAL, bool CLAMP>
-__device__ __noinline__ void fix_pair(const float4 r, const D4 r64, int rtrow, int rser, const float2 *tab, float lx,
-                                      float ly, float lz, float lq, int lt, int lser, double X, double Y, double Z,
-                                      const Thresholds thr, float *av, float *ae, int *lc, int *rfix) {
+__device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, const gd_pose_frame &f, int pose, int j, float4 r,
+                                        int ridx, int rtrow, int rser, float lx, float ly, float lz, float lq, int lt,
+                                        int lser) {
+  FixOut o{0.0f, 0.0f, 0};
   const float d2 = d2f(r, lx, ly, lz);
   const float tv = __fsub_rn(d2, 72.0f);
   const float te = __fsub_rn(d2, 113.0f);
@@ -159,24 +168,24 @@ __device__ __noinline__ void fix_pair(const float4 r, const D4 r64, int rtrow, i
   if (SERIAL) pv32 = pv32 && (rser != lser);
   const bool pe32 = fabsf(te) < 112.0f;
   const bool pd32 = d2 < 64.0f;
+  double X, Y, Z;
+  ligand_atom(p, f, pose, j, X, Y, Z);
+  const D4 r64 = p.rec_pos64[ridx];
   const double d2x = exact_d2(r64.x, r64.y, r64.z, X, Y, Z);
-  bool pv64 = d2x > 0.0 && d2x < thr.vdw_lt;
+  bool pv64 = d2x > 0.0 && d2x < p.thr.vdw_lt;
   if (SERIAL) pv64 = pv64 && (rser != lser);
-  const bool pe64 = d2x > thr.elec_gt && d2x < thr.elec_lt;
-  const bool pd64 = d2x < thr.desolv_lt;
+  const bool pe64 = d2x > p.thr.elec_gt && d2x < p.thr.elec_lt;
+  const bool pd64 = d2x < p.thr.desolv_lt;
   if (pv64 != pv32) {
-    const float v = vdw_term<CLAMP>(d2, __ldg(&tab[rtrow + lt]));
-    *av += pv64 ? v : -v;
+    const float v = vdw_term<CLAMP>(d2, __ldg(reinterpret_cast<const float2 *>(p.tab32) + rtrow + lt));
+    o.dv = pv64 ? v : -v;
   }
   if (pe64 != pe32) {
     const float e = (r.w * lq) * rcp_approx(d2);
-    *ae += pe64 ? e : -e;
+    o.de = pe64 ? e : -e;
   }
-  if (pd64 != pd32) {
-    const int dlt = pd64 ? 1 : -1;
-    *lc += dlt;
-    *rfix += dlt;
-  }
+  if (pd64 != pd32) o.dl = pd64 ? 1 : -1;
+  return o;
 }
 
 __device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
@@ -185,7 +194,7 @@ __device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
 }
 
 template <int S, bool SERIAL, bool CLAMP>
-__global__ void __launch_bounds__(kWarps * 32) k_score_f32w(const BatchParams bp) {
+__global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams bp) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const WarpSmem L = warp_layout(bp.smem_cnt);
@@ -313,11 +322,11 @@ __global__ void __launch_bounds__(kWarps * 32) k_score_f32w(const BatchParams bp
           if (act == 0) continue;
           const int bend = min(b0 + kBlk, na);
 #pragma unroll 1
-          for (int h = b0; h < bend; h += 4) {
-            float4 r[4];
-            int rt[4], rs[4], rc[4];
+          for (int h = b0; h < bend; h += kAtoms) {
+            float4 r[kAtoms];
+            int rt[kAtoms], rs[kAtoms], rc[kAtoms];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < kAtoms; ++i) {
               rc[i] = 0;
               if (h + i < bend) {
                 r[i] = s_pos[st * kSeg + h + i];
@@ -335,33 +344,31 @@ __global__ void __launch_bounds__(kWarps * 32) k_score_f32w(const BatchParams bp
             for (int s = 0; s < S; ++s) {
               if (!(act & (1u << s))) continue;
 #pragma unroll
-              for (int i = 0; i < 4; ++i)
+              for (int i = 0; i < kAtoms; ++i)
                 pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], gv, ge, gdd,
                                       av, ae, lcnt[s], rc[i], amb);
             }
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              const int tot = __reduce_add_sync(kFull, rc[i]);
-              if (lane == 0 && tot) bump_count(cnt, gbase + h + i, tot);
-            }
             if (__any_sync(kFull, amb)) {
 #pragma unroll 1
-              for (int i = 0; i < 4 && h + i < bend; ++i) {
-                const D4 r64 = p.rec_pos64[gbase + h + i];
-                int rfix = 0;
+              for (int i = 0; i < kAtoms && h + i < bend; ++i) {
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
                   const int j = ch * kChunk + s * 32 + lane;
                   if (j >= p.nl || !(act & (1u << s))) continue;
                   if (!near_band(d2f(r[i], lx[s], ly[s], lz[s]), gv, ge, gdd)) continue;
-                  double X, Y, Z;
-                  ligand_atom(p, f, pose, j, X, Y, Z);
-                  fix_pair<SERIAL, CLAMP>(r[i], r64, rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], X,
-                                          Y, Z, p.thr, &av, &ae, &lcnt[s], &rfix);
+                  const FixOut fo = fix_pair<SERIAL, CLAMP>(p, f, pose, j, r[i], gbase + h + i, rt[i], rs[i], lx[s],
+                                                            ly[s], lz[s], lq[s], lt[s], lser[s]);
+                  av += fo.dv;
+                  ae += fo.de;
+                  lcnt[s] += fo.dl;
+                  rc[i] += fo.dl;
                 }
-                const int fx = __reduce_add_sync(kFull, rfix);
-                if (lane == 0 && fx) bump_count(cnt, gbase + h + i, fx);
               }
+            }
+#pragma unroll
+            for (int i = 0; i < kAtoms; ++i) {
+              const int tot = __reduce_add_sync(kFull, rc[i]);
+              if (lane == 0 && tot) bump_count(cnt, gbase + h + i, tot);
             }
           }
         }

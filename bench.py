@@ -205,6 +205,23 @@ def main():
         ctx.check(lib.gd_score_frames_device(cx.h, frames.data_ptr(), n, prec, max_disp, out.data_ptr(),
                                              stream.cuda_stream))
 
+    # --- slots-per-lane sweep (a small autotune on a pose sample) ---
+    tune = {}
+    for slots in (2, 4, 6, 8):
+        ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
+        ns_t = min(NP, 8192)
+        launch(gd.GD_PREC_F32, ns_t)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch(gd.GD_PREC_F32, ns_t)
+        e1.record(stream)
+        e1.synchronize()
+        tune[slots] = ns_t / (e0.elapsed_time(e1) / 1e3)
+    best_slots = max(tune, key=tune.get)
+    ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, best_slots)
+    ctx.sync()
+
     # --- device-resident throughput (value) ---
     for _ in range(args.warmup):
         launch(gd.GD_PREC_F32)
@@ -276,6 +293,7 @@ def main():
             "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES,
                     "d2h_bytes_per_step": NP * 48},
             "gpu_launches": args.steps,
+            "autotune": {"f32_slots": best_slots, "poses_per_s_by_slots": {str(k): v for k, v in tune.items()}},
             "pair_evals_per_s": pairs * value,
             "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,
                            "tflops": FLOP_PER_PAIR * pairs * plain / 1e12,

@@ -21,8 +21,10 @@ EXPORTS = (
     "gd_abi_version", "gd_status_string", "gd_context_create", "gd_context_destroy", "gd_last_error",
     "gd_context_bytes_in_use", "gd_complex_create", "gd_complex_destroy", "gd_complex_num_restraints",
     "gd_complex_set_weights", "gd_make_frames", "gd_score_poses", "gd_score_frames_device", "gd_sync",
-    "gd_score_models", "gd_pose_contacts", "gd_cluster", "gd_cluster_sets",
+    "gd_score_models", "gd_pose_contacts", "gd_cluster", "gd_cluster_sets", "gd_context_set_tuning",
+    "gd_context_get_tuning",
 )
+GD_TUNE_F32_SLOTS = 0
 
 
 class GdAtoms(C.Structure):
@@ -83,6 +85,8 @@ def load(path: Path = LIB_PATH):
         "gd_pose_contacts": ([vp, vp, i32, vp, i64, vp], C.c_int),
         "gd_cluster": ([vp, vp, i32, C.POINTER(GdClusterCfg), C.POINTER(i32), vp, vp, vp], C.c_int),
         "gd_cluster_sets": ([vp, vp, vp, i32, C.POINTER(GdClusterCfg), C.POINTER(i32), vp, vp, vp], C.c_int),
+        "gd_context_set_tuning": ([vp, i32, i32], C.c_int),
+        "gd_context_get_tuning": ([vp, i32], i32),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)
@@ -131,6 +135,9 @@ class Context:
 
     def sync(self):
         self.check(self.lib.gd_sync(self.h))
+
+    def set_tuning(self, knob: int, value: int):
+        self.check(self.lib.gd_context_set_tuning(self.h, knob, value))
 
     @property
     def bytes_in_use(self) -> int:

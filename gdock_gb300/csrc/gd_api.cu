@@ -299,6 +299,23 @@ gd_status gd_context_destroy(gd_context *ctx) {
 
 const char *gd_last_error(const gd_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
+gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
+  if (!ctx) return GD_ERR_INVALID_ARG;
+  if (knob == GD_TUNE_F32_SLOTS) {
+    if (value != 0 && value != 2 && value != 4 && value != 6 && value != 8)
+      return fail(ctx, GD_ERR_INVALID_ARG, "F32 slots must be 0, 2, 4, 6 or 8");
+    ctx->tune_f32_slots = value;
+    return GD_OK;
+  }
+  return fail(ctx, GD_ERR_INVALID_ARG, "unknown tuning knob");
+}
+
+int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob) {
+  if (!ctx) return -1;
+  if (knob == GD_TUNE_F32_SLOTS) return ctx->tune_f32_slots;
+  return -1;
+}
+
 uint64_t gd_context_bytes_in_use(const gd_context *ctx) { return ctx ? ctx->in_use : 0; }
 
 gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms *lig, const int32_t *restraint_pairs,

@@ -101,6 +101,7 @@ struct gd_context {
   void *d_batch = nullptr;
   size_t d_batch_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int tune_f32_slots = 0;  // 0: automatic
 };
 
 struct gd_complex {

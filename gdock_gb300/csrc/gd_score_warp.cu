@@ -35,7 +35,7 @@ constexpr int kWarps = 4;      // warps per CTA (independent)
 constexpr int kSeg = 64;       // receptor atoms per ring stage
 constexpr int kWS = 4;         // ring stages per warp
 constexpr int kBlk = 8;        // receptor atoms per culling sphere
-constexpr int kAtoms = 2;      // receptor atoms held in registers per inner step
+constexpr int kAtoms = 1;      // receptor atoms held in registers per inner step
 constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
 
 struct BatchParams {
@@ -349,12 +349,12 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams
                                       av, ae, lcnt[s], rc[i], amb);
             }
             if (__any_sync(kFull, amb)) {
-#pragma unroll 1
-              for (int i = 0; i < kAtoms && h + i < bend; ++i) {
+#pragma unroll
+              for (int i = 0; i < kAtoms; ++i) {
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
                   const int j = ch * kChunk + s * 32 + lane;
-                  if (j >= p.nl || !(act & (1u << s))) continue;
+                  if (h + i >= bend || j >= p.nl || !(act & (1u << s))) continue;
                   if (!near_band(d2f(r[i], lx[s], ly[s], lz[s]), gv, ge, gdd)) continue;
                   const FixOut fo = fix_pair<SERIAL, CLAMP>(p, f, pose, j, r[i], gbase + h + i, rt[i], rs[i], lx[s],
                                                             ly[s], lz[s], lq[s], lt[s], lser[s]);

@@ -100,6 +100,13 @@ const char *gd_status_string(gd_status s);
  * the device's memory". */
 gd_status gd_context_create(int32_t device, uint64_t hbm_budget_bytes, gd_context **out);
 gd_status gd_context_destroy(gd_context *ctx);
+/* Tuning knobs of the context's kernels (the autotuner sets these).
+ *   GD_TUNE_F32_SLOTS: ligand atoms per lane per pass of the FP32 scoring
+ *                      kernel (2, 4, 6 or 8; 0 = automatic). */
+enum { GD_TUNE_F32_SLOTS = 0 };
+gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
+int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob);
+
 /* Message of the last failing call on this context ("" if none). */
 const char *gd_last_error(const gd_context *ctx);
 /* Bytes of device memory the context's objects hold. */

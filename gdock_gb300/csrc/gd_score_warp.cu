@@ -472,76 +472,103 @@ cudaError_t occupancy_w(bool serial, bool clamp, size_t smem, int *per_sm) {
 
 }  // namespace
 
+// Launch geometry of a batch: slots per lane, shared memory, grid.
+struct BatchPlan {
+  int S, smem_cnt, max_nr, grid;
+  size_t smem;
+  std::vector<long long> start;
+};
+
+static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
+                            int slots, BatchPlan *pl) {
+  const int ncx = static_cast<int>(descs.size());
+  pl->start.assign(ncx + 1, 0);
+  pl->max_nr = 0;
+  for (int c = 0; c < ncx; ++c) {
+    pl->start[c + 1] = pl->start[c] + descs[c].n_poses;
+    pl->max_nr = std::max(pl->max_nr, descs[c].nr);
+  }
+  pl->smem_cnt = pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0;
+  pl->smem = warp_layout(pl->smem_cnt).total * kWarps;
+  pl->S = slots <= 2 ? 2 : (slots <= 4 ? 4 : (slots <= 6 ? 6 : 8));
+  int per_sm = 0;
+  cudaError_t e;
+  switch (pl->S) {
+    case 2: e = occupancy_w<2>(serial, clamp, pl->smem, &per_sm); break;
+    case 4: e = occupancy_w<4>(serial, clamp, pl->smem, &per_sm); break;
+    case 6: e = occupancy_w<6>(serial, clamp, pl->smem, &per_sm); break;
+    default: e = occupancy_w<8>(serial, clamp, pl->smem, &per_sm); break;
+  }
+  if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
+  const long long items = pl->start[ncx];
+  pl->grid = static_cast<int>(std::max<long long>(
+      1, std::min<long long>((items + kWarps - 1) / kWarps, static_cast<long long>(per_sm) * ctx->sm_count)));
+  return GD_OK;
+}
+
+// Upload descriptors and prefix sums to `arg` (device), clear the work
+// counter, and launch.
+static gd_status run_batch(gd_context *ctx, const std::vector<ScoreParams> &descs, const BatchPlan &pl, bool serial,
+                           bool clamp, char *arg, uint8_t *gcounts, size_t gstride, cudaStream_t stream) {
+  const int ncx = static_cast<int>(descs.size());
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t db = sizeof(ScoreParams) * ncx, sb = sizeof(long long) * (ncx + 1);
+  ScoreParams *d_desc = reinterpret_cast<ScoreParams *>(arg);
+  long long *d_start = reinterpret_cast<long long *>(arg + al(db));
+  unsigned long long *d_queue = reinterpret_cast<unsigned long long *>(arg + al(db) + al(sb));
+  // staged from pageable memory: the copy has left the host buffer when the
+  // call returns, so back-to-back launches cannot race on it
+  std::vector<char> h(al(db) + sb);
+  std::memcpy(h.data(), descs.data(), db);
+  std::memcpy(h.data() + al(db), pl.start.data(), sb);
+  cudaError_t e = cudaMemcpyAsync(arg, h.data(), h.size(), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring setup");
+  BatchParams bp{};
+  bp.descs = d_desc;
+  bp.item_start = d_start;
+  bp.ncx = ncx;
+  bp.total = pl.start[ncx];
+  bp.queue = d_queue;
+  bp.gcounts = gcounts;
+  bp.gcount_stride = static_cast<int>(gstride);
+  bp.smem_cnt = pl.smem_cnt;
+  bp.max_nr = pl.max_nr;
+  bp.warp_smem = static_cast<int>(warp_layout(pl.smem_cnt).total);
+  bp.err = ctx->d_err;
+  switch (pl.S) {
+    case 2: e = launch_w<2>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
+    case 4: e = launch_w<4>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
+    case 6: e = launch_w<6>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
+    default: e = launch_w<8>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
+  return GD_OK;
+}
+
+static size_t arg_bytes(int ncx) {
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  return al(sizeof(ScoreParams) * ncx) + al(sizeof(long long) * (ncx + 1)) + al(sizeof(unsigned long long));
+}
+
 // Score the poses of several complexes in one persistent launch (FP32 form).
 // descs[c] describes complex c with its frames/models, outputs and pose count.
 gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
                                  int slots, cudaStream_t stream) {
   const int ncx = static_cast<int>(descs.size());
   if (ncx == 0) return GD_OK;
-  std::vector<long long> start(ncx + 1, 0);
-  int max_nr = 0;
-  for (int c = 0; c < ncx; ++c) {
-    start[c + 1] = start[c] + descs[c].n_poses;
-    max_nr = std::max(max_nr, descs[c].nr);
-  }
-  if (start[ncx] == 0) return GD_OK;
-  const int smem_cnt = max_nr <= kCntSmemMax ? ((max_nr + 15) / 16) * 16 : 0;
-  const WarpSmem L = warp_layout(smem_cnt);
-  const size_t smem = L.total * kWarps;
-  int per_sm = 0;
-  cudaError_t e;
-  const int S = slots <= 2 ? 2 : (slots <= 4 ? 4 : (slots <= 6 ? 6 : 8));
-  switch (S) {
-    case 2: e = occupancy_w<2>(serial, clamp, smem, &per_sm); break;
-    case 4: e = occupancy_w<4>(serial, clamp, smem, &per_sm); break;
-    case 6: e = occupancy_w<6>(serial, clamp, smem, &per_sm); break;
-    default: e = occupancy_w<8>(serial, clamp, smem, &per_sm); break;
-  }
-  if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
-  const long long warps_needed = start[ncx];
-  const int grid = static_cast<int>(std::max<long long>(
-      1, std::min<long long>((warps_needed + kWarps - 1) / kWarps, static_cast<long long>(per_sm) * ctx->sm_count)));
-  // device-side argument block: descriptors, prefix sums, queue counter, counters
-  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-  const size_t db = sizeof(ScoreParams) * ncx, sb = sizeof(long long) * (ncx + 1), qb = sizeof(unsigned long long);
-  const size_t gstride = smem_cnt ? 0 : ((max_nr + 127) / 128) * 128;
-  const size_t gb = gstride * static_cast<size_t>(grid) * kWarps;
-  gd_status s = ensure_batch_scratch(ctx, al(db) + al(sb) + al(qb) + al(gb));
+  BatchPlan pl;
+  gd_status s = plan_batch(ctx, descs, serial, clamp, slots, &pl);
   if (s != GD_OK) return s;
-  char *base = static_cast<char *>(ctx->d_batch);
-  ScoreParams *d_desc = reinterpret_cast<ScoreParams *>(base);
-  long long *d_start = reinterpret_cast<long long *>(base + al(db));
-  unsigned long long *d_queue = reinterpret_cast<unsigned long long *>(base + al(db) + al(sb));
-  uint8_t *d_gcnt = reinterpret_cast<uint8_t *>(base + al(db) + al(sb) + al(qb));
-  // staged from pageable memory: the copy has left the host buffer when the
-  // call returns, so back-to-back launches cannot race on it
-  std::vector<char> h(al(db) + sb);
-  std::memcpy(h.data(), descs.data(), db);
-  std::memcpy(h.data() + al(db), start.data(), sb);
-  e = cudaMemcpyAsync(base, h.data(), h.size(), cudaMemcpyHostToDevice, stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, qb, stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring setup");
-  BatchParams bp{};
-  bp.descs = d_desc;
-  bp.item_start = d_start;
-  bp.ncx = ncx;
-  bp.total = start[ncx];
-  bp.queue = d_queue;
-  bp.gcounts = d_gcnt;
-  bp.gcount_stride = static_cast<int>(gstride);
-  bp.smem_cnt = smem_cnt;
-  bp.max_nr = max_nr;
-  bp.warp_smem = static_cast<int>(L.total);
-  bp.err = ctx->d_err;
-  switch (S) {
-    case 2: e = launch_w<2>(bp, serial, clamp, smem, grid, stream); break;
-    case 4: e = launch_w<4>(bp, serial, clamp, smem, grid, stream); break;
-    case 6: e = launch_w<6>(bp, serial, clamp, smem, grid, stream); break;
-    default: e = launch_w<8>(bp, serial, clamp, smem, grid, stream); break;
-  }
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
-  return GD_OK;
+  if (pl.start[ncx] == 0) return GD_OK;
+  const size_t gstride = pl.smem_cnt ? 0 : ((pl.max_nr + 127) / 128) * 128;
+  const size_t gb = gstride * static_cast<size_t>(pl.grid) * kWarps;
+  s = ensure_batch_scratch(ctx, arg_bytes(ncx) + gb);
+  if (s != GD_OK) return s;
+  char *arg = static_cast<char *>(ctx->d_batch);
+  return run_batch(ctx, descs, pl, serial, clamp, arg, reinterpret_cast<uint8_t *>(arg + arg_bytes(ncx)), gstride,
+                   stream);
 }
 
 }  // namespace gd

@@ -22,7 +22,7 @@ EXPORTS = (
     "gd_context_bytes_in_use", "gd_complex_create", "gd_complex_destroy", "gd_complex_num_restraints",
     "gd_complex_set_weights", "gd_make_frames", "gd_score_poses", "gd_score_frames_device", "gd_sync",
     "gd_score_models", "gd_pose_contacts", "gd_cluster", "gd_cluster_sets", "gd_context_set_tuning",
-    "gd_context_get_tuning",
+    "gd_context_get_tuning", "gd_score_frames_device_noalloc",
 )
 GD_TUNE_F32_SLOTS = 0
 
@@ -87,6 +87,7 @@ def load(path: Path = LIB_PATH):
         "gd_cluster_sets": ([vp, vp, vp, i32, C.POINTER(GdClusterCfg), C.POINTER(i32), vp, vp, vp], C.c_int),
         "gd_context_set_tuning": ([vp, i32, i32], C.c_int),
         "gd_context_get_tuning": ([vp, i32], i32),
+        "gd_score_frames_device_noalloc": ([vp, vp, i32, d, vp, vp], C.c_int),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)

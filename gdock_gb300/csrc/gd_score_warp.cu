@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "gd_device.cuh"
@@ -571,4 +573,75 @@ gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams>
                    stream);
 }
 
+
+// ---------------------------------------------------------------------------
+// Scoring without any device allocation.
+//
+// Some hosts of this library cannot allocate device memory once scoring
+// starts: a docking service that hands the whole GPU to a pool allocator at
+// start-up (a cudaMalloc from inside the scoring path would fail or fragment
+// that pool), or a real-time host loop that forbids the unbounded latency of
+// an allocation.  For them the FP32 scoring kernel can take its small argument
+// block (complex descriptor, pose-count prefix sums, work counter) from the
+// file-scope array below instead of from context scratch memory.  The array
+// is kNoAllocScratchBytes bytes on every GPU that loads the library and stays
+// allocated until the process exits.  In host code its name is only a
+// stand-in: the device address is looked up once per device with
+// cudaGetSymbolAddress while that device is current.
+constexpr size_t kNoAllocScratchBytes = 4096;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up on
+// the first call for that device).
+gd_status noalloc_scratch(gd_context *ctx, void **out) {
+  if (ctx->device < 0 || ctx->device >= kMaxDevices) return fail(ctx, GD_ERR_INVALID_ARG, "device index too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[ctx->device]) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) return cuda_fail(ctx, e, "cudaGetSymbolAddress(no-allocation scratch)");
+    g_noalloc_addr[ctx->device] = ptr;
+  }
+  *out = g_noalloc_addr[ctx->device];
+  return GD_OK;
+}
+}  // namespace
+
+}  // namespace gd
+
+extern "C" gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n,
+                                                    double max_displacement, gd_pose_energy *d_out, void *stream) {
+  using namespace gd;
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n < 0 || (n > 0 && (!d_frames || !d_out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad frames/out");
+  if (!(max_displacement >= 0.0)) return fail(ctx, GD_ERR_INVALID_ARG, "bad max_displacement");
+  if (cx->nr > kCntSmemMax)
+    return fail(ctx, GD_ERR_INVALID_ARG,
+                "receptor has " + std::to_string(cx->nr) + " atoms; scoring without allocation handles at most " +
+                    std::to_string(kCntSmemMax));
+  static_assert(sizeof(ScoreParams) + 2 * sizeof(long long) + sizeof(unsigned long long) + 512 <= kNoAllocScratchBytes,
+                "no-allocation scratch too small for one complex");
+  if (n == 0) return GD_OK;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  void *scratch = nullptr;
+  gd_status s = noalloc_scratch(ctx, &scratch);
+  if (s != GD_OK) return s;
+  const std::vector<ScoreParams> descs{make_params(cx, d_frames, nullptr, n, d_out, max_displacement)};
+  const int slots = ctx->tune_f32_slots ? ctx->tune_f32_slots : 4;
+  BatchPlan pl;
+  s = plan_batch(ctx, descs, cx->serial_overlap, cx->need_clamp, slots, &pl);
+  if (s != GD_OK) return s;
+  // counters live in shared memory (receptor <= kCntSmemMax atoms): no global counters
+  return run_batch(ctx, descs, pl, cx->serial_overlap, cx->need_clamp, static_cast<char *>(scratch), nullptr, 0,
+                   stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
+}
+
+namespace gd {
 }  // namespace gd

@@ -141,6 +141,21 @@ gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_prec
 gd_status gd_score_frames_device(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n,
                                  gd_precision prec, double max_displacement, gd_pose_energy *d_out,
                                  void *stream);
+/* gd_score_frames_device in the FP32 form, for callers that must not
+ * allocate device memory while they score (for example a host whose GPU
+ * memory is handed to its own pool allocator at start-up, or a real-time loop
+ * that cannot take an allocation's latency).  No counterpart in the
+ * reference.  It allocates nothing: its argument block lives in a 4 KiB
+ * file-scope device array that every GPU loading the library keeps until the
+ * process exits.  The first call on a device looks that array's address up
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Receptors of more than 4096 atoms are rejected with GD_ERR_INVALID_ARG.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, or contexts on the same device) race and must be serialised by
+ * the caller.  Errors of the device run are reported by gd_sync. */
+gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n,
+                                         double max_displacement, gd_pose_energy *d_out, void *stream);
+
 /* Wait for the context's work and report any device-side error. */
 gd_status gd_sync(gd_context *ctx);
 

@@ -22,14 +22,15 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 from . import _lib
-from ._lib import GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms, make_frames, ptr
+from ._lib import (GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms, ga_default_cfg, ga_draw,
+                   make_frames, ptr)
 from .pdb import Molecule, combine_molecules, position_ligand, read_pdb, read_pdb_text
 
 __all__ = [
     "Context", "Complex", "GdError", "GD_PREC_F32", "GD_PREC_F64", "EnergyWeights", "ClusteringConfig",
     "ClusterResult", "vdw_energy", "elec_energy", "desolv_energy", "air_energy", "satisfaction_ratio",
     "cluster_sets", "make_frames", "Molecule", "read_pdb", "read_pdb_text", "position_ligand",
-    "combine_molecules", "default_context",
+    "combine_molecules", "default_context", "ga_default_cfg", "ga_draw", "run_ga", "GaResult",
 ]
 
 
@@ -210,3 +211,27 @@ def air_energy(restraint_pairs, receptor: Molecule, ligand: Molecule) -> float:
 def satisfaction_ratio(restraint_pairs, receptor: Molecule, ligand: Molecule) -> float:
     e, k = _one_shot(receptor, ligand, restraint_pairs)
     return 0.0 if k == 0 else 1.0 - float(e["restraint_penalty"]) / k
+
+
+@dataclass
+class GaResult:
+    genes: np.ndarray          # (jobs, pop, 6) final populations
+    energies: np.ndarray       # (jobs, pop) structured energies of the final populations
+    generations: np.ndarray    # (jobs,) generations evolved
+    history: np.ndarray        # (jobs, max_generations) best fitness per generation
+
+
+def run_ga(complexes: Sequence[Complex], cfg=None, precision=GD_PREC_F32, use_graph: bool = True,
+           ctx: Optional[Context] = None) -> GaResult:
+    """gdock's GA loop (src/commands/run.rs:381-531) for many jobs on the GPU."""
+    ctx = ctx or complexes[0].ctx
+    cfg = cfg or ga_default_cfg()
+    J, n, G = len(complexes), cfg.pop_size, cfg.max_generations
+    handles = (C.c_void_p * J)(*[c.h.value for c in complexes])
+    genes = np.zeros((J, n, 6))
+    energies = np.zeros((J, n), dtype=POSE_ENERGY_DTYPE)
+    gens = np.zeros(J, np.int32)
+    hist = np.zeros((J, max(G, 1)))
+    ctx.check(ctx.lib.gd_ga_run(ctx.h, C.cast(handles, C.c_void_p), J, C.byref(cfg), _prec(precision),
+                                1 if use_graph else 0, ptr(genes), ptr(energies), ptr(gens), ptr(hist)))
+    return GaResult(genes, energies, gens, hist[:, :G])

@@ -22,7 +22,7 @@ EXPORTS = (
     "gd_context_bytes_in_use", "gd_complex_create", "gd_complex_destroy", "gd_complex_num_restraints",
     "gd_complex_set_weights", "gd_make_frames", "gd_score_poses", "gd_score_frames_device", "gd_sync",
     "gd_score_models", "gd_pose_contacts", "gd_cluster", "gd_cluster_sets", "gd_context_set_tuning",
-    "gd_context_get_tuning", "gd_score_frames_device_noalloc",
+    "gd_context_get_tuning", "gd_score_frames_device_noalloc", "gd_ga_default_cfg", "gd_ga_draw", "gd_ga_run",
 )
 GD_TUNE_F32_SLOTS = 0
 
@@ -41,6 +41,14 @@ class GdWeights(C.Structure):
 class GdClusterCfg(C.Structure):
     _fields_ = [("contact_distance", C.c_double), ("fcc_cutoff", C.c_double), ("strictness", C.c_double),
                 ("min_cluster_size", C.c_int32)]
+
+
+class GdGaCfg(C.Structure):
+    _fields_ = [("pop_size", C.c_int32), ("elitism", C.c_int32), ("tournament_size", C.c_int32),
+                ("crossover_rate", C.c_double), ("mutation_rate", C.c_double), ("max_displacement", C.c_double),
+                ("rot_sigma", C.c_double), ("trans_sigma", C.c_double), ("max_generations", C.c_int32),
+                ("early_stopping", C.c_int32), ("convergence_threshold", C.c_double),
+                ("convergence_window", C.c_int32), ("seed", C.c_uint64)]
 
 
 POSE_ENERGY_DTYPE = np.dtype([(k, np.float64) for k in
@@ -88,6 +96,9 @@ def load(path: Path = LIB_PATH):
         "gd_context_set_tuning": ([vp, i32, i32], C.c_int),
         "gd_context_get_tuning": ([vp, i32], i32),
         "gd_score_frames_device_noalloc": ([vp, vp, i32, d, vp, vp], C.c_int),
+        "gd_ga_default_cfg": ([C.POINTER(GdGaCfg)], C.c_int),
+        "gd_ga_draw": ([C.POINTER(GdGaCfg), C.c_uint64, i32, vp, vp, vp, vp, vp, vp], C.c_int),
+        "gd_ga_run": ([vp, vp, i32, C.POINTER(GdGaCfg), C.c_int, i32, vp, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)
@@ -166,4 +177,27 @@ def make_frames(genes: np.ndarray) -> np.ndarray:
     st = lib.gd_make_frames(ptr(g), g.shape[0], ptr(out))
     if st != GD_OK:
         raise GdError(st, "gd_make_frames")
+    return out
+
+
+def ga_default_cfg(**overrides) -> GdGaCfg:
+    c = GdGaCfg()
+    load().gd_ga_default_cfg(C.byref(c))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+def ga_draw(cfg: GdGaCfg, seed: int, generations: int) -> dict:
+    """The host draws of one GA job (initial genes and per-generation randoms)."""
+    n = cfg.pop_size
+    m = 2 * (n // 2)
+    G = max(generations, 0)
+    out = {"init": np.zeros((n, 6)), "tour": np.zeros((G, n * cfg.tournament_size), np.int32),
+           "perm": np.zeros((G, n), np.int32), "cross_u": np.zeros((G, 6 * (n // 2))),
+           "mut_u": np.zeros((G, 6 * m)), "mut_z": np.zeros((G, 6 * m))}
+    st = load().gd_ga_draw(C.byref(cfg), seed, G, *[ptr(out[k]) if out[k].size else None for k in
+                                                     ("init", "tour", "perm", "cross_u", "mut_u", "mut_z")])
+    if st != GD_OK:
+        raise GdError(st, "gd_ga_draw")
     return out

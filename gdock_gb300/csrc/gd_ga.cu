@@ -1,0 +1,506 @@
+// Device-resident genetic algorithm: gdock's generation loop
+// (src/commands/run.rs:381-531) with Population::evolve (src/population.rs:74-121)
+// on the GPU, for one or many docking jobs at once.
+//
+// Randomness.  The number and order of random draws of a generation do not
+// depend on fitness (3n tournament indices, the shuffle, 6 uniforms per
+// crossover pair, 6 uniforms per mutated individual plus one normal sample
+// where a uniform triggers), so the host draws them up front in the
+// reference's order from a seeded generator and uploads them; the device then
+// applies them to whatever individuals fitness selects.  The generator is
+// xoshiro256** seeded through SplitMix64 (Blackman & Vigna; Steele, Lea &
+// Flood), uniforms are 53-bit, normals are Box-Muller; gdock's own stream
+// (rand's StdRng) is not reproduced.
+//
+// Per generation, for all jobs: pose frames from genes (device sin/cos),
+// batched scoring (the persistent FP32 kernel, or the plain FP64 kernel per
+// job), then one CTA per job runs the convergence bookkeeping of the
+// reference loop and, unless the job stopped, evolve.  One generation is
+// captured as a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gd_device.cuh"
+
+namespace gd {
+namespace {
+
+// ------------------------------------------------------------ host RNG ----
+
+struct Rng {
+  uint64_t s[4];
+  static uint64_t splitmix(uint64_t &x) {
+    uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+  }
+  explicit Rng(uint64_t seed) {
+    uint64_t x = seed;
+    for (auto &v : s) v = splitmix(x);
+  }
+  static uint64_t rotl(uint64_t v, int k) { return (v << k) | (v >> (64 - k)); }
+  uint64_t next() {
+    const uint64_t r = rotl(s[1] * 5, 7) * 9;
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return r;
+  }
+  double uniform() { return static_cast<double>(next() >> 11) * 0x1.0p-53; }  // [0, 1)
+  int range(int n) {                                                           // [0, n)
+    const int v = static_cast<int>(uniform() * n);
+    return v < n ? v : n - 1;
+  }
+  double normal() {  // Box-Muller, one value per call
+    const double u1 = 1.0 - uniform(), u2 = uniform();
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+  }
+};
+
+// Random inputs of one generation of one job, in consumption order.
+struct GenDraws {
+  std::vector<int> tour, perm;
+  std::vector<double> cross_u, mut_u, mut_z;
+};
+
+void draw_generation(Rng &rng, const gd_ga_cfg &c, GenDraws &d) {
+  const int n = c.pop_size, m = 2 * (n / 2);
+  d.tour.resize(static_cast<size_t>(c.tournament_size) * n);
+  for (auto &t : d.tour) t = rng.range(n);  // tournament_selection (src/population.rs:135-142)
+  d.perm.resize(n);
+  for (int k = 0; k < n; ++k) d.perm[k] = k;
+  for (int i = n - 1; i >= 1; --i) std::swap(d.perm[i], d.perm[rng.range(i + 1)]);  // shuffle (:88)
+  d.cross_u.resize(static_cast<size_t>(6) * (n / 2));
+  for (auto &u : d.cross_u) u = rng.uniform();  // ga::crossover (src/ga.rs:19-31)
+  d.mut_u.resize(static_cast<size_t>(6) * m);
+  d.mut_z.resize(static_cast<size_t>(6) * m);
+  for (int k = 0; k < m; ++k)  // Chromosome::mutate (src/chromosome.rs:61-76)
+    for (int g = 0; g < 6; ++g) {
+      const double u = rng.uniform();
+      d.mut_u[6 * k + g] = u;
+      d.mut_z[6 * k + g] = u <= c.mutation_rate ? (g < 3 ? c.rot_sigma : c.trans_sigma) * rng.normal() : 0.0;
+    }
+}
+
+// Chromosome::new (src/chromosome.rs:27-34): angles in [0, 2pi], displacement in [-M, M]
+void draw_initial(Rng &rng, const gd_ga_cfg &c, double *genes) {
+  for (int k = 0; k < c.pop_size; ++k) {
+    for (int g = 0; g < 3; ++g) genes[6 * k + g] = 6.283185307179586 * rng.uniform();
+    for (int g = 3; g < 6; ++g) genes[6 * k + g] = -c.max_displacement + 2.0 * c.max_displacement * rng.uniform();
+  }
+}
+
+// ------------------------------------------------------------- kernels ----
+
+// Pose frames from genes on the device (CUDA's sin/cos; the composite
+// entries in the reference's operation order).
+__global__ void k_frames(const double *genes, gd_pose_frame *frames, const int *job_of, const GaJobState *state,
+                         int total) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  if (state[job_of[k]].stop) return;
+  const double *g = genes + 6 * static_cast<size_t>(k);
+  double sa, ca, sb, cb, sg, cg;
+  sincos(g[0], &sa, &ca);
+  sincos(g[1], &sb, &cb);
+  sincos(g[2], &sg, &cg);
+  gd_pose_frame f;
+  f.ca = ca;
+  f.sa = sa;
+  f.cb = cb;
+  f.sb = sb;
+  f.cg = cg;
+  f.sg = sg;
+  f.m01 = __dadd_rn(__dmul_rn(-sa, cg), __dmul_rn(__dmul_rn(ca, sb), sg));
+  f.m02 = __dadd_rn(__dmul_rn(sa, sg), __dmul_rn(__dmul_rn(ca, sb), cg));
+  f.m11 = __dadd_rn(__dmul_rn(ca, cg), __dmul_rn(__dmul_rn(sa, sb), sg));
+  f.m12 = __dadd_rn(__dmul_rn(-ca, sg), __dmul_rn(__dmul_rn(sa, sb), cg));
+  f.dx = g[3];
+  f.dy = g[4];
+  f.dz = g[5];
+  f.pad[0] = f.pad[1] = f.pad[2] = 0.0;
+  frames[k] = f;
+}
+
+struct GaStepParams {
+  double *genes;              // [jobs][n][6], updated in place
+  double *genes_tmp;          // scratch [jobs][m][6]
+  const gd_pose_energy *energies;  // [jobs][n]
+  GaJobState *state;          // [jobs]
+  double *history;            // [jobs][max_gen] best fitness per generation
+  const int *tour, *perm;     // [jobs][max_gen][...]
+  const double *cross_u, *mut_u, *mut_z;
+  gd_ga_cfg cfg;
+};
+
+// NaN ranks after every number (a total order the reference's partial_cmp
+// sort does not define; it never arises for finite inputs)
+__device__ __forceinline__ double key_of(double f) { return f != f ? INFINITY : f; }
+
+// One CTA per job: the reference loop's bookkeeping for the fitness just
+// computed, then evolve.
+__global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const gd_ga_cfg &c = P.cfg;
+  const int job = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int n = c.pop_size, m = 2 * (n / 2);
+  double *f = reinterpret_cast<double *>(smem);   // [n] fitness of the evaluated population
+  double *f2 = f + n;                              // [m] fitness carried by the offspring
+  int *sel = reinterpret_cast<int *>(f2 + m);      // [n] tournament winners
+  int *elite = sel + n;                            // [elitism]
+  __shared__ double s_eg[64 * 6];                  // elites' genes, staged before the population is overwritten
+  __shared__ double s_best;
+  __shared__ int s_evolve;
+  GaJobState &st = P.state[job];
+  if (st.stop) return;
+  const gd_pose_energy *E = P.energies + static_cast<size_t>(job) * n;
+  for (int k = tid; k < n; k += nt) f[k] = E[k].fitness;
+  __syncthreads();
+  if (tid == 0) {
+    const int gen = st.gen;
+    if (gen >= c.max_generations) {
+      // the evaluation just done was of the final population: stop here
+      st.stop = 2;
+      s_evolve = 0;
+    } else {
+      // best of this generation, first minimum (src/commands/run.rs:391-398)
+      int bi = 0;
+      for (int k = 1; k < n; ++k)
+        if (f[bi] > f[k]) bi = k;
+      const double best = f[bi];
+      P.history[static_cast<size_t>(job) * c.max_generations + gen] = best;
+      if (gen > 0) {  // convergence window (src/commands/run.rs:400-409)
+        const double imp = (st.last_best - best) / fabs(st.last_best);
+        if (imp < c.convergence_threshold) st.stagnant += 1;
+        else st.stagnant = 0;
+      }
+      st.last_best = best;
+      if (c.early_stopping && st.stagnant >= c.convergence_window) {
+        st.stop = 1;  // converged: this population is the final one
+        s_evolve = 0;
+      } else {
+        st.gen = gen + 1;
+        s_evolve = 1;
+      }
+      s_best = best;
+    }
+  }
+  __syncthreads();
+  if (!s_evolve) return;
+  const int gen = st.gen - 1;  // draws of the generation being evolved
+  const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;
+  const int *tour = P.tour + jg * c.tournament_size * n;
+  const int *perm = P.perm + jg * n;
+  const double *cu = P.cross_u + jg * 6 * (n / 2);
+  const double *mu = P.mut_u + jg * 6 * m;
+  const double *mz = P.mut_z + jg * 6 * m;
+  double *G = P.genes + static_cast<size_t>(job) * n * 6;
+  double *T = P.genes_tmp + static_cast<size_t>(job) * m * 6;
+  const int ne = c.elitism < n ? c.elitism : n;
+  // elites: stable ascending order, first ne (src/population.rs:76-82)
+  for (int k = tid; k < n; k += nt) {
+    const double fk = key_of(f[k]);
+    int r = 0;
+    for (int q = 0; q < n; ++q) {
+      const double fq = key_of(f[q]);
+      r += (fq < fk) || (fq == fk && q < k);
+    }
+    if (r < ne) elite[r] = k;
+  }
+  // tournament: first minimum of the draws (src/population.rs:136-156)
+  for (int k = tid; k < n; k += nt) {
+    int best = tour[c.tournament_size * k];
+    for (int t = 1; t < c.tournament_size; ++t) {
+      const int q = tour[c.tournament_size * k + t];
+      if (f[best] > f[q]) best = q;
+    }
+    sel[k] = best;
+  }
+  __syncthreads();
+  for (int i = tid; i < ne * 6; i += nt) s_eg[i] = G[6 * elite[i / 6] + i % 6];
+  // shuffle + crossover + mutation (src/population.rs:88-107, src/ga.rs:7-39,
+  // src/chromosome.rs:56-77)
+  const double two_pi = 6.283185307179586;
+  for (int p = tid; p < n / 2; p += nt) {
+    const int a = sel[perm[2 * p]], b = sel[perm[2 * p + 1]];
+    for (int g = 0; g < 6; ++g) {
+      const double ga = G[6 * a + g], gb = G[6 * b + g];
+      const bool sw = cu[6 * p + g] <= c.crossover_rate;
+      double o[2] = {sw ? gb : ga, sw ? ga : gb};
+      for (int h = 0; h < 2; ++h) {
+        const int k = 2 * p + h;
+        if (mu[6 * k + g] <= c.mutation_rate) {
+          double v = __dadd_rn(o[h], mz[6 * k + g]);
+          if (g < 3) {
+            double r = fmod(v, two_pi);  // f64::rem_euclid
+            if (r < 0.0) r = __dadd_rn(r, two_pi);
+            v = r;
+          } else {
+            v = v < -c.max_displacement ? -c.max_displacement : (v > c.max_displacement ? c.max_displacement : v);
+          }
+          o[h] = v;
+        }
+        T[6 * k + g] = o[h];
+      }
+    }
+    f2[2 * p] = f[a];
+    f2[2 * p + 1] = f[b];
+  }
+  __syncthreads();
+  // stable descending order by the carried fitness; elites over the first
+  // slots (src/population.rs:110-118)
+  for (int k = tid; k < m; k += nt) {
+    const double fk = key_of(f2[k]);
+    int r = 0;
+    for (int q = 0; q < m; ++q) {
+      const double fq = key_of(f2[q]);
+      r += (fq > fk) || (fq == fk && q < k);
+    }
+    if (r >= ne) {
+      for (int g = 0; g < 6; ++g) G[6 * r + g] = T[6 * k + g];
+    }
+  }
+  for (int i = tid; i < ne * 6; i += nt) G[i] = s_eg[i];
+}
+
+}  // namespace
+}  // namespace gd
+
+using namespace gd;
+
+extern "C" {
+
+gd_status gd_ga_default_cfg(gd_ga_cfg *cfg) {
+  if (!cfg) return GD_ERR_INVALID_ARG;
+  // src/constants.rs:2-16 and src/chromosome.rs:64-71
+  *cfg = gd_ga_cfg{150, 5, 3, 0.6, 0.1, 50.0, 0.174, 1.0, 250, 1, 0.001, 10, 42};
+  return GD_OK;
+}
+
+gd_status gd_ga_draw(const gd_ga_cfg *cfg, uint64_t seed, int32_t generations, double *init_genes, int32_t *tour,
+                     int32_t *perm, double *cross_u, double *mut_u, double *mut_z) {
+  if (!cfg || generations < 0 || cfg->pop_size < 2 || cfg->tournament_size < 1) return GD_ERR_INVALID_ARG;
+  Rng rng(seed);
+  const int n = cfg->pop_size, m = 2 * (n / 2);
+  if (init_genes) draw_initial(rng, *cfg, init_genes);
+  GenDraws d;
+  for (int g = 0; g < generations; ++g) {
+    draw_generation(rng, *cfg, d);
+    if (tour) std::memcpy(tour + static_cast<size_t>(g) * cfg->tournament_size * n, d.tour.data(), sizeof(int) * d.tour.size());
+    if (perm) std::memcpy(perm + static_cast<size_t>(g) * n, d.perm.data(), sizeof(int) * n);
+    if (cross_u) std::memcpy(cross_u + static_cast<size_t>(g) * 6 * (n / 2), d.cross_u.data(), sizeof(double) * d.cross_u.size());
+    if (mut_u) std::memcpy(mut_u + static_cast<size_t>(g) * 6 * m, d.mut_u.data(), sizeof(double) * d.mut_u.size());
+    if (mut_z) std::memcpy(mut_z + static_cast<size_t>(g) * 6 * m, d.mut_z.data(), sizeof(double) * d.mut_z.size());
+  }
+  return GD_OK;
+}
+
+}  // extern "C"
+
+namespace gd {
+
+// Device buffers of a GA batch.
+struct GaRun {
+  int jobs = 0, n = 0, G = 0;
+  double *genes = nullptr, *genes_tmp = nullptr, *history = nullptr, *cross_u = nullptr, *mut_u = nullptr,
+         *mut_z = nullptr;
+  int *tour = nullptr, *perm = nullptr, *job_of = nullptr;
+  gd_pose_frame *frames = nullptr;
+  gd_pose_energy *energies = nullptr;
+  GaJobState *state = nullptr;
+  std::vector<std::pair<void *, size_t>> allocs;
+};
+
+static gd_status ga_alloc(gd_context *ctx, GaRun &R, size_t bytes, void **p) {
+  gd_status s = dev_alloc(ctx, bytes, p);
+  if (s == GD_OK) R.allocs.push_back({*p, bytes});
+  return s;
+}
+
+static void ga_release(gd_context *ctx, GaRun &R) {
+  for (auto &a : R.allocs) dev_free(ctx, a.first, a.second);
+  R.allocs.clear();
+}
+
+}  // namespace gd
+
+extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs, const gd_ga_cfg *cfg,
+                               gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
+                               int32_t *out_generations, double *out_history) {
+  using namespace gd;
+  if (!ctx) return GD_ERR_INVALID_ARG;
+  if (!complexes || jobs <= 0 || !cfg || !out_genes || !out_energies)
+    return fail(ctx, GD_ERR_INVALID_ARG, "bad GA arguments");
+  const gd_ga_cfg c = *cfg;
+  if (c.pop_size < 2 || c.pop_size % 2 || c.tournament_size < 1 || c.elitism < 0 || c.elitism > 64 ||
+      c.elitism > c.pop_size || c.max_generations < 0 || c.pop_size > 8192)
+    return fail(ctx, GD_ERR_INVALID_ARG, "GA config: even pop_size in [2, 8192], elitism <= 64");
+  if (prec != GD_PREC_F32 && prec != GD_PREC_F64) return fail(ctx, GD_ERR_INVALID_ARG, "bad precision");
+  for (int j = 0; j < jobs; ++j)
+    if (!complexes[j] || complexes[j]->ctx != ctx) return fail(ctx, GD_ERR_INVALID_ARG, "complex of another context");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  const int n = c.pop_size, m = n, G = c.max_generations;
+  GaRun R;
+  R.jobs = jobs;
+  R.n = n;
+  R.G = G;
+  // host draws: initial genes + every generation's randoms, per job
+  const size_t gT = static_cast<size_t>(c.tournament_size) * n, gC = 6 * static_cast<size_t>(n / 2), gM = 6 * static_cast<size_t>(m);
+  std::vector<double> h_genes(static_cast<size_t>(jobs) * n * 6);
+  std::vector<int> h_tour(static_cast<size_t>(jobs) * std::max(G, 1) * gT), h_perm(static_cast<size_t>(jobs) * std::max(G, 1) * n);
+  std::vector<double> h_cu(static_cast<size_t>(jobs) * std::max(G, 1) * gC), h_mu(static_cast<size_t>(jobs) * std::max(G, 1) * gM),
+      h_mz(static_cast<size_t>(jobs) * std::max(G, 1) * gM);
+  for (int j = 0; j < jobs; ++j) {
+    gd_ga_draw(&c, c.seed + static_cast<uint64_t>(j), G, &h_genes[static_cast<size_t>(j) * n * 6],
+               &h_tour[static_cast<size_t>(j) * G * gT], &h_perm[static_cast<size_t>(j) * G * n],
+               &h_cu[static_cast<size_t>(j) * G * gC], &h_mu[static_cast<size_t>(j) * G * gM],
+               &h_mz[static_cast<size_t>(j) * G * gM]);
+  }
+  std::vector<int> h_job(static_cast<size_t>(jobs) * n);
+  for (int j = 0; j < jobs; ++j)
+    for (int k = 0; k < n; ++k) h_job[static_cast<size_t>(j) * n + k] = j;
+  std::vector<GaJobState> h_state(jobs);
+  for (auto &s : h_state) s = GaJobState{0, 0, 0, 0, 1.7976931348623157e308};
+
+  auto up = [&](const void *src, size_t bytes, void **dst) -> gd_status {
+    gd_status s = ga_alloc(ctx, R, std::max<size_t>(bytes, 16), dst);
+    if (s != GD_OK) return s;
+    const cudaError_t ee = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    return ee == cudaSuccess ? GD_OK : cuda_fail(ctx, ee, "GA upload");
+  };
+  gd_status s;
+  void *p;
+  const size_t jn = static_cast<size_t>(jobs) * n;
+  if ((s = up(h_genes.data(), sizeof(double) * h_genes.size(), &p)) != GD_OK) goto done;
+  R.genes = static_cast<double *>(p);
+  if ((s = up(h_tour.data(), sizeof(int) * h_tour.size(), &p)) != GD_OK) goto done;
+  R.tour = static_cast<int *>(p);
+  if ((s = up(h_perm.data(), sizeof(int) * h_perm.size(), &p)) != GD_OK) goto done;
+  R.perm = static_cast<int *>(p);
+  if ((s = up(h_cu.data(), sizeof(double) * h_cu.size(), &p)) != GD_OK) goto done;
+  R.cross_u = static_cast<double *>(p);
+  if ((s = up(h_mu.data(), sizeof(double) * h_mu.size(), &p)) != GD_OK) goto done;
+  R.mut_u = static_cast<double *>(p);
+  if ((s = up(h_mz.data(), sizeof(double) * h_mz.size(), &p)) != GD_OK) goto done;
+  R.mut_z = static_cast<double *>(p);
+  if ((s = up(h_job.data(), sizeof(int) * h_job.size(), &p)) != GD_OK) goto done;
+  R.job_of = static_cast<int *>(p);
+  if ((s = up(h_state.data(), sizeof(GaJobState) * jobs, &p)) != GD_OK) goto done;
+  R.state = static_cast<GaJobState *>(p);
+  if ((s = ga_alloc(ctx, R, sizeof(double) * jn * 6, &p)) != GD_OK) goto done;
+  R.genes_tmp = static_cast<double *>(p);
+  if ((s = ga_alloc(ctx, R, sizeof(double) * static_cast<size_t>(jobs) * std::max(G, 1), &p)) != GD_OK) goto done;
+  R.history = static_cast<double *>(p);
+  if ((s = ga_alloc(ctx, R, sizeof(gd_pose_frame) * jn, &p)) != GD_OK) goto done;
+  R.frames = static_cast<gd_pose_frame *>(p);
+  if ((s = ga_alloc(ctx, R, sizeof(gd_pose_energy) * jn, &p)) != GD_OK) goto done;
+  R.energies = static_cast<gd_pose_energy *>(p);
+  {
+    // one scoring descriptor per job; poses outside [-M, M] never occur
+    std::vector<ScoreParams> descs;
+    bool serial = false, clamp = false;
+    for (int j = 0; j < jobs; ++j) {
+      ScoreParams d = make_params(complexes[j], R.frames + static_cast<size_t>(j) * n, nullptr, n,
+                                  R.energies + static_cast<size_t>(j) * n, c.max_displacement);
+      d.skip = &R.state[j].stop;
+      descs.push_back(d);
+      serial |= complexes[j]->serial_overlap;
+      clamp |= complexes[j]->need_clamp;
+    }
+    BatchLaunch *bl = nullptr;
+    if (prec == GD_PREC_F32) {
+      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 4, &bl);
+      if (s != GD_OK) goto done;
+    }
+    GaStepParams P{};
+    P.genes = R.genes;
+    P.genes_tmp = R.genes_tmp;
+    P.energies = R.energies;
+    P.state = R.state;
+    P.history = R.history;
+    P.tour = R.tour;
+    P.perm = R.perm;
+    P.cross_u = R.cross_u;
+    P.mut_u = R.mut_u;
+    P.mut_z = R.mut_z;
+    P.cfg = c;
+    const size_t ga_smem = sizeof(double) * (n + m) + sizeof(int) * (n + 64);
+    cudaStream_t st = ctx->stream;
+    auto generation = [&]() -> gd_status {
+      const int total = static_cast<int>(jn);
+      k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total);
+      cudaError_t ee = cudaGetLastError();
+      if (ee != cudaSuccess) return cuda_fail(ctx, ee, "frames kernel");
+      if (prec == GD_PREC_F32) {
+        gd_status ss = batch_launch(ctx, bl, st);
+        if (ss != GD_OK) return ss;
+      } else {
+        // plain form: one FP64 launch per job; finished jobs are skipped on
+        // the device by the GA step, so their scores stay final
+        for (int j = 0; j < jobs; ++j) {
+          gd_status ss = launch_score(complexes[j], descs[j].frames, nullptr, n, GD_PREC_F64, descs[j].out, st,
+                                      c.max_displacement);
+          if (ss != GD_OK) return ss;
+        }
+      }
+      k_ga_step<<<jobs, 256, ga_smem, st>>>(P);
+      ee = cudaGetLastError();
+      return ee == cudaSuccess ? GD_OK : cuda_fail(ctx, ee, "GA step kernel");
+    };
+    if (ga_smem > 48 * 1024) cudaFuncSetAttribute(k_ga_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  static_cast<int>(ga_smem));
+    const int iters = G + 1;  // G evolutions + the evaluation of the final population
+    if (use_graph && prec == GD_PREC_F32) {
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) {
+        s = cuda_fail(ctx, e, "begin graph capture");
+      } else {
+        s = generation();
+        e = cudaStreamEndCapture(st, &graph);
+        if (s == GD_OK && e != cudaSuccess) s = cuda_fail(ctx, e, "end graph capture");
+        if (s == GD_OK && (e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess)
+          s = cuda_fail(ctx, e, "graph instantiate");
+        for (int it = 0; s == GD_OK && it < iters; ++it)
+          if ((e = cudaGraphLaunch(exec, st)) != cudaSuccess) s = cuda_fail(ctx, e, "graph launch");
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+      }
+    } else {
+      for (int it = 0; s == GD_OK && it < iters; ++it) s = generation();
+    }
+    if (s == GD_OK) {
+      e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) s = cuda_fail(ctx, e, "GA run");
+    }
+    if (s == GD_OK) s = check_device_error(ctx);
+    if (bl) batch_free(ctx, bl);
+    if (s != GD_OK) goto done;
+  }
+  {
+    // results: the final population, its energies, generations and history
+    e = cudaMemcpy(out_genes, R.genes, sizeof(double) * jn * 6, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_energies, R.energies, sizeof(gd_pose_energy) * jn, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_state.data(), R.state, sizeof(GaJobState) * jobs, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && out_history && G > 0)
+      e = cudaMemcpy(out_history, R.history, sizeof(double) * jobs * G, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      s = cuda_fail(ctx, e, "GA results");
+      goto done;
+    }
+    if (out_generations)
+      for (int j = 0; j < jobs; ++j) out_generations[j] = h_state[j].gen;
+  }
+done:
+  ga_release(ctx, R);
+  return s;
+}

@@ -28,6 +28,13 @@ constexpr int kMaxTypes = 64;
 // device error codes written to the context's error word
 enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };
 
+// Per-job state of the device GA (the reference loop's counters,
+// src/commands/run.rs:371-425).  stop: 0 running, 1 converged, 2 done.
+struct GaJobState {
+  int gen, stop, stagnant, pad;
+  double last_best;
+};
+
 // Per-pair parameters of one type pair, FP32 form: R6 = (Rmin_i + Rmin_j)^6,
 // eps = sqrt(eps_i eps_j).
 struct TypePair32 { float r6, eps; };
@@ -78,6 +85,7 @@ struct ScoreParams {
   int n_poses;
   gd_pose_energy *out;
   int *err;
+  const int *skip;          // when non-null and nonzero, the complex's poses are not scored
 };
 
 }  // namespace gd
@@ -153,4 +161,9 @@ ScoreParams make_params(gd_complex *cx, const gd_pose_frame *d_frames, const dou
                         gd_pose_energy *d_out, double max_disp);
 gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
                                  int slots, cudaStream_t stream);
+struct BatchLaunch;
+gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp, int slots,
+                        BatchLaunch **out);
+gd_status batch_launch(gd_context *ctx, BatchLaunch *b, cudaStream_t stream);
+void batch_free(gd_context *ctx, BatchLaunch *b);
 }  // namespace gd

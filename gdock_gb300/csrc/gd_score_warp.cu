@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams
     }
     __syncwarp();
     const ScoreParams &p = *s_desc;
+    if (p.skip && *p.skip) continue;  // this complex is finished (e.g. a converged GA job)
     if (!p.models && lane < 16)
       reinterpret_cast<double *>(s_frame)[lane] = reinterpret_cast<const double *>(p.frames + pose)[lane];
     __syncwarp();
@@ -573,6 +574,89 @@ gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams>
                    stream);
 }
 
+
+// A batched scoring launch whose argument block is uploaded once and whose
+// launch (work-counter reset + kernel) can be replayed, e.g. inside a
+// captured CUDA graph.
+struct BatchLaunch {
+  BatchPlan plan;
+  bool serial = false, clamp = false;
+  char *d_arg = nullptr;
+  size_t bytes = 0, gstride = 0;
+  int ncx = 0;
+};
+
+gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp, int slots,
+                        BatchLaunch **out) {
+  *out = nullptr;
+  BatchLaunch *b = new BatchLaunch();
+  b->serial = serial;
+  b->clamp = clamp;
+  b->ncx = static_cast<int>(descs.size());
+  gd_status s = plan_batch(ctx, descs, serial, clamp, slots, &b->plan);
+  if (s != GD_OK) {
+    delete b;
+    return s;
+  }
+  b->gstride = b->plan.smem_cnt ? 0 : ((b->plan.max_nr + 127) / 128) * 128;
+  b->bytes = arg_bytes(b->ncx) + b->gstride * static_cast<size_t>(b->plan.grid) * kWarps;
+  void *p = nullptr;
+  s = dev_alloc(ctx, b->bytes, &p);
+  if (s != GD_OK) {
+    delete b;
+    return s;
+  }
+  b->d_arg = static_cast<char *>(p);
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t db = sizeof(ScoreParams) * b->ncx, sb = sizeof(long long) * (b->ncx + 1);
+  std::vector<char> h(al(db) + sb);
+  std::memcpy(h.data(), descs.data(), db);
+  std::memcpy(h.data() + al(db), b->plan.start.data(), sb);
+  const cudaError_t e = cudaMemcpy(b->d_arg, h.data(), h.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    batch_free(ctx, b);
+    return cuda_fail(ctx, e, "batched scoring arguments");
+  }
+  *out = b;
+  return GD_OK;
+}
+
+gd_status batch_launch(gd_context *ctx, BatchLaunch *b, cudaStream_t stream) {
+  if (b->plan.start[b->ncx] == 0) return GD_OK;
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t db = sizeof(ScoreParams) * b->ncx, sb = sizeof(long long) * (b->ncx + 1);
+  char *arg = b->d_arg;
+  unsigned long long *d_queue = reinterpret_cast<unsigned long long *>(arg + al(db) + al(sb));
+  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring queue reset");
+  BatchParams bp{};
+  bp.descs = reinterpret_cast<const ScoreParams *>(arg);
+  bp.item_start = reinterpret_cast<const long long *>(arg + al(db));
+  bp.ncx = b->ncx;
+  bp.total = b->plan.start[b->ncx];
+  bp.queue = d_queue;
+  bp.gcounts = reinterpret_cast<uint8_t *>(arg + arg_bytes(b->ncx));
+  bp.gcount_stride = static_cast<int>(b->gstride);
+  bp.smem_cnt = b->plan.smem_cnt;
+  bp.max_nr = b->plan.max_nr;
+  bp.warp_smem = static_cast<int>(warp_layout(b->plan.smem_cnt).total);
+  bp.err = ctx->d_err;
+  const BatchPlan &pl = b->plan;
+  switch (pl.S) {
+    case 2: e = launch_w<2>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
+    case 4: e = launch_w<4>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
+    case 6: e = launch_w<6>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
+    default: e = launch_w<8>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
+  return GD_OK;
+}
+
+void batch_free(gd_context *ctx, BatchLaunch *b) {
+  if (!b) return;
+  if (b->d_arg) dev_free(ctx, b->d_arg, b->bytes);
+  delete b;
+}
 
 // ---------------------------------------------------------------------------
 // Scoring without any device allocation.

@@ -186,6 +186,44 @@ gd_status gd_cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *o
                           const gd_cluster_cfg *cfg, int32_t *n_clusters, int32_t *centers,
                           int32_t *sizes, int32_t *members);
 
+/* ----------------------------------------------------------------- GA --
+ * gdock's generation loop (src/commands/run.rs:381-531: evaluate, track the
+ * best, stop after convergence_window stagnant generations, evolve) with
+ * Population::evolve (src/population.rs:74-121) on the GPU, for many jobs at
+ * once.  The random draws of each generation are made on the host in the
+ * reference's order from a seeded xoshiro256** stream (not rand's StdRng). */
+typedef struct gd_ga_cfg {
+  int32_t pop_size;             /* POPULATION_SIZE (150); even */
+  int32_t elitism;              /* ELITISM_COUNT (5) */
+  int32_t tournament_size;      /* TOURNAMENT_SIZE (3) */
+  double crossover_rate;        /* CROSSOVER_RATE (0.6) */
+  double mutation_rate;         /* MUTATION_RATE (0.1) */
+  double max_displacement;      /* MAX_DISPLACEMENT (50 A) */
+  double rot_sigma;             /* creep sigma of the angles (0.174 rad) */
+  double trans_sigma;           /* creep sigma of the displacement (1 A) */
+  int32_t max_generations;      /* MAX_GENERATIONS (250) */
+  int32_t early_stopping;       /* ENABLE_EARLY_STOPPING (1) */
+  double convergence_threshold; /* CONVERGENCE_THRESHOLD (0.001) */
+  int32_t convergence_window;   /* CONVERGENCE_WINDOW (10) */
+  uint64_t seed;                /* job j uses seed + j */
+} gd_ga_cfg;
+
+/* The reference's constants (src/constants.rs:2-16, src/chromosome.rs:64-71). */
+gd_status gd_ga_default_cfg(gd_ga_cfg *cfg);
+/* The host draws of one job: initial genes (pop_size x 6) and, per
+ * generation, tournament indices, the shuffled order, crossover and mutation
+ * uniforms and the mutation perturbations (any pointer may be NULL). */
+gd_status gd_ga_draw(const gd_ga_cfg *cfg, uint64_t seed, int32_t generations, double *init_genes, int32_t *tour,
+                     int32_t *perm, double *cross_u, double *mut_u, double *mut_z);
+/* Run the GA of `jobs` complexes to completion on the device; with
+ * use_graph (FP32 form) one generation is a captured CUDA graph replayed.
+ * Outputs: final populations (jobs x pop x 6), their energies
+ * (jobs x pop), generations evolved per job, best fitness per generation
+ * (jobs x max_generations, may be NULL). */
+gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs, const gd_ga_cfg *cfg,
+                    gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
+                    int32_t *out_generations, double *out_history);
+
 #ifdef __cplusplus
 }
 #endif

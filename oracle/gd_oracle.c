@@ -561,3 +561,93 @@ int32_t orc_cluster(const int64_t *keys, const int64_t *offsets, int32_t n, doub
   free(mem);
   return kept;
 }
+
+/* ------------------------------------------------------------------ GA -- */
+
+/* stable ascending order of fitness (slice::sort_by with partial_cmp) */
+static void stable_order(int32_t n, const double *f, int descending, int32_t *order) {
+  for (int32_t i = 0; i < n; i++) order[i] = i;
+  /* insertion sort: stable */
+  for (int32_t i = 1; i < n; i++) {
+    int32_t v = order[i], j = i - 1;
+    while (j >= 0 && (descending ? (f[order[j]] < f[v]) : (f[order[j]] > f[v]))) {
+      order[j + 1] = order[j];
+      j--;
+    }
+    order[j + 1] = v;
+  }
+}
+
+void orc_evolve(int32_t n, const double *genes, const double *fitness, int32_t elitism,
+                const int32_t *tour, int32_t tour_size, const int32_t *perm, const double *cross_u,
+                double crossover_rate, const double *mut_u, const double *mut_z, double mutation_rate,
+                double max_displacement, double *genes_out, double *fit_out) {
+  const double TWO_PI = 2.0 * PI_F64;
+  int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  int32_t *sel = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  /* elitism: stable sort ascending, take the first `elitism` (:76-82) */
+  stable_order(n, fitness, 0, order);
+  int32_t ne = elitism < n ? elitism : n;
+  int32_t elite[64];
+  for (int32_t i = 0; i < ne && i < 64; i++) elite[i] = order[i];
+  /* tournament: the first minimum of tour_size draws (:136-156) */
+  for (int32_t k = 0; k < n; k++) {
+    int32_t best = tour[tour_size * k];
+    for (int32_t t = 1; t < tour_size; t++) {
+      int32_t c = tour[tour_size * k + t];
+      if (fitness[best] > fitness[c]) best = c;
+    }
+    sel[k] = best;
+  }
+  /* shuffle then pairwise crossover; an odd last individual is dropped (:88-99) */
+  int32_t m = 2 * (n / 2);
+  double *g2 = (double *)malloc(sizeof(double) * 6 * (size_t)(m > 0 ? m : 1));
+  double *f2 = (double *)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
+  for (int32_t p = 0; p < n / 2; p++) {
+    int32_t a = sel[perm[2 * p]], b = sel[perm[2 * p + 1]];
+    for (int32_t g = 0; g < 6; g++) {
+      double ga = genes[6 * a + g], gb = genes[6 * b + g];
+      if (cross_u[6 * p + g] <= crossover_rate) {
+        g2[6 * (2 * p) + g] = gb;
+        g2[6 * (2 * p + 1) + g] = ga;
+      } else {
+        g2[6 * (2 * p) + g] = ga;
+        g2[6 * (2 * p + 1) + g] = gb;
+      }
+    }
+    f2[2 * p] = fitness[a];
+    f2[2 * p + 1] = fitness[b];
+  }
+  /* creep mutation (src/chromosome.rs:56-77) */
+  for (int32_t k = 0; k < m; k++) {
+    for (int32_t g = 0; g < 6; g++) {
+      if (mut_u[6 * k + g] <= mutation_rate) {
+        double v = g2[6 * k + g] + mut_z[6 * k + g];
+        if (g < 3) {
+          double r = fmod(v, TWO_PI); /* f64::rem_euclid */
+          if (r < 0.0) r = r + fabs(TWO_PI);
+          v = r;
+        } else {
+          if (v < -max_displacement) v = -max_displacement;
+          if (v > max_displacement) v = max_displacement;
+        }
+        g2[6 * k + g] = v;
+      }
+    }
+  }
+  /* stable sort descending by the carried fitness, elites over the first
+   * slots (:110-118) */
+  stable_order(m, f2, 1, order);
+  for (int32_t k = 0; k < m; k++) {
+    for (int32_t g = 0; g < 6; g++) genes_out[6 * k + g] = g2[6 * order[k] + g];
+    fit_out[k] = f2[order[k]];
+  }
+  for (int32_t i = 0; i < ne && i < m; i++) {
+    for (int32_t g = 0; g < 6; g++) genes_out[6 * i + g] = genes[6 * elite[i] + g];
+    fit_out[i] = fitness[elite[i]];
+  }
+  free(order);
+  free(sel);
+  free(g2);
+  free(f2);
+}

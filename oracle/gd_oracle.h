@@ -76,6 +76,20 @@ int32_t orc_cluster(const int64_t *keys, const int64_t *offsets, int32_t n, doub
 /* pairwise FCC values (n*n, row i col j) */
 void orc_pairwise_fcc(const int64_t *keys, const int64_t *offsets, int32_t n, double *fcc, double *fcc_v);
 
+/* Population::evolve (src/population.rs:74-121) with every random draw given
+ * explicitly, in the order the reference consumes them:
+ *   tour[3n]      tournament indices (tournament_selection, :124-158)
+ *   perm[n]       the shuffled order: shuffled[k] = selected[perm[k]] (:88)
+ *   cross_u[6(n/2)] uniform draws of ga::crossover (src/ga.rs:7-39)
+ *   mut_u[6m], mut_z[6m] uniform draws of Chromosome::mutate and the normal
+ *                 perturbation drawn when one triggers (src/chromosome.rs:56-77),
+ *                 m = 2(n/2).
+ * genes_out/fit_out receive m individuals (genes and the stale fitness the
+ * reference carries), elites written over the first `elitism` slots. */
+void orc_evolve(int32_t n, const double *genes, const double *fitness, int32_t elitism,
+                const int32_t *tour, int32_t tour_size, const int32_t *perm, const double *cross_u,
+                double crossover_rate, const double *mut_u, const double *mut_z, double mutation_rate,
+                double max_displacement, double *genes_out, double *fit_out);
 #ifdef __cplusplus
 }
 #endif

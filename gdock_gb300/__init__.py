@@ -30,7 +30,7 @@ __all__ = [
     "Context", "Complex", "GdError", "GD_PREC_F32", "GD_PREC_F64", "EnergyWeights", "ClusteringConfig",
     "ClusterResult", "vdw_energy", "elec_energy", "desolv_energy", "air_energy", "satisfaction_ratio",
     "cluster_sets", "make_frames", "Molecule", "read_pdb", "read_pdb_text", "position_ligand",
-    "combine_molecules", "default_context", "ga_default_cfg", "ga_draw", "run_ga", "GaResult",
+    "combine_molecules", "default_context", "ga_default_cfg", "ga_draw", "run_ga", "GaResult", "Server",
 ]
 
 
@@ -235,3 +235,78 @@ def run_ga(complexes: Sequence[Complex], cfg=None, precision=GD_PREC_F32, use_gr
     ctx.check(ctx.lib.gd_ga_run(ctx.h, C.cast(handles, C.c_void_p), J, C.byref(cfg), _prec(precision),
                                 1 if use_graph else 0, ptr(genes), ptr(energies), ptr(gens), ptr(hist)))
     return GaResult(genes, energies, gens, hist[:, :G])
+
+
+class Server:
+    """The serving loop (gd_server): docking jobs admitted into resident slots
+    by HBM budget and advanced together, one generation per tick."""
+
+    def __init__(self, ctx: Optional[Context] = None, max_slots: int = 64, hbm_budget: int = 0, ga=None,
+                 precision=GD_PREC_F32):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        cfg = _lib.GdServerCfg()
+        self.lib.gd_server_default_cfg(C.byref(cfg))
+        cfg.max_slots = max_slots
+        cfg.hbm_budget = hbm_budget
+        if ga is not None:
+            cfg.ga = ga
+        cfg.precision = _prec(precision)
+        self.cfg = cfg
+        h = C.c_void_p()
+        self.ctx.check(self.lib.gd_server_create(self.ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def submit(self, receptor: Molecule, ligand: Molecule, restraint_pairs=(), seed: int = 42,
+               weights: EnergyWeights = EnergyWeights()) -> int:
+        r, l = PackedAtoms(receptor), PackedAtoms(ligand)
+        pairs = np.ascontiguousarray(np.asarray(list(restraint_pairs), dtype=np.int32).reshape(-1, 2))
+        w = _lib.GdWeights(weights.vdw, weights.elec, weights.desolv, weights.air)
+        jid = C.c_int64()
+        self.ctx.check(self.lib.gd_server_submit(self.h, C.byref(r.s), C.byref(l.s), ptr(pairs) if pairs.size else None,
+                                                 pairs.shape[0], C.byref(w), seed, C.byref(jid)))
+        return jid.value
+
+    def step(self) -> int:
+        a = C.c_int32()
+        self.ctx.check(self.lib.gd_server_step(self.h, C.byref(a)))
+        return a.value
+
+    def start(self):
+        self.ctx.check(self.lib.gd_server_start(self.h))
+
+    def stop(self):
+        self.ctx.check(self.lib.gd_server_stop(self.h))
+
+    def wait(self, job: int, timeout_s: float = 600.0) -> int:
+        st = C.c_int32()
+        self.lib.gd_server_wait(self.h, job, timeout_s, C.byref(st))
+        return st.value
+
+    def result(self, job: int):
+        n, G = self.cfg.ga.pop_size, max(self.cfg.ga.max_generations, 1)
+        res = _lib.GdJobResult()
+        genes = np.zeros((n, 6))
+        energies = np.zeros(n, dtype=POSE_ENERGY_DTYPE)
+        hist = np.zeros(G)
+        self.ctx.check(self.lib.gd_server_result(self.h, job, C.byref(res), ptr(genes), ptr(energies), ptr(hist)))
+        return res, genes, energies, hist[: self.cfg.ga.max_generations]
+
+    def release(self, job: int):
+        self.ctx.check(self.lib.gd_server_release(self.h, job))
+
+    def stats(self) -> "_lib.GdServerStats":
+        s = _lib.GdServerStats()
+        self.ctx.check(self.lib.gd_server_get_stats(self.h, C.byref(s)))
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gd_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

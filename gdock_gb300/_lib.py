@@ -23,7 +23,11 @@ EXPORTS = (
     "gd_complex_set_weights", "gd_make_frames", "gd_score_poses", "gd_score_frames_device", "gd_sync",
     "gd_score_models", "gd_pose_contacts", "gd_cluster", "gd_cluster_sets", "gd_context_set_tuning",
     "gd_context_get_tuning", "gd_score_frames_device_noalloc", "gd_ga_default_cfg", "gd_ga_draw", "gd_ga_run",
+    "gd_server_default_cfg", "gd_server_create", "gd_server_destroy", "gd_server_submit", "gd_server_step",
+    "gd_server_start", "gd_server_stop", "gd_server_wait", "gd_server_result", "gd_server_release",
+    "gd_server_get_stats",
 )
+GD_JOB_QUEUED, GD_JOB_RUNNING, GD_JOB_DONE, GD_JOB_FAILED = range(4)
 GD_TUNE_F32_SLOTS = 0
 
 
@@ -49,6 +53,21 @@ class GdGaCfg(C.Structure):
                 ("rot_sigma", C.c_double), ("trans_sigma", C.c_double), ("max_generations", C.c_int32),
                 ("early_stopping", C.c_int32), ("convergence_threshold", C.c_double),
                 ("convergence_window", C.c_int32), ("seed", C.c_uint64)]
+
+
+class GdServerCfg(C.Structure):
+    _fields_ = [("max_slots", C.c_int32), ("hbm_budget", C.c_uint64), ("ga", GdGaCfg), ("precision", C.c_int32)]
+
+
+class GdJobResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("error", C.c_int32), ("generations", C.c_int32),
+                ("latency_s", C.c_double), ("queue_s", C.c_double)]
+
+
+class GdServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("queued", C.c_int64), ("resident", C.c_int64),
+                ("generations_run", C.c_int64), ("poses_scored", C.c_int64), ("device_bytes", C.c_uint64),
+                ("latency_p50_s", C.c_double), ("latency_p99_s", C.c_double), ("latency_max_s", C.c_double)]
 
 
 POSE_ENERGY_DTYPE = np.dtype([(k, np.float64) for k in
@@ -99,6 +118,18 @@ def load(path: Path = LIB_PATH):
         "gd_ga_default_cfg": ([C.POINTER(GdGaCfg)], C.c_int),
         "gd_ga_draw": ([C.POINTER(GdGaCfg), C.c_uint64, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "gd_ga_run": ([vp, vp, i32, C.POINTER(GdGaCfg), C.c_int, i32, vp, vp, vp, vp], C.c_int),
+        "gd_server_default_cfg": ([C.POINTER(GdServerCfg)], C.c_int),
+        "gd_server_create": ([vp, C.POINTER(GdServerCfg), C.POINTER(vp)], C.c_int),
+        "gd_server_destroy": ([vp], C.c_int),
+        "gd_server_submit": ([vp, C.POINTER(GdAtoms), C.POINTER(GdAtoms), vp, i32, C.POINTER(GdWeights),
+                              C.c_uint64, C.POINTER(i64)], C.c_int),
+        "gd_server_step": ([vp, C.POINTER(i32)], C.c_int),
+        "gd_server_start": ([vp], C.c_int),
+        "gd_server_stop": ([vp], C.c_int),
+        "gd_server_wait": ([vp, i64, d, C.POINTER(i32)], C.c_int),
+        "gd_server_result": ([vp, i64, C.POINTER(GdJobResult), vp, vp, vp], C.c_int),
+        "gd_server_release": ([vp, i64], C.c_int),
+        "gd_server_get_stats": ([vp, C.POINTER(GdServerStats)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)

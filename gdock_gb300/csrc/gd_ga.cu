@@ -504,3 +504,528 @@ done:
   ga_release(ctx, R);
   return s;
 }
+
+// =========================================================================
+// Serving loop: docking jobs admitted into resident slots by HBM budget,
+// all resident jobs advanced one generation per tick in shared launches.
+// =========================================================================
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+
+namespace gd {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct HostMol {
+  std::vector<double> x, y, z, eps, rmin2, q, r;
+  std::vector<int32_t> serial;
+  std::vector<int16_t> resseq;
+  std::vector<uint8_t> chain, elem, ca;
+  void copy(const gd_atoms *a) {
+    const int n = a->n;
+    x.assign(a->x, a->x + n);
+    y.assign(a->y, a->y + n);
+    z.assign(a->z, a->z + n);
+    eps.assign(a->epsilon, a->epsilon + n);
+    rmin2.assign(a->rmin2, a->rmin2 + n);
+    q.assign(a->charge, a->charge + n);
+    r.assign(a->vdw_radius, a->vdw_radius + n);
+    serial.assign(a->serial, a->serial + n);
+    resseq.assign(a->resseq, a->resseq + n);
+    chain.assign(a->chain, a->chain + n);
+    elem.assign(a->element, a->element + n);
+    ca.assign(a->is_ca, a->is_ca + n);
+  }
+  gd_atoms view() const {
+    return gd_atoms{static_cast<int32_t>(x.size()), x.data(), y.data(), z.data(), eps.data(), rmin2.data(),
+                    q.data(), r.data(), serial.data(), resseq.data(), chain.data(), elem.data(), ca.data()};
+  }
+};
+
+struct Job {
+  int64_t id = 0;
+  HostMol rec, lig;
+  std::vector<int32_t> pairs;
+  gd_weights w{};
+  uint64_t seed = 0;
+  int status = GD_JOB_QUEUED;
+  Clock::time_point t_submit, t_admit, t_done;
+  gd_complex *cx = nullptr;
+  int slot = -1;
+  int generations = 0;
+  std::vector<double> genes, history;
+  std::vector<gd_pose_energy> energies;
+  int error = GD_OK;
+};
+
+}  // namespace
+}  // namespace gd
+
+struct gd_server {
+  gd_context *ctx = nullptr;
+  gd_server_cfg cfg{};
+  gd::GaRun arena;  // max_slots "jobs" worth of device buffers
+  std::vector<gd::Job *> slot_job;
+  gd::BatchLaunch *bl = nullptr;
+  uint64_t job_bytes = 0;  // device bytes held by resident complexes
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<gd::Job *> queue;
+  std::map<int64_t, gd::Job *> jobs;
+  int64_t next_id = 1;
+  std::thread worker;
+  bool running = false;
+  // statistics
+  int64_t completed = 0, poses_scored = 0, generations_run = 0;
+  std::vector<double> latencies;
+  gd::Clock::time_point t_first;
+  bool started_clock = false;
+};
+
+namespace gd {
+namespace {
+
+constexpr int kStopFree = 3;  // slot without a job
+
+gd_status server_alloc(gd_server *S) {
+  gd_context *ctx = S->ctx;
+  const gd_ga_cfg &c = S->cfg.ga;
+  GaRun &R = S->arena;
+  const int J = S->cfg.max_slots, n = c.pop_size, G = std::max(c.max_generations, 1);
+  R.jobs = J;
+  R.n = n;
+  R.G = c.max_generations;
+  const size_t jn = static_cast<size_t>(J) * n;
+  void *p;
+  gd_status s;
+  auto A = [&](size_t bytes, void **out) { return ga_alloc(ctx, R, std::max<size_t>(bytes, 16), out); };
+  if ((s = A(sizeof(double) * jn * 6, &p)) != GD_OK) return s;
+  R.genes = static_cast<double *>(p);
+  if ((s = A(sizeof(double) * jn * 6, &p)) != GD_OK) return s;
+  R.genes_tmp = static_cast<double *>(p);
+  if ((s = A(sizeof(double) * static_cast<size_t>(J) * G, &p)) != GD_OK) return s;
+  R.history = static_cast<double *>(p);
+  if ((s = A(sizeof(int) * jn * c.tournament_size * G, &p)) != GD_OK) return s;
+  R.tour = static_cast<int *>(p);
+  if ((s = A(sizeof(int) * jn * G, &p)) != GD_OK) return s;
+  R.perm = static_cast<int *>(p);
+  if ((s = A(sizeof(double) * static_cast<size_t>(J) * 6 * (n / 2) * G, &p)) != GD_OK) return s;
+  R.cross_u = static_cast<double *>(p);
+  if ((s = A(sizeof(double) * jn * 6 * G, &p)) != GD_OK) return s;
+  R.mut_u = static_cast<double *>(p);
+  if ((s = A(sizeof(double) * jn * 6 * G, &p)) != GD_OK) return s;
+  R.mut_z = static_cast<double *>(p);
+  if ((s = A(sizeof(gd_pose_frame) * jn, &p)) != GD_OK) return s;
+  R.frames = static_cast<gd_pose_frame *>(p);
+  if ((s = A(sizeof(gd_pose_energy) * jn, &p)) != GD_OK) return s;
+  R.energies = static_cast<gd_pose_energy *>(p);
+  if ((s = A(sizeof(GaJobState) * J, &p)) != GD_OK) return s;
+  R.state = static_cast<GaJobState *>(p);
+  if ((s = A(sizeof(int) * jn, &p)) != GD_OK) return s;
+  R.job_of = static_cast<int *>(p);
+  std::vector<int> job_of(jn);
+  for (size_t k = 0; k < jn; ++k) job_of[k] = static_cast<int>(k / n);
+  std::vector<GaJobState> st(J, GaJobState{0, kStopFree, 0, 0, 0.0});
+  cudaError_t e = cudaMemcpy(R.job_of, job_of.data(), sizeof(int) * jn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(R.state, st.data(), sizeof(GaJobState) * J, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "server arena");
+  S->slot_job.assign(J, nullptr);
+  return GD_OK;
+}
+
+// Upload a job's draws and initial state into slot j.
+gd_status server_load_slot(gd_server *S, int j, Job *job) {
+  const gd_ga_cfg &c = S->cfg.ga;
+  GaRun &R = S->arena;
+  const int n = c.pop_size, m = n, G = c.max_generations;
+  const size_t gT = static_cast<size_t>(c.tournament_size) * n, gC = 6 * static_cast<size_t>(n / 2),
+               gM = 6 * static_cast<size_t>(m);
+  std::vector<double> genes(static_cast<size_t>(n) * 6), cu(gC * std::max(G, 1)), mu(gM * std::max(G, 1)),
+      mz(gM * std::max(G, 1));
+  std::vector<int> tour(gT * std::max(G, 1)), perm(static_cast<size_t>(n) * std::max(G, 1));
+  gd_ga_draw(&c, job->seed, G, genes.data(), tour.data(), perm.data(), cu.data(), mu.data(), mz.data());
+  const size_t Gs = static_cast<size_t>(G);
+  cudaStream_t st = S->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(R.genes + static_cast<size_t>(j) * n * 6, genes.data(), sizeof(double) * genes.size(),
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && G > 0) {
+    e = cudaMemcpyAsync(R.tour + j * Gs * gT, tour.data(), sizeof(int) * gT * Gs, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(R.perm + j * Gs * n, perm.data(), sizeof(int) * n * Gs, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(R.cross_u + j * Gs * gC, cu.data(), sizeof(double) * gC * Gs, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(R.mut_u + j * Gs * gM, mu.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(R.mut_z + j * Gs * gM, mz.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice, st);
+  }
+  GaJobState s0{0, 0, 0, 0, 1.7976931348623157e308};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(R.state + j, &s0, sizeof(s0), cudaMemcpyHostToDevice, st);
+  // pageable sources: staged before the calls return
+  if (e != cudaSuccess) return cuda_fail(S->ctx, e, "server slot upload");
+  return GD_OK;
+}
+
+// One tick: admit, run one generation of every resident job, retire.
+gd_status server_tick(gd_server *S, int *active_out) {
+  gd_context *ctx = S->ctx;
+  const gd_ga_cfg &c = S->cfg.ga;
+  GaRun &R = S->arena;
+  const int J = S->cfg.max_slots, n = c.pop_size;
+  gd_status s = GD_OK;
+  // 1. admission: FIFO into free slots while the HBM budget allows
+  for (;;) {
+    int free_slot = -1;
+    for (int j = 0; j < J; ++j)
+      if (!S->slot_job[j]) {
+        free_slot = j;
+        break;
+      }
+    Job *job = nullptr;
+    {
+      std::lock_guard<std::mutex> lock(S->mu);
+      if (free_slot < 0 || S->queue.empty()) break;
+      job = S->queue.front();
+    }
+    const gd_atoms ra = job->rec.view(), la = job->lig.view();
+    gd_complex *cx = nullptr;
+    const uint64_t before = ctx->in_use;
+    s = gd_complex_create(ctx, &ra, &la, job->pairs.empty() ? nullptr : job->pairs.data(),
+                          static_cast<int32_t>(job->pairs.size() / 2), &job->w, &cx);
+    if (s == GD_ERR_OOM) break;  // wait for a resident job to finish
+    const uint64_t bytes = ctx->in_use - before;
+    if (s == GD_OK && S->cfg.hbm_budget && S->job_bytes + bytes > S->cfg.hbm_budget && S->job_bytes > 0) {
+      gd_complex_destroy(cx);  // over the server's budget: admit later
+      break;
+    }
+    {
+      std::lock_guard<std::mutex> lock(S->mu);
+      S->queue.pop_front();
+      if (s != GD_OK) {
+        job->status = GD_JOB_FAILED;
+        job->error = s;
+        job->t_done = Clock::now();
+        S->cv.notify_all();
+        continue;
+      }
+      job->cx = cx;
+      job->slot = free_slot;
+      job->status = GD_JOB_RUNNING;
+      job->t_admit = Clock::now();
+      S->slot_job[free_slot] = job;
+    }
+    S->job_bytes += bytes;
+    s = server_load_slot(S, free_slot, job);
+    if (s != GD_OK) return s;
+  }
+  int active = 0;
+  for (Job *j : S->slot_job) active += j != nullptr;
+  if (active_out) *active_out = active;
+  if (active == 0) return GD_OK;
+  // 2. one generation for all resident jobs
+  std::vector<ScoreParams> descs(J);
+  bool serial = false, clamp = false;
+  for (int j = 0; j < J; ++j) {
+    Job *job = S->slot_job[j];
+    if (job) {
+      descs[j] = make_params(job->cx, R.frames + static_cast<size_t>(j) * n, nullptr, n,
+                             R.energies + static_cast<size_t>(j) * n, c.max_displacement);
+      descs[j].skip = &R.state[j].stop;
+      serial |= job->cx->serial_overlap;
+      clamp |= job->cx->need_clamp;
+    } else {
+      descs[j] = ScoreParams{};
+      descs[j].n_poses = 0;
+    }
+  }
+  cudaStream_t st = ctx->stream;
+  const int total = J * n;
+  k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "frames kernel");
+  if (S->cfg.precision == GD_PREC_F32) {
+    if (S->bl) batch_free(ctx, S->bl);
+    S->bl = nullptr;
+    s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 4, &S->bl);
+    if (s == GD_OK) s = batch_launch(ctx, S->bl, st);
+  } else {
+    for (int j = 0; j < J && s == GD_OK; ++j)
+      if (S->slot_job[j])
+        s = launch_score(S->slot_job[j]->cx, descs[j].frames, nullptr, n, GD_PREC_F64, descs[j].out, st,
+                         c.max_displacement);
+  }
+  if (s != GD_OK) return s;
+  GaStepParams P{};
+  P.genes = R.genes;
+  P.genes_tmp = R.genes_tmp;
+  P.energies = R.energies;
+  P.state = R.state;
+  P.history = R.history;
+  P.tour = R.tour;
+  P.perm = R.perm;
+  P.cross_u = R.cross_u;
+  P.mut_u = R.mut_u;
+  P.mut_z = R.mut_z;
+  P.cfg = c;
+  const size_t ga_smem = sizeof(double) * 2 * n + sizeof(int) * (n + 64);
+  if (ga_smem > 48 * 1024)
+    cudaFuncSetAttribute(k_ga_step, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ga_smem));
+  k_ga_step<<<J, 256, ga_smem, st>>>(P);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "GA step kernel");
+  std::vector<GaJobState> states(J);
+  e = cudaMemcpyAsync(states.data(), R.state, sizeof(GaJobState) * J, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "server tick");
+  s = check_device_error(ctx);
+  if (s != GD_OK) return s;
+  S->generations_run += 1;
+  S->poses_scored += static_cast<int64_t>(active) * n;
+  // 3. retire finished jobs
+  for (int j = 0; j < J; ++j) {
+    Job *job = S->slot_job[j];
+    if (!job || states[j].stop == 0) continue;
+    job->generations = states[j].gen;
+    job->genes.resize(static_cast<size_t>(n) * 6);
+    job->energies.resize(n);
+    job->history.resize(std::max(c.max_generations, 0));
+    e = cudaMemcpy(job->genes.data(), R.genes + static_cast<size_t>(j) * n * 6, sizeof(double) * n * 6,
+                   cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(job->energies.data(), R.energies + static_cast<size_t>(j) * n, sizeof(gd_pose_energy) * n,
+                     cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && c.max_generations > 0)
+      e = cudaMemcpy(job->history.data(), R.history + static_cast<size_t>(j) * c.max_generations,
+                     sizeof(double) * c.max_generations, cudaMemcpyDeviceToHost);
+    GaJobState freed{0, kStopFree, 0, 0, 0.0};
+    if (e == cudaSuccess) e = cudaMemcpy(R.state + j, &freed, sizeof(freed), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "server retire");
+    const uint64_t before = ctx->in_use;
+    gd_complex_destroy(job->cx);
+    S->job_bytes -= std::min<uint64_t>(S->job_bytes, before - ctx->in_use);
+    job->cx = nullptr;
+    // history entries past the generations this job ran are not its own
+    const int valid = std::min(c.max_generations, states[j].stop == 1 ? states[j].gen + 1 : states[j].gen);
+    for (int g = std::max(valid, 0); g < c.max_generations; ++g) job->history[g] = NAN;
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->slot_job[j] = nullptr;
+    job->status = GD_JOB_DONE;
+    job->t_done = Clock::now();
+    S->completed += 1;
+    S->latencies.push_back(std::chrono::duration<double>(job->t_done - job->t_submit).count());
+    S->cv.notify_all();
+  }
+  return GD_OK;
+}
+
+}  // namespace
+}  // namespace gd
+
+using gd::Clock;
+
+extern "C" {
+
+gd_status gd_server_default_cfg(gd_server_cfg *cfg) {
+  if (!cfg) return GD_ERR_INVALID_ARG;
+  cfg->max_slots = 64;
+  cfg->hbm_budget = 0;
+  gd_ga_default_cfg(&cfg->ga);
+  cfg->ga.max_generations = 200;
+  cfg->precision = GD_PREC_F32;
+  return GD_OK;
+}
+
+gd_status gd_server_create(gd_context *ctx, const gd_server_cfg *cfg, gd_server **out) {
+  if (!ctx || !cfg || !out) return GD_ERR_INVALID_ARG;
+  *out = nullptr;
+  const gd_ga_cfg &c = cfg->ga;
+  if (cfg->max_slots < 1 || cfg->max_slots > 4096 || c.pop_size < 2 || c.pop_size % 2 || c.elitism > 64 ||
+      c.elitism > c.pop_size || c.tournament_size < 1 || c.max_generations < 0 ||
+      (cfg->precision != GD_PREC_F32 && cfg->precision != GD_PREC_F64))
+    return gd::fail(ctx, GD_ERR_INVALID_ARG, "bad server config");
+  cudaSetDevice(ctx->device);
+  gd_server *S = new gd_server();
+  S->ctx = ctx;
+  S->cfg = *cfg;
+  gd_status s = gd::server_alloc(S);
+  if (s != GD_OK) {
+    gd::ga_release(ctx, S->arena);
+    delete S;
+    return s;
+  }
+  *out = S;
+  return GD_OK;
+}
+
+gd_status gd_server_submit(gd_server *S, const gd_atoms *rec, const gd_atoms *lig, const int32_t *pairs,
+                           int32_t n_pairs, const gd_weights *w, uint64_t seed, int64_t *job_id) {
+  if (!S || !rec || !lig || !job_id || n_pairs < 0 || (n_pairs > 0 && !pairs)) return GD_ERR_INVALID_ARG;
+  gd::Job *job = new gd::Job();
+  job->rec.copy(rec);
+  job->lig.copy(lig);
+  job->pairs.assign(pairs, pairs + 2 * static_cast<size_t>(n_pairs));
+  job->w = w ? *w : gd_weights{0.4, 0.05, 3.4, 1.0};
+  job->seed = seed;
+  job->t_submit = Clock::now();
+  std::lock_guard<std::mutex> lock(S->mu);
+  job->id = S->next_id++;
+  if (!S->started_clock) {
+    S->t_first = job->t_submit;
+    S->started_clock = true;
+  }
+  S->jobs[job->id] = job;
+  S->queue.push_back(job);
+  *job_id = job->id;
+  S->cv.notify_all();
+  return GD_OK;
+}
+
+gd_status gd_server_step(gd_server *S, int32_t *active) {
+  if (!S) return GD_ERR_INVALID_ARG;
+  if (S->running) return gd::fail(S->ctx, GD_ERR_STATE, "the server's own thread is running");
+  cudaSetDevice(S->ctx->device);
+  return gd::server_tick(S, active);
+}
+
+gd_status gd_server_start(gd_server *S) {
+  if (!S) return GD_ERR_INVALID_ARG;
+  if (S->running) return GD_OK;
+  S->running = true;
+  S->worker = std::thread([S]() {
+    cudaSetDevice(S->ctx->device);
+    while (true) {
+      {
+        std::unique_lock<std::mutex> lock(S->mu);
+        bool idle = S->queue.empty();
+        for (auto *j : S->slot_job) idle = idle && j == nullptr;
+        if (!S->running && idle) break;
+        if (idle) S->cv.wait_for(lock, std::chrono::milliseconds(5));
+        if (!S->running && S->queue.empty()) {
+          bool none = true;
+          for (auto *j : S->slot_job) none = none && j == nullptr;
+          if (none) break;
+        }
+      }
+      int active = 0;
+      if (gd::server_tick(S, &active) != GD_OK) {
+        std::lock_guard<std::mutex> lock(S->mu);
+        for (auto &kv : S->jobs)
+          if (kv.second->status == GD_JOB_RUNNING || kv.second->status == GD_JOB_QUEUED) {
+            kv.second->status = GD_JOB_FAILED;
+            kv.second->error = GD_ERR_CUDA;
+          }
+        S->cv.notify_all();
+        break;
+      }
+    }
+  });
+  return GD_OK;
+}
+
+gd_status gd_server_stop(gd_server *S) {
+  if (!S) return GD_ERR_INVALID_ARG;
+  if (S->worker.joinable()) {
+    {
+      std::lock_guard<std::mutex> lock(S->mu);
+      S->running = false;
+      S->cv.notify_all();
+    }
+    S->worker.join();
+  }
+  S->running = false;
+  return GD_OK;
+}
+
+gd_status gd_server_wait(gd_server *S, int64_t job_id, double timeout_s, int32_t *status) {
+  if (!S) return GD_ERR_INVALID_ARG;
+  std::unique_lock<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return gd::fail(S->ctx, GD_ERR_INVALID_ARG, "unknown job");
+  gd::Job *job = it->second;
+  const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(timeout_s));
+  while (job->status == GD_JOB_QUEUED || job->status == GD_JOB_RUNNING) {
+    if (S->cv.wait_until(lock, deadline) == std::cv_status::timeout) break;
+  }
+  if (status) *status = job->status;
+  return (job->status == GD_JOB_DONE || job->status == GD_JOB_FAILED) ? GD_OK : GD_ERR_TIMEOUT;
+}
+
+gd_status gd_server_result(gd_server *S, int64_t job_id, gd_job_result *res, double *genes, gd_pose_energy *energies,
+                           double *history) {
+  if (!S || !res) return GD_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return gd::fail(S->ctx, GD_ERR_INVALID_ARG, "unknown job");
+  gd::Job *job = it->second;
+  res->status = job->status;
+  res->error = job->error;
+  res->generations = job->generations;
+  const auto now = Clock::now();
+  const auto end = job->status == GD_JOB_DONE || job->status == GD_JOB_FAILED ? job->t_done : now;
+  res->latency_s = std::chrono::duration<double>(end - job->t_submit).count();
+  res->queue_s = job->status == GD_JOB_QUEUED
+                     ? std::chrono::duration<double>(now - job->t_submit).count()
+                     : std::chrono::duration<double>(job->t_admit - job->t_submit).count();
+  if (job->status == GD_JOB_DONE) {
+    if (genes) std::memcpy(genes, job->genes.data(), sizeof(double) * job->genes.size());
+    if (energies) std::memcpy(energies, job->energies.data(), sizeof(gd_pose_energy) * job->energies.size());
+    if (history) std::memcpy(history, job->history.data(), sizeof(double) * job->history.size());
+  }
+  return GD_OK;
+}
+
+gd_status gd_server_release(gd_server *S, int64_t job_id) {
+  if (!S) return GD_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return gd::fail(S->ctx, GD_ERR_INVALID_ARG, "unknown job");
+  if (it->second->status != GD_JOB_DONE && it->second->status != GD_JOB_FAILED)
+    return gd::fail(S->ctx, GD_ERR_STATE, "job still queued or running");
+  delete it->second;
+  S->jobs.erase(it);
+  return GD_OK;
+}
+
+gd_status gd_server_get_stats(gd_server *S, gd_server_stats *out) {
+  if (!S || !out) return GD_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lock(S->mu);
+  out->completed = S->completed;
+  out->queued = static_cast<int64_t>(S->queue.size());
+  int act = 0;
+  for (auto *j : S->slot_job) act += j != nullptr;
+  out->resident = act;
+  out->generations_run = S->generations_run;
+  out->poses_scored = S->poses_scored;
+  out->device_bytes = S->job_bytes;
+  std::vector<double> l = S->latencies;
+  std::sort(l.begin(), l.end());
+  auto pct = [&](double p) {
+    if (l.empty()) return 0.0;
+    const size_t k = static_cast<size_t>(std::ceil(p * l.size())) - 1;
+    return l[std::min(k, l.size() - 1)];
+  };
+  out->latency_p50_s = pct(0.50);
+  out->latency_p99_s = pct(0.99);
+  out->latency_max_s = l.empty() ? 0.0 : l.back();
+  return GD_OK;
+}
+
+gd_status gd_server_destroy(gd_server *S) {
+  if (!S) return GD_ERR_INVALID_ARG;
+  gd_server_stop(S);
+  cudaSetDevice(S->ctx->device);
+  cudaStreamSynchronize(S->ctx->stream);
+  for (auto *j : S->slot_job)
+    if (j && j->cx) gd_complex_destroy(j->cx);
+  if (S->bl) gd::batch_free(S->ctx, S->bl);
+  gd::ga_release(S->ctx, S->arena);
+  for (auto &kv : S->jobs) delete kv.second;
+  delete S;
+  return GD_OK;
+}
+
+}  // extern "C"

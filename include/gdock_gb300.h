@@ -224,6 +224,53 @@ gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs,
                     gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
                     int32_t *out_generations, double *out_history);
 
+/* ------------------------------------------------------------- serving --
+ * A request loop for docking jobs (gdock's `run` GA per job): jobs are
+ * admitted first-come first-served into resident slots as slots and the HBM
+ * budget allow; every tick advances all resident jobs by one generation in
+ * shared launches (continuous batching), keeping each job's coordinates,
+ * parameters and population on the device; finished jobs leave their slot to
+ * the next queued job.  A job's result does not depend on the other jobs. */
+typedef struct gd_server gd_server;
+typedef struct gd_server_cfg {
+  int32_t max_slots;    /* jobs resident at once */
+  uint64_t hbm_budget;  /* device bytes resident complexes may hold (0: the context's budget only) */
+  gd_ga_cfg ga;         /* GA settings of every job (seed ignored: per job) */
+  int32_t precision;    /* gd_precision */
+} gd_server_cfg;
+enum { GD_JOB_QUEUED = 0, GD_JOB_RUNNING = 1, GD_JOB_DONE = 2, GD_JOB_FAILED = 3 };
+typedef struct gd_job_result {
+  int32_t status, error, generations;
+  double latency_s; /* submit -> done (or -> now) */
+  double queue_s;   /* submit -> admitted */
+} gd_job_result;
+typedef struct gd_server_stats {
+  int64_t completed, queued, resident, generations_run, poses_scored;
+  uint64_t device_bytes;
+  double latency_p50_s, latency_p99_s, latency_max_s;
+} gd_server_stats;
+
+gd_status gd_server_default_cfg(gd_server_cfg *cfg);
+gd_status gd_server_create(gd_context *ctx, const gd_server_cfg *cfg, gd_server **out);
+gd_status gd_server_destroy(gd_server *s);
+/* Queue a job (inputs copied); thread-safe. */
+gd_status gd_server_submit(gd_server *s, const gd_atoms *receptor, const gd_atoms *ligand,
+                           const int32_t *restraint_pairs, int32_t n_pairs, const gd_weights *w, uint64_t seed,
+                           int64_t *job_id);
+/* One tick on the caller's thread (admit, one generation, retire). */
+gd_status gd_server_step(gd_server *s, int32_t *resident_jobs);
+/* Run ticks on the server's own thread until gd_server_stop (which drains
+ * queued and resident jobs first). */
+gd_status gd_server_start(gd_server *s);
+gd_status gd_server_stop(gd_server *s);
+gd_status gd_server_wait(gd_server *s, int64_t job_id, double timeout_s, int32_t *status);
+/* Status and, when done, final population (pop x 6), its energies and the
+ * best fitness per generation (max_generations); pointers may be NULL. */
+gd_status gd_server_result(gd_server *s, int64_t job_id, gd_job_result *res, double *genes,
+                           gd_pose_energy *energies, double *history);
+gd_status gd_server_release(gd_server *s, int64_t job_id);
+gd_status gd_server_get_stats(gd_server *s, gd_server_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -207,9 +207,9 @@ def main():
 
     # --- slots-per-lane sweep (a small autotune on a pose sample) ---
     tune = {}
-    for slots in (2, 4, 6, 8):
+    for slots in (4, 6, 8, 16 + 4, 16 + 6, 16 + 8):  # slots per lane (+16: two receptor atoms per step)
         ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
-        ns_t = min(NP, 8192)
+        ns_t = min(NP, 16384)
         launch(gd.GD_PREC_F32, ns_t)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -293,7 +293,8 @@ def main():
             "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES,
                     "d2h_bytes_per_step": NP * 48},
             "gpu_launches": args.steps,
-            "autotune": {"f32_slots": best_slots, "poses_per_s_by_slots": {str(k): v for k, v in tune.items()}},
+            "autotune": {"f32_slots": best_slots % 16, "receptor_atoms_per_step": 1 + best_slots // 16,
+                         "poses_per_s_by_variant": {f"S{k % 16}xA{1 + k // 16}": v for k, v in tune.items()}},
             "pair_evals_per_s": pairs * value,
             "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,
                            "tflops": FLOP_PER_PAIR * pairs * plain / 1e12,

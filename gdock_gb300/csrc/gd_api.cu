@@ -302,8 +302,9 @@ const char *gd_last_error(const gd_context *ctx) { return ctx ? ctx->last_error.
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (knob == GD_TUNE_F32_SLOTS) {
-    if (value != 0 && value != 2 && value != 4 && value != 6 && value != 8)
-      return fail(ctx, GD_ERR_INVALID_ARG, "F32 slots must be 0, 2, 4, 6 or 8");
+    const int sv = value % 16, av = value / 16;
+    if (value != 0 && ((sv != 2 && sv != 4 && sv != 6 && sv != 8) || av > 1))
+      return fail(ctx, GD_ERR_INVALID_ARG, "F32 tuning: slots 2/4/6/8, plus 16 for two receptor atoms per step");
     ctx->tune_f32_slots = value;
     return GD_OK;
   }

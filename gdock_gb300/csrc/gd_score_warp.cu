@@ -37,7 +37,6 @@ constexpr int kWarps = 4;      // warps per CTA (independent)
 constexpr int kSeg = 64;       // receptor atoms per ring stage
 constexpr int kWS = 4;         // ring stages per warp
 constexpr int kBlk = 8;        // receptor atoms per culling sphere
-constexpr int kAtoms = 1;      // receptor atoms held in registers per inner step
 constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
 
 struct BatchParams {
@@ -195,7 +194,7 @@ __device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
   cnt[i] = static_cast<uint8_t>(c > 255 ? 255 : (c < 0 ? 0 : c));
 }
 
-template <int S, bool SERIAL, bool CLAMP>
+template <int S, int kAtoms, bool SERIAL, bool CLAMP>
 __global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams bp) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -451,7 +450,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams
   }
 }
 
-template <int S>
+template <int S, int A>
 cudaError_t launch_w(const BatchParams &bp, bool serial, bool clamp, size_t smem, int grid, cudaStream_t st) {
   auto go = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -459,25 +458,65 @@ cudaError_t launch_w(const BatchParams &bp, bool serial, bool clamp, size_t smem
     kern<<<grid, kWarps * 32, smem, st>>>(bp);
     return cudaGetLastError();
   };
-  if (!serial && !clamp) return go(k_score_f32w<S, false, false>);
-  if (serial && !clamp) return go(k_score_f32w<S, true, false>);
-  if (!serial && clamp) return go(k_score_f32w<S, false, true>);
-  return go(k_score_f32w<S, true, true>);
+  if (!serial && !clamp) return go(k_score_f32w<S, A, false, false>);
+  if (serial && !clamp) return go(k_score_f32w<S, A, true, false>);
+  if (!serial && clamp) return go(k_score_f32w<S, A, false, true>);
+  return go(k_score_f32w<S, A, true, true>);
 }
 
-template <int S>
+template <int S, int A>
 cudaError_t occupancy_w(bool serial, bool clamp, size_t smem, int *per_sm) {
-  if (!serial && !clamp) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, false, false>, kWarps * 32, smem);
-  if (serial && !clamp) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, true, false>, kWarps * 32, smem);
-  if (!serial && clamp) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, false, true>, kWarps * 32, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, true, true>, kWarps * 32, smem);
+  if (!serial && !clamp)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, false, false>, kWarps * 32, smem);
+  if (serial && !clamp)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, true, false>, kWarps * 32, smem);
+  if (!serial && clamp)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, false, true>, kWarps * 32, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, true, true>, kWarps * 32, smem);
+}
+
+// Kernel variants: slots per lane x receptor atoms per inner step.
+// `slots` encodes both: slots % 16 = S (2/4/6/8), slots / 16 = atoms - 1.
+cudaError_t occupancy_var(int S, int A, bool serial, bool clamp, size_t smem, int *per_sm) {
+  if (A == 2) {
+    switch (S) {
+      case 2: return occupancy_w<2, 2>(serial, clamp, smem, per_sm);
+      case 4: return occupancy_w<4, 2>(serial, clamp, smem, per_sm);
+      case 6: return occupancy_w<6, 2>(serial, clamp, smem, per_sm);
+      default: return occupancy_w<8, 2>(serial, clamp, smem, per_sm);
+    }
+  }
+  switch (S) {
+    case 2: return occupancy_w<2, 1>(serial, clamp, smem, per_sm);
+    case 4: return occupancy_w<4, 1>(serial, clamp, smem, per_sm);
+    case 6: return occupancy_w<6, 1>(serial, clamp, smem, per_sm);
+    default: return occupancy_w<8, 1>(serial, clamp, smem, per_sm);
+  }
+}
+
+cudaError_t launch_var(int S, int A, const BatchParams &bp, bool serial, bool clamp, size_t smem, int grid,
+                       cudaStream_t st) {
+  if (A == 2) {
+    switch (S) {
+      case 2: return launch_w<2, 2>(bp, serial, clamp, smem, grid, st);
+      case 4: return launch_w<4, 2>(bp, serial, clamp, smem, grid, st);
+      case 6: return launch_w<6, 2>(bp, serial, clamp, smem, grid, st);
+      default: return launch_w<8, 2>(bp, serial, clamp, smem, grid, st);
+    }
+  }
+  switch (S) {
+    case 2: return launch_w<2, 1>(bp, serial, clamp, smem, grid, st);
+    case 4: return launch_w<4, 1>(bp, serial, clamp, smem, grid, st);
+    case 6: return launch_w<6, 1>(bp, serial, clamp, smem, grid, st);
+    default: return launch_w<8, 1>(bp, serial, clamp, smem, grid, st);
+  }
 }
 
 }  // namespace
 
 // Launch geometry of a batch: slots per lane, shared memory, grid.
 struct BatchPlan {
-  int S, smem_cnt, max_nr, grid;
+  int S, A, smem_cnt, max_nr, grid;
   size_t smem;
   std::vector<long long> start;
 };
@@ -493,15 +532,11 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   }
   pl->smem_cnt = pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0;
   pl->smem = warp_layout(pl->smem_cnt).total * kWarps;
-  pl->S = slots <= 2 ? 2 : (slots <= 4 ? 4 : (slots <= 6 ? 6 : 8));
+  const int sv = slots % 16;
+  pl->S = sv <= 2 ? 2 : (sv <= 4 ? 4 : (sv <= 6 ? 6 : 8));
+  pl->A = slots / 16 >= 1 ? 2 : 1;
   int per_sm = 0;
-  cudaError_t e;
-  switch (pl->S) {
-    case 2: e = occupancy_w<2>(serial, clamp, pl->smem, &per_sm); break;
-    case 4: e = occupancy_w<4>(serial, clamp, pl->smem, &per_sm); break;
-    case 6: e = occupancy_w<6>(serial, clamp, pl->smem, &per_sm); break;
-    default: e = occupancy_w<8>(serial, clamp, pl->smem, &per_sm); break;
-  }
+  cudaError_t e = occupancy_var(pl->S, pl->A, serial, clamp, pl->smem, &per_sm);
   if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
   const long long items = pl->start[ncx];
@@ -540,12 +575,7 @@ static gd_status run_batch(gd_context *ctx, const std::vector<ScoreParams> &desc
   bp.max_nr = pl.max_nr;
   bp.warp_smem = static_cast<int>(warp_layout(pl.smem_cnt).total);
   bp.err = ctx->d_err;
-  switch (pl.S) {
-    case 2: e = launch_w<2>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
-    case 4: e = launch_w<4>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
-    case 6: e = launch_w<6>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
-    default: e = launch_w<8>(bp, serial, clamp, pl.smem, pl.grid, stream); break;
-  }
+  e = launch_var(pl.S, pl.A, bp, serial, clamp, pl.smem, pl.grid, stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
   return GD_OK;
 }
@@ -642,12 +672,7 @@ gd_status batch_launch(gd_context *ctx, BatchLaunch *b, cudaStream_t stream) {
   bp.warp_smem = static_cast<int>(warp_layout(b->plan.smem_cnt).total);
   bp.err = ctx->d_err;
   const BatchPlan &pl = b->plan;
-  switch (pl.S) {
-    case 2: e = launch_w<2>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
-    case 4: e = launch_w<4>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
-    case 6: e = launch_w<6>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
-    default: e = launch_w<8>(bp, b->serial, b->clamp, pl.smem, pl.grid, stream); break;
-  }
+  e = launch_var(pl.S, pl.A, bp, b->serial, b->clamp, pl.smem, pl.grid, stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
   return GD_OK;
 }

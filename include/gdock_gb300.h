@@ -102,7 +102,8 @@ gd_status gd_context_create(int32_t device, uint64_t hbm_budget_bytes, gd_contex
 gd_status gd_context_destroy(gd_context *ctx);
 /* Tuning knobs of the context's kernels (the autotuner sets these).
  *   GD_TUNE_F32_SLOTS: ligand atoms per lane per pass of the FP32 scoring
- *                      kernel (2, 4, 6 or 8; 0 = automatic). */
+ *                      kernel (2, 4, 6 or 8; 0 = automatic), plus 16 to
+ *                      evaluate two receptor atoms per inner step. */
 enum { GD_TUNE_F32_SLOTS = 0 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob);

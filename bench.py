@@ -158,6 +158,144 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+
+# --------------------------------------------------------------------------
+# Other configurations (`--workload c3|c4|c5`): each prints one JSON line.
+
+def _uneven_complexes(count, seed, rec_range=(100, 800), lig_range=(50, 300), restr=(6, 20)):
+    from gdock_gb300 import position_ligand, synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for j in range(count):
+        nr = int(round(np.exp(rng.uniform(np.log(rec_range[0]), np.log(rec_range[1])))))
+        nl = int(round(np.exp(rng.uniform(np.log(lig_range[0]), np.log(lig_range[1])))))
+        k = int(rng.integers(restr[0], restr[1] + 1))
+        c = synth.make_complex(nr, nl, k, seed=seed * 1000 + j)
+        out.append((c.receptor, position_ligand(c.receptor, c.ligand), c.restraint_pairs))
+    return out
+
+
+def _fp64_ga_cost(gd, _lib, ctx, jobs, pop, gens):
+    """Seconds per pose-evaluation of the plain FP64 GA on a sample of jobs."""
+    cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=gens, early_stopping=0, seed=5)
+    cxs = [gd.Complex(r, l, p, ctx=ctx) for r, l, p in jobs]
+    t0 = time.perf_counter()
+    res = gd.run_ga(cxs, cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
+    dt = time.perf_counter() - t0
+    pairs = sum(len(r) * len(l) for r, l, _ in jobs) * pop * (gens + 1)
+    for c in cxs:
+        c.close()
+    return dt, pairs
+
+
+def run_c3(args):
+    import gdock_gb300 as gd
+    from gdock_gb300 import _lib
+    ctx = gd.Context(0)
+    jobs = _uneven_complexes(64, 33)
+    G, pop = 50, 150
+    cxs = [gd.Complex(r, l, p, ctx=ctx) for r, l, p in jobs]
+    cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=G, early_stopping=0, seed=3)
+    gd.run_ga(cxs[:2], _lib.ga_default_cfg(pop_size=pop, max_generations=2, early_stopping=0), ctx=ctx)  # warm
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        res = gd.run_ga(cxs, cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    evals = len(jobs) * pop * (G + 1)
+    pairs = sum(len(r) * len(l) for r, l, _ in jobs) * pop * (G + 1)
+    # FCC clustering of each final population
+    t0 = time.perf_counter()
+    n_clusters = [len(cx.cluster(res.genes[j])) for j, cx in enumerate(cxs)]
+    t_fcc = time.perf_counter() - t0
+    # plain FP64 GA on a sample of 4 jobs x 2 generations, per pair
+    dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, jobs[:4], pop, 2)
+    line = {"metric": "docks/s (batched uneven GA, 64 complexes, pop 150, 50 generations, CUDA graphs)",
+            "value": len(jobs) / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": 1,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "64 synthetic complexes, receptor 100-800 residues, ligand 50-300 residues "
+                                   "(log-uniform), 6-20 restraints; GA pop 150 x 50 generations",
+                       "receptor_atoms": [min(len(r) for r, _, _ in jobs), max(len(r) for r, _, _ in jobs)],
+                       "ligand_atoms": [min(len(l) for _, l, _ in jobs), max(len(l) for _, l, _ in jobs)]},
+            "poses_per_s": evals / t, "pair_evals_per_s": pairs / t,
+            "fcc_clustering": {"seconds_for_64_populations": t_fcc, "clusters_found": int(sum(n_clusters))},
+            "plain_fp64_pair_evals_per_s": pairs64 / dt64,
+            "f32_batched_over_plain_f64": (pairs / t) / (pairs64 / dt64)}
+    print(json.dumps(line), flush=True)
+
+
+def run_c4(args):
+    import gdock_gb300 as gd
+    from gdock_gb300 import _lib
+    ctx = gd.Context(0)
+    pool = _uneven_complexes(48, 44)
+    ga = _lib.ga_default_cfg(pop_size=150, max_generations=200, early_stopping=1)
+    rates = [float(r) for r in os.environ.get("GD_C4_RATES", "2,8,32").split(",")]
+    per_rate = int(os.environ.get("GD_C4_JOBS", "32"))
+    sweep = []
+    for rate in rates:
+        srv = gd.Server(ctx, max_slots=64, ga=ga)
+        srv.start()
+        rng = np.random.default_rng(int(rate * 100))
+        ids, t0 = [], time.perf_counter()
+        for i in range(per_rate):
+            r, l, p = pool[i % len(pool)]
+            ids.append(srv.submit(r, l, p, seed=1000 + i))
+            time.sleep(float(rng.exponential(1.0 / rate)))
+        for jid in ids:
+            srv.wait(jid, 600.0)
+        t_all = time.perf_counter() - t0
+        st = srv.stats()
+        gens = [srv.result(j)[0].generations for j in ids]
+        srv.stop()
+        sweep.append({"rate_jobs_per_s": rate, "jobs": per_rate, "jobs_per_s": per_rate / t_all,
+                      "latency_p50_s": st.latency_p50_s, "latency_p99_s": st.latency_p99_s,
+                      "mean_generations": float(np.mean(gens)), "poses_scored": int(st.poses_scored)})
+        srv.close()
+    # plain FP64: one job at a time, 3 generations of a sample job, scaled to its generations
+    dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, pool[:2], 150, 3)
+    best = max(sweep, key=lambda x: x["jobs_per_s"])
+    line = {"metric": "served docking jobs/s with p50/p99 latency (continuous batching)",
+            "value": best["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "Poisson arrivals of synthetic complexes (C3 sizes), GA pop 150, early "
+                                   "stopping after 10 stagnant generations, cap 200", "slots": 64},
+            "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64}
+    print(json.dumps(line), flush=True)
+
+
+def run_c5(args):
+    import gdock_gb300 as gd
+    from gdock_gb300 import _lib, position_ligand, synth
+    ctx = gd.Context(0)
+    c = synth.make_complex(2000, 500, 30, seed=55)
+    lig = position_ligand(c.receptor, c.ligand)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    G = int(os.environ.get("GD_C5_GENERATIONS", "100"))
+    cfg = _lib.ga_default_cfg(pop_size=4096, max_generations=G, early_stopping=0, seed=9)
+    t0 = time.perf_counter()
+    res = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
+    t_ga = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    clusters = cx.cluster(res.genes[0])
+    t_fcc = time.perf_counter() - t0
+    pairs = len(c.receptor) * len(lig) * 4096 * (G + 1)
+    line = {"metric": "poses/s (large complex GA, pop 4096) and FCC clustering time over 4096 poses",
+            "value": 4096 * (G + 1) / t_ga, "unit": "poses/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": t_ga * 1e3 / (G + 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "synthetic receptor 2000 residues x ligand 500 residues, 30 restraints, "
+                                   f"GA pop 4096 x {G} generations", "receptor_atoms": len(c.receptor),
+                       "ligand_atoms": len(lig)},
+            "pair_evals_per_s": pairs / t_ga, "ga_seconds": t_ga,
+            "fcc": {"poses": 4096, "seconds": t_fcc, "fcc_pairs_per_s": 4096 * 4096 / t_fcc,
+                    "clusters": len(clusters)}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -166,12 +304,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-sample", type=int, default=2048)
     ap.add_argument("--cpu-sample", type=int, default=32)
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+                    help="c2: single-complex scoring (default); c3: batched uneven GA; c4: served jobs; "
+                         "c5: large complex")
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
     args = ap.parse_args()
     NP = args.poses
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "c2":
+        return {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
 
     import torch
     import torch.distributed as dist

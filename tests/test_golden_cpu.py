@@ -1,0 +1,39 @@
+"""The committed golden fixtures against the oracle (regression of both), and
+the fixture's parsed arrays against gdock's test structures when the
+reference checkout is present."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from golden_data import cluster_list, contact_sets, load
+
+
+def test_2oob_energies_contacts_clusters(oracle):
+    d, rec, lig = load("2oob.npz")
+    e = oracle.score_poses(rec, lig, d["restraints"], d["genes"])
+    np.testing.assert_array_equal(e, d["energies"])
+    sets = contact_sets(d)
+    for g, keys in zip(d["genes"][8:40], sets):
+        np.testing.assert_array_equal(oracle.pose_contacts(rec, lig, g), keys)
+    assert oracle.cluster(sets, min_size=1) == cluster_list(d)
+    assert max(d["cluster_sizes"]) > 4  # the near-native poses form a real cluster
+
+
+def test_1h590_score_models(oracle):
+    d, rec, lig = load("1h590_score.npz")
+    assert len(set(rec.serial.tolist()) & set(lig.serial.tolist())) > 0  # equal serials skip vdW pairs
+    e = oracle.score_models(rec, lig, [], d["models_xyz"][:10])
+    np.testing.assert_array_equal(e, d["energies"][:10])
+
+
+def test_fixture_matches_reference_structures():
+    ref = Path("/root/reference/data")
+    if not ref.exists():
+        pytest.skip("reference checkout not present")
+    from gdock_gb300 import pdb
+    d, rec, lig = load("2oob.npz")
+    r = pdb.read_pdb(ref / "2oob_A.pdb")[0]
+    np.testing.assert_array_equal(r.x, rec.x)
+    np.testing.assert_array_equal(r.epsilon, rec.epsilon)
+    np.testing.assert_array_equal(r.charge, rec.charge)

@@ -35,6 +35,9 @@ sys.path.insert(0, str(ROOT))
 
 N_REC_RES, N_LIG_RES, N_RESTRAINTS, N_POSES, SEED = 300, 150, 12, 65536, 2026
 FLOP_PER_PAIR = 37  # convention: d2 8, LJ 18, Coulomb 4, cutoff tests 5, burial 2
+# DRAM bytes per pose of the FP32 scoring kernel: 1.407 MB read + 0 B written
+# over a 4,096-pose launch of this workload (profiles/k_score_f32w_single_complex.md)
+TRAFFIC_PER_POSE = 1.407232e6 / 4096
 METRIC = "poses/s (batched FP32 scoring, single complex)"
 
 
@@ -132,6 +135,20 @@ def cpu_sample(c, lig, genes, n_sample, threads):
     t0 = time.perf_counter()
     oracle.score_poses(c.receptor, lig, c.restraint_pairs, g, nthreads=threads)
     return n_sample / (time.perf_counter() - t0)
+
+
+def replica_throughput(t_step: float, units: int, world: int, device: str = "cpu"):
+    """Replicas-only scaling: every rank scores its own `units` poses; the job
+    takes as long as the slowest rank, and all ranks' poses count.
+    Returns (max step time over ranks, whole-job units per second)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([t_step], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+        dist.barrier()
+    return t_step, world * units / t_step
 
 
 def run_reference(args):
@@ -386,12 +403,7 @@ def main():
     torch.cuda.synchronize()
     ctx.sync()
     t_step = float(np.sum(times)) / args.steps
-    if world > 1:
-        t = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-        dist.barrier()
-    value = world * NP / t_step
+    t_step, value = replica_throughput(t_step, NP, world, "cuda")
     res32 = out.cpu().numpy().copy()
 
     # --- end to end through the C ABI with host buffers (e2e) ---
@@ -445,7 +457,9 @@ def main():
             "f32_over_f64_speedup": value / plain,
             "f32_rel_error_vs_f64": err,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32"], "unit": "TFLOP/s",
-                         "frac": achieved / peaks["fp32"], "traffic": None,
+                         "frac": achieved / peaks["fp32"], "traffic": TRAFFIC_PER_POSE * NP,
+                         "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
+                                           "(4,096 poses), scaled per pose",
                          "peak_source": "cuBLAS SGEMM (TF32 off) measured in this run; "
                                         "37 flop per receptor-ligand pair convention"},
             "cpu_baseline": {"value": cpu_v, "unit": "poses/s", "cores": cpu_threads, "kind": "port",

@@ -367,7 +367,7 @@ def main():
 
     # --- slots-per-lane sweep (a small autotune on a pose sample) ---
     tune = {}
-    for slots in (4, 6, 8, 16 + 4, 16 + 6, 16 + 8):  # slots per lane (+16: two receptor atoms per step)
+    for slots in (4, 8, 16 + 4, 16 + 6, 16 + 8, 32 + 4, 32 + 16 + 4):  # see GD_TUNE_F32_SLOTS
         ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
         ns_t = min(NP, 16384)
         launch(gd.GD_PREC_F32, ns_t)
@@ -448,8 +448,10 @@ def main():
             "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES,
                     "d2h_bytes_per_step": NP * 48},
             "gpu_launches": args.steps,
-            "autotune": {"f32_slots": best_slots % 16, "receptor_atoms_per_step": 1 + best_slots // 16,
-                         "poses_per_s_by_variant": {f"S{k % 16}xA{1 + k // 16}": v for k, v in tune.items()}},
+            "autotune": {"f32_slots": best_slots % 16, "receptor_atoms_per_step": 1 + (best_slots // 16) % 2,
+                         "min_ctas_per_sm": 6 if best_slots >= 32 else 4,
+                         "poses_per_s_by_variant": {f"S{k % 16}xA{1 + (k // 16) % 2}xB{6 if k >= 32 else 4}": v
+                                                    for k, v in tune.items()}},
             "pair_evals_per_s": pairs * value,
             "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,
                            "tflops": FLOP_PER_PAIR * pairs * plain / 1e12,

@@ -4,6 +4,8 @@
 // gd_status with a message in gd_last_error().
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
@@ -14,6 +16,15 @@
 #include "gd_internal.cuh"
 
 namespace gd {
+
+bool trace_on() {
+  static const bool on = std::getenv("GD_TRACE") != nullptr;
+  return on;
+}
+
+void trace(const char *phase, double seconds) {
+  if (trace_on()) std::fprintf(stderr, "[gdock_gb300] %-32s %10.3f ms\n", phase, seconds * 1e3);
+}
 
 gd_status fail(gd_context *ctx, gd_status s, const std::string &msg) {
   if (ctx) ctx->last_error = msg;
@@ -302,9 +313,13 @@ const char *gd_last_error(const gd_context *ctx) { return ctx ? ctx->last_error.
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (knob == GD_TUNE_F32_SLOTS) {
-    const int sv = value % 16, av = value / 16;
-    if (value != 0 && ((sv != 2 && sv != 4 && sv != 6 && sv != 8) || av > 1))
-      return fail(ctx, GD_ERR_INVALID_ARG, "F32 tuning: slots 2/4/6/8, plus 16 for two receptor atoms per step");
+    static const int kValid[] = {0, 4, 8, 16 + 4, 16 + 6, 16 + 8, 32 + 4, 32 + 16 + 4};
+    bool ok = false;
+    for (int v : kValid) ok = ok || v == value;
+    if (!ok)
+      return fail(ctx, GD_ERR_INVALID_ARG,
+                  "F32 tuning: one of 4, 8, 20, 22, 24, 36, 52 (slots + 16 for two atoms per step + 32 for the "
+                  "higher-occupancy register cap)");
     ctx->tune_f32_slots = value;
     return GD_OK;
   }

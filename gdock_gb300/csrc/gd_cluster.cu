@@ -22,6 +22,7 @@
 // ligand-only inter-chain contacts of multi-chain molecules, the universe
 // compaction, and the greedy clustering over the adjacency bit matrix.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -55,6 +56,13 @@ struct ClusterTopo {
 namespace {
 
 constexpr int kMaxGroupAtoms = 64;
+
+struct PhaseTimer {
+  const char *name;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit PhaseTimer(const char *n) : name(n) {}
+  ~PhaseTimer() { trace(name, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count()); }
+};
 
 __device__ __forceinline__ void xform(const gd_pose_frame &f, double cx, double cy, double cz, double xo, double yo,
                                       double zo, double &X, double &Y, double &Z) {
@@ -472,6 +480,7 @@ void free_cluster_cache(gd_complex *cx) {
 gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double cutoff, std::vector<int64_t> &keys,
                              std::vector<int64_t> &offs) {
   gd_context *ctx = cx->ctx;
+  PhaseTimer pt_all("contacts: total");
   ClusterTopo *t = nullptr;
   gd_status s = get_topo(cx, &t);
   if (s != GD_OK) return s;
@@ -542,6 +551,7 @@ gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double 
     e = cudaMemcpyAsync(counts.data(), d_counts, cb, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "contacts kernel");
+    trace("contacts: kernel + counts", std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
     const int maxc = n > 0 ? *std::max_element(counts.begin(), counts.end()) : 0;
     if (maxc > cap) {  // rerun once with room for the largest pose
       cap = maxc;
@@ -560,6 +570,7 @@ gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double 
     }
     break;
   }
+  PhaseTimer pt_keys("contacts: host keys");
   keys.clear();
   offs.assign(1, 0);
   std::vector<int64_t> pk;
@@ -591,6 +602,7 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
                        int32_t *n_clusters, int32_t *centers, int32_t *sizes, int32_t *members) {
   *n_clusters = 0;
   if (n <= 0) return GD_OK;
+  PhaseTimer pt_all("fcc: total");
   // compacted contact universe
   std::vector<int64_t> uni(keys, keys + offs[n]);
   std::sort(uni.begin(), uni.end());
@@ -615,6 +627,9 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
   unsigned long long *d_bits = reinterpret_cast<unsigned long long *>(base);
   int *d_sz = reinterpret_cast<int *>(base + al(bb));
   uint32_t *d_adj = reinterpret_cast<uint32_t *>(base + al(bb) + al(sb));
+  trace("fcc: universe + bitsets (host)",
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+  const auto t_k = std::chrono::steady_clock::now();
   cudaError_t e = cudaMemcpyAsync(d_bits, bits.data(), bb, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_sz, sz.data(), sb, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_adj, 0, ab, ctx->stream);
@@ -635,6 +650,8 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
   e = cudaMemcpyAsync(adj.data(), d_adj, ab, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel");
+  trace("fcc: kernel + transfers", std::chrono::duration<double>(std::chrono::steady_clock::now() - t_k).count());
+  PhaseTimer pt_g("fcc: greedy clustering (host)");
   *n_clusters = greedy_clusters(adj, n, aw, cfg.min_cluster_size, centers, sizes, members);
   return GD_OK;
 }

@@ -417,7 +417,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     }
     BatchLaunch *bl = nullptr;
     if (prec == GD_PREC_F32) {
-      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 4, &bl);
+      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4, &bl);
       if (s != GD_OK) goto done;
     }
     GaStepParams P{};
@@ -572,6 +572,7 @@ struct gd_server {
   gd::GaRun arena;  // max_slots "jobs" worth of device buffers
   std::vector<gd::Job *> slot_job;
   gd::BatchLaunch *bl = nullptr;
+  bool dirty = true;       // slot membership changed since bl was prepared
   uint64_t job_bytes = 0;  // device bytes held by resident complexes
   std::mutex mu;
   std::condition_variable cv;
@@ -720,6 +721,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
       S->slot_job[free_slot] = job;
     }
     S->job_bytes += bytes;
+    S->dirty = true;
     s = server_load_slot(S, free_slot, job);
     if (s != GD_OK) return s;
   }
@@ -749,9 +751,13 @@ gd_status server_tick(gd_server *S, int *active_out) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "frames kernel");
   if (S->cfg.precision == GD_PREC_F32) {
-    if (S->bl) batch_free(ctx, S->bl);
-    S->bl = nullptr;
-    s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 4, &S->bl);
+    // the argument block only changes when jobs enter or leave a slot
+    if (S->dirty || !S->bl) {
+      if (S->bl) batch_free(ctx, S->bl);
+      S->bl = nullptr;
+      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4, &S->bl);
+      S->dirty = false;
+    }
     if (s == GD_OK) s = batch_launch(ctx, S->bl, st);
   } else {
     for (int j = 0; j < J && s == GD_OK; ++j)
@@ -811,6 +817,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
     // history entries past the generations this job ran are not its own
     const int valid = std::min(c.max_generations, states[j].stop == 1 ? states[j].gen + 1 : states[j].gen);
     for (int g = std::max(valid, 0); g < c.max_generations; ++g) job->history[g] = NAN;
+    S->dirty = true;
     std::lock_guard<std::mutex> lock(S->mu);
     S->slot_job[j] = nullptr;
     job->status = GD_JOB_DONE;

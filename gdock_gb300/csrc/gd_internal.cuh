@@ -144,6 +144,10 @@ struct gd_complex {
 };
 
 namespace gd {
+// Host-side phase trace, printed to stderr when GD_TRACE is set in the
+// environment (off by default).
+bool trace_on();
+void trace(const char *phase, double seconds);
 gd_status fail(gd_context *ctx, gd_status s, const std::string &msg);
 gd_status cuda_fail(gd_context *ctx, cudaError_t e, const char *what);
 gd_status dev_alloc(gd_context *ctx, uint64_t bytes, void **p);

@@ -292,7 +292,7 @@ gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const doub
   const bool serial = cx->serial_overlap, clamp = cx->need_clamp;
   if (prec == GD_PREC_F32)
     return launch_score_batch_f32(ctx, std::vector<ScoreParams>{p}, serial, clamp,
-                                  ctx->tune_f32_slots ? ctx->tune_f32_slots : 4, stream);
+                                  ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4, stream);
   cudaError_t e;
   const size_t smem = smem_layout<D4>(p.nt, p.nr, kNT, sizeof(D4)).total;
   const int S = std::max(1, std::min(4, (p.nl + kNT - 1) / kNT));

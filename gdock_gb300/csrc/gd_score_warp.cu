@@ -194,8 +194,8 @@ __device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
   cnt[i] = static_cast<uint8_t>(c > 255 ? 255 : (c < 0 ? 0 : c));
 }
 
-template <int S, int kAtoms, bool SERIAL, bool CLAMP>
-__global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams bp) {
+template <int S, int kAtoms, int MINB, bool SERIAL, bool CLAMP>
+__global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchParams bp) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const WarpSmem L = warp_layout(bp.smem_cnt);
@@ -450,73 +450,60 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_score_f32w(const BatchParams
   }
 }
 
-template <int S, int A>
-cudaError_t launch_w(const BatchParams &bp, bool serial, bool clamp, size_t smem, int grid, cudaStream_t st) {
-  auto go = [&](auto kern) -> cudaError_t {
+// Kernel variants.  The common case (no equal receptor/ligand serials, no
+// clamp needed) has a tuning grid of slots per lane S, receptor atoms per
+// inner step A and minimum CTAs per SM (register cap); the rare cases run
+// one variant.  The tuning value encodes S + 16*(A-1) + 32*(MINB > 4).
+template <typename F>
+cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
+  if (serial || clamp) {
+    if (serial && clamp) return f(k_score_f32w<4, 1, 4, true, true>);
+    if (serial) return f(k_score_f32w<4, 1, 4, true, false>);
+    return f(k_score_f32w<4, 1, 4, false, true>);
+  }
+  switch (tune) {
+    case 4: return f(k_score_f32w<4, 1, 4, false, false>);
+    case 8: return f(k_score_f32w<8, 1, 4, false, false>);
+    case 16 + 6: return f(k_score_f32w<6, 2, 4, false, false>);
+    case 16 + 8: return f(k_score_f32w<8, 2, 4, false, false>);
+    case 32 + 4: return f(k_score_f32w<4, 1, 6, false, false>);
+    case 32 + 16 + 4: return f(k_score_f32w<4, 2, 6, false, false>);
+    default: return f(k_score_f32w<4, 2, 4, false, false>);  // 16 + 4
+  }
+}
+
+cudaError_t occupancy_var(int tune, bool serial, bool clamp, size_t smem, int *per_sm) {
+  return with_variant(tune, serial, clamp, [&](auto kern) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, kWarps * 32, smem);
+  });
+}
+
+cudaError_t launch_var(int tune, const BatchParams &bp, bool serial, bool clamp, size_t smem, int grid,
+                       cudaStream_t st) {
+  return with_variant(tune, serial, clamp, [&](auto kern) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     kern<<<grid, kWarps * 32, smem, st>>>(bp);
     return cudaGetLastError();
-  };
-  if (!serial && !clamp) return go(k_score_f32w<S, A, false, false>);
-  if (serial && !clamp) return go(k_score_f32w<S, A, true, false>);
-  if (!serial && clamp) return go(k_score_f32w<S, A, false, true>);
-  return go(k_score_f32w<S, A, true, true>);
-}
-
-template <int S, int A>
-cudaError_t occupancy_w(bool serial, bool clamp, size_t smem, int *per_sm) {
-  if (!serial && !clamp)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, false, false>, kWarps * 32, smem);
-  if (serial && !clamp)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, true, false>, kWarps * 32, smem);
-  if (!serial && clamp)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, false, true>, kWarps * 32, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_score_f32w<S, A, true, true>, kWarps * 32, smem);
-}
-
-// Kernel variants: slots per lane x receptor atoms per inner step.
-// `slots` encodes both: slots % 16 = S (2/4/6/8), slots / 16 = atoms - 1.
-cudaError_t occupancy_var(int S, int A, bool serial, bool clamp, size_t smem, int *per_sm) {
-  if (A == 2) {
-    switch (S) {
-      case 2: return occupancy_w<2, 2>(serial, clamp, smem, per_sm);
-      case 4: return occupancy_w<4, 2>(serial, clamp, smem, per_sm);
-      case 6: return occupancy_w<6, 2>(serial, clamp, smem, per_sm);
-      default: return occupancy_w<8, 2>(serial, clamp, smem, per_sm);
-    }
-  }
-  switch (S) {
-    case 2: return occupancy_w<2, 1>(serial, clamp, smem, per_sm);
-    case 4: return occupancy_w<4, 1>(serial, clamp, smem, per_sm);
-    case 6: return occupancy_w<6, 1>(serial, clamp, smem, per_sm);
-    default: return occupancy_w<8, 1>(serial, clamp, smem, per_sm);
-  }
-}
-
-cudaError_t launch_var(int S, int A, const BatchParams &bp, bool serial, bool clamp, size_t smem, int grid,
-                       cudaStream_t st) {
-  if (A == 2) {
-    switch (S) {
-      case 2: return launch_w<2, 2>(bp, serial, clamp, smem, grid, st);
-      case 4: return launch_w<4, 2>(bp, serial, clamp, smem, grid, st);
-      case 6: return launch_w<6, 2>(bp, serial, clamp, smem, grid, st);
-      default: return launch_w<8, 2>(bp, serial, clamp, smem, grid, st);
-    }
-  }
-  switch (S) {
-    case 2: return launch_w<2, 1>(bp, serial, clamp, smem, grid, st);
-    case 4: return launch_w<4, 1>(bp, serial, clamp, smem, grid, st);
-    case 6: return launch_w<6, 1>(bp, serial, clamp, smem, grid, st);
-    default: return launch_w<8, 1>(bp, serial, clamp, smem, grid, st);
-  }
+  });
 }
 
 }  // namespace
 
+// Work items are taken from the queue in descriptor order: put the complexes
+// with the costliest poses first so that the last items of a launch are the
+// cheap ones (longest-processing-time-first).
+static std::vector<ScoreParams> lpt_order(const std::vector<ScoreParams> &descs) {
+  std::vector<ScoreParams> v = descs;
+  std::stable_sort(v.begin(), v.end(), [](const ScoreParams &a, const ScoreParams &b) {
+    return static_cast<long long>(a.nr) * a.nl > static_cast<long long>(b.nr) * b.nl;
+  });
+  return v;
+}
+
 // Launch geometry of a batch: slots per lane, shared memory, grid.
 struct BatchPlan {
-  int S, A, smem_cnt, max_nr, grid;
+  int tune, smem_cnt, max_nr, grid;
   size_t smem;
   std::vector<long long> start;
 };
@@ -532,11 +519,9 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   }
   pl->smem_cnt = pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0;
   pl->smem = warp_layout(pl->smem_cnt).total * kWarps;
-  const int sv = slots % 16;
-  pl->S = sv <= 2 ? 2 : (sv <= 4 ? 4 : (sv <= 6 ? 6 : 8));
-  pl->A = slots / 16 >= 1 ? 2 : 1;
+  pl->tune = slots;
   int per_sm = 0;
-  cudaError_t e = occupancy_var(pl->S, pl->A, serial, clamp, pl->smem, &per_sm);
+  cudaError_t e = occupancy_var(pl->tune, serial, clamp, pl->smem, &per_sm);
   if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
   const long long items = pl->start[ncx];
@@ -575,7 +560,7 @@ static gd_status run_batch(gd_context *ctx, const std::vector<ScoreParams> &desc
   bp.max_nr = pl.max_nr;
   bp.warp_smem = static_cast<int>(warp_layout(pl.smem_cnt).total);
   bp.err = ctx->d_err;
-  e = launch_var(pl.S, pl.A, bp, serial, clamp, pl.smem, pl.grid, stream);
+  e = launch_var(pl.tune, bp, serial, clamp, pl.smem, pl.grid, stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
   return GD_OK;
 }
@@ -587,8 +572,9 @@ static size_t arg_bytes(int ncx) {
 
 // Score the poses of several complexes in one persistent launch (FP32 form).
 // descs[c] describes complex c with its frames/models, outputs and pose count.
-gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
+gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams> &descs_in, bool serial, bool clamp,
                                  int slots, cudaStream_t stream) {
+  const std::vector<ScoreParams> descs = lpt_order(descs_in);
   const int ncx = static_cast<int>(descs.size());
   if (ncx == 0) return GD_OK;
   BatchPlan pl;
@@ -616,9 +602,10 @@ struct BatchLaunch {
   int ncx = 0;
 };
 
-gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp, int slots,
+gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs_in, bool serial, bool clamp, int slots,
                         BatchLaunch **out) {
   *out = nullptr;
+  const std::vector<ScoreParams> descs = lpt_order(descs_in);
   BatchLaunch *b = new BatchLaunch();
   b->serial = serial;
   b->clamp = clamp;
@@ -672,7 +659,7 @@ gd_status batch_launch(gd_context *ctx, BatchLaunch *b, cudaStream_t stream) {
   bp.warp_smem = static_cast<int>(warp_layout(b->plan.smem_cnt).total);
   bp.err = ctx->d_err;
   const BatchPlan &pl = b->plan;
-  e = launch_var(pl.S, pl.A, bp, b->serial, b->clamp, pl.smem, pl.grid, stream);
+  e = launch_var(pl.tune, bp, b->serial, b->clamp, pl.smem, pl.grid, stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
   return GD_OK;
 }
@@ -743,7 +730,7 @@ extern "C" gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pos
   gd_status s = noalloc_scratch(ctx, &scratch);
   if (s != GD_OK) return s;
   const std::vector<ScoreParams> descs{make_params(cx, d_frames, nullptr, n, d_out, max_displacement)};
-  const int slots = ctx->tune_f32_slots ? ctx->tune_f32_slots : 4;
+  const int slots = ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4;
   BatchPlan pl;
   s = plan_batch(ctx, descs, cx->serial_overlap, cx->need_clamp, slots, &pl);
   if (s != GD_OK) return s;

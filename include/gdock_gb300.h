@@ -101,9 +101,11 @@ const char *gd_status_string(gd_status s);
 gd_status gd_context_create(int32_t device, uint64_t hbm_budget_bytes, gd_context **out);
 gd_status gd_context_destroy(gd_context *ctx);
 /* Tuning knobs of the context's kernels (the autotuner sets these).
- *   GD_TUNE_F32_SLOTS: ligand atoms per lane per pass of the FP32 scoring
- *                      kernel (2, 4, 6 or 8; 0 = automatic), plus 16 to
- *                      evaluate two receptor atoms per inner step. */
+ *   GD_TUNE_F32_SLOTS: variant of the FP32 scoring kernel: ligand slots per
+ *                      lane (4, 6 or 8), plus 16 to evaluate two receptor
+ *                      atoms per inner step, plus 32 for the register cap of
+ *                      six resident CTAs per SM; valid: 4, 8, 20, 22, 24, 36,
+ *                      52; 0 = automatic (20). */
 enum { GD_TUNE_F32_SLOTS = 0 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob);

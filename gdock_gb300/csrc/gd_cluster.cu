@@ -23,6 +23,7 @@
 // compaction, and the greedy clustering over the adjacency bit matrix.
 #include <algorithm>
 #include <chrono>
+#include <iterator>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -40,6 +41,8 @@ struct ClusterTopo {
   std::vector<int> rg_off, lg_off;      // atom ranges
   std::vector<int> r_atoms, l_atoms;    // original atom indices, grouped
   bool multi_chain_rec = false, multi_chain_lig = false;
+  bool mixed = false;  // a (chain, resseq) residue with atoms in both molecules
+  float4 *d_r32 = nullptr;  // receptor heavy atoms (x-O, y-O, z-O, 0) FP32, grouped
   std::vector<int64_t> rr_keys;         // receptor-only inter-chain contacts (pose independent)
   double rr_cutoff = -1.0;
   // device
@@ -244,6 +247,149 @@ __global__ void k_compact_lists(const uint32_t *lists, const int *counts, const 
   }
 }
 
+// ---- contact bitmaps on the device (single-chain receptor and ligand) ----
+
+struct BitsParams {
+  const float4 *r32;
+  const double *rx, *ry, *rz;
+  const int *rg_off;
+  const float4 *rg_sph;
+  const uint8_t *rg_chain;
+  const double *lx, *ly, *lz;
+  const int *lg_off;
+  const D4 *lg_sph;
+  const uint8_t *lg_chain;
+  int GR, GL;
+  double cx, cy, cz, ox, oy, oz;
+  const gd_pose_frame *frames;
+  int n;
+  double t_le;       // exact decision d2 <= t_le
+  float t32, guard;  // FP32 decision d2 <= t32 outside |d2 - t32| < guard
+  float reach;
+  uint32_t *bits;    // [n][words], bit rg*GL + lg
+  long long words;
+};
+
+// One warp per (pose, ligand residue): the residue's atoms are transformed
+// exactly and kept in FP64 and FP32; each lane tests receptor residues (culled
+// by bounding spheres), first in FP32, re-deciding in FP64 the atom pairs
+// whose FP32 d2 is within the guard band of the cutoff.
+__global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsParams p) {
+  __shared__ double s_xyz[kContactWarps][3][kMaxGroupAtoms];
+  __shared__ float4 s_f[kContactWarps][kMaxGroupAtoms];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long items = static_cast<long long>(p.n) * p.GL;
+  for (long long it = static_cast<long long>(blockIdx.x) * kContactWarps + wib; it < items;
+       it += static_cast<long long>(gridDim.x) * kContactWarps) {
+    const int pose = static_cast<int>(it / p.GL), lg = static_cast<int>(it % p.GL);
+    const gd_pose_frame f = p.frames[pose];
+    const int a0 = p.lg_off[lg], na = min(p.lg_off[lg + 1] - a0, kMaxGroupAtoms);
+    for (int a = lane; a < na; a += 32) {
+      double X, Y, Z;
+      xform(f, p.cx, p.cy, p.cz, p.lx[a0 + a], p.ly[a0 + a], p.lz[a0 + a], X, Y, Z);
+      s_xyz[wib][0][a] = X;
+      s_xyz[wib][1][a] = Y;
+      s_xyz[wib][2][a] = Z;
+      s_f[wib][a] = make_float4(static_cast<float>(X - p.ox), static_cast<float>(Y - p.oy),
+                                static_cast<float>(Z - p.oz), 0.0f);
+    }
+    __syncwarp();
+    const D4 ls = p.lg_sph[lg];
+    double CX, CY, CZ;
+    xform(f, p.cx, p.cy, p.cz, ls.x, ls.y, ls.z, CX, CY, CZ);
+    const float lcx = static_cast<float>(CX - p.ox), lcy = static_cast<float>(CY - p.oy),
+                lcz = static_cast<float>(CZ - p.oz);
+    const float lrad = static_cast<float>(ls.w);
+    const uint8_t lchain = p.lg_chain[lg];
+    uint32_t *row = p.bits + static_cast<size_t>(pose) * p.words;
+    for (int rg = lane; rg < p.GR; rg += 32) {
+      if (p.rg_chain[rg] == lchain) continue;
+      const float4 rs = p.rg_sph[rg];
+      const float dx = rs.x - lcx, dy = rs.y - lcy, dz = rs.z - lcz;
+      const float lim = rs.w + lrad + p.reach;
+      if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+      bool found = false;
+      for (int b = p.rg_off[rg]; b < p.rg_off[rg + 1] && !found; ++b) {
+        const float4 rb = p.r32[b];
+        for (int a = 0; a < na; ++a) {
+          const float4 la = s_f[wib][a];
+          const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
+          const float d2 = ex * ex + ey * ey + ez * ez;
+          if (d2 > p.t32 + p.guard) continue;
+          if (d2 < p.t32 - p.guard ||
+              d2_exact(p.rx[b], p.ry[b], p.rz[b], s_xyz[wib][0][a], s_xyz[wib][1][a], s_xyz[wib][2][a]) <= p.t_le) {
+            found = true;
+            break;
+          }
+        }
+      }
+      if (found) {
+        const long long idx = static_cast<long long>(rg) * p.GL + lg;
+        atomicOr(&row[idx >> 5], 1u << (idx & 31));
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Union over poses and set-bit count of each bitmap word.
+__global__ void k_union(const uint32_t *bits, int n, long long words, uint32_t *ubits, int *ucount) {
+  for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < words;
+       w += static_cast<long long>(gridDim.x) * blockDim.x) {
+    uint32_t u = 0;
+    for (int p = 0; p < n; ++p) u |= bits[static_cast<size_t>(p) * words + w];
+    ubits[w] = u;
+    ucount[w] = __popc(u);
+  }
+}
+
+// Exclusive prefix sum of the per-word counts (one CTA) -> compacted offsets.
+__global__ void __launch_bounds__(1024) k_scan(const int *cnt, long long words, int *base, int *total) {
+  __shared__ int s[1024];
+  const int t = threadIdx.x;
+  const long long per = (words + 1023) / 1024;
+  const long long w0 = t * per, w1 = min(words, w0 + per);
+  int sum = 0;
+  for (long long w = w0; w < w1; ++w) sum += cnt[w];
+  s[t] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int v = t >= o ? s[t - o] : 0;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  int run = s[t] - sum;
+  for (long long w = w0; w < w1; ++w) {
+    base[w] = run;
+    run += cnt[w];
+  }
+  if (t == 1023) *total = s[1023];
+}
+
+// Pose bitsets over the compacted universe: bit base[w] + rank of the bit
+// within ubits[w].
+__global__ void k_compact(const uint32_t *bits, const uint32_t *ubits, const int *base, int n, long long words, int W,
+                          unsigned long long *out, int *sizes) {
+  for (long long it = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; it < static_cast<long long>(n) * words;
+       it += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int p = static_cast<int>(it / words);
+    const long long w = it % words;
+    const uint32_t u = ubits[w];
+    if (!u) continue;
+    uint32_t v = bits[static_cast<size_t>(p) * words + w] & u;
+    if (!v) continue;
+    atomicAdd(&sizes[p], __popc(v));
+    unsigned long long *row = out + static_cast<size_t>(p) * W;
+    while (v) {
+      const int b = __ffs(v) - 1;
+      v &= v - 1;
+      const int pos = base[w] + __popc(u & ((1u << b) - 1u));
+      atomicOr(&row[pos >> 6], 1ull << (pos & 63));
+    }
+  }
+}
+
 // host mirror of the device transform (same operation order, no fused ops)
 void xform_host(const gd_pose_frame &f, double cx, double cy, double cz, double xo, double yo, double zo, double &X,
                 double &Y, double &Z) {
@@ -325,6 +471,11 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
   t->GL = static_cast<int>(t->lg_key.size());
   for (int g = 1; g < t->GR; ++g) t->multi_chain_rec |= (t->rg_key[g] >> 16) != (t->rg_key[0] >> 16);
   for (int g = 1; g < t->GL; ++g) t->multi_chain_lig |= (t->lg_key[g] >> 16) != (t->lg_key[0] >> 16);
+  {
+    std::vector<int64_t> a = t->rg_key, b = t->lg_key, both;
+    std::set_intersection(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(both));
+    t->mixed = !both.empty();
+  }
   std::vector<double> rx, ry, rz, lx, ly, lz;
   for (int i : t->r_atoms) {
     rx.push_back(cx->h_rx[i]);
@@ -336,6 +487,10 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
     ly.push_back(cx->h_ly[i]);
     lz.push_back(cx->h_lz[i]);
   }
+  std::vector<float4> r32(rx.size());
+  for (size_t a = 0; a < rx.size(); ++a)
+    r32[a] = make_float4(static_cast<float>(rx[a] - cx->ox), static_cast<float>(ry[a] - cx->oy),
+                         static_cast<float>(rz[a] - cx->oz), 0.0f);
   std::vector<float4> rsph(t->GR);
   std::vector<uint8_t> rch(t->GR), lch(t->GL);
   for (int g = 0; g < t->GR; ++g) {
@@ -379,7 +534,7 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
       (s = topo_upload(ctx, t, t->rg_off, &t->d_rg_off)) != GD_OK ||
       (s = topo_upload(ctx, t, t->lg_off, &t->d_lg_off)) != GD_OK || (s = topo_upload(ctx, t, rsph, &t->d_rg_sph)) != GD_OK ||
       (s = topo_upload(ctx, t, lsph, &t->d_lg_sph)) != GD_OK || (s = topo_upload(ctx, t, rch, &t->d_rg_chain)) != GD_OK ||
-      (s = topo_upload(ctx, t, lch, &t->d_lg_chain)) != GD_OK) {
+      (s = topo_upload(ctx, t, lch, &t->d_lg_chain)) != GD_OK || (s = topo_upload(ctx, t, r32, &t->d_r32)) != GD_OK) {
     for (void *p : t->allocs) cudaFree(p);
     ctx->in_use -= std::min<uint64_t>(ctx->in_use, t->bytes);
     delete t;
@@ -656,6 +811,137 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
   return GD_OK;
 }
 
+// cluster_structures entirely on the device for a single-chain receptor and
+// ligand that share no residue: contact bitmaps, union, compaction, FCC; the
+// greedy pass runs on the host.  Returns GD_ERR_STATE when the topology or the
+// bitmap size calls for the general path.
+gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cluster_cfg &cfg, int32_t *n_clusters,
+                         int32_t *centers, int32_t *sizes, int32_t *members) {
+  gd_context *ctx = cx->ctx;
+  PhaseTimer pt_all("cluster (device): total");
+  ClusterTopo *t = nullptr;
+  gd_status s = get_topo(cx, &t);
+  if (s != GD_OK) return s;
+  if (t->multi_chain_rec || t->multi_chain_lig || t->mixed) return GD_ERR_STATE;
+  for (int g = 0; g < t->GL; ++g)
+    if (t->lg_off[g + 1] - t->lg_off[g] > kMaxGroupAtoms) return GD_ERR_STATE;  // residues staged whole
+  const long long pairs = static_cast<long long>(t->GR) * t->GL;
+  const long long words = std::max<long long>(1, (pairs + 31) / 32);
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t bits_b = sizeof(uint32_t) * words * static_cast<size_t>(n);
+  if (bits_b > (static_cast<size_t>(8) << 30)) return GD_ERR_STATE;  // > 8 GiB of bitmaps
+  const Thresholds thr = make_thresholds(cfg.contact_distance);
+  std::vector<gd_pose_frame> frames(n);
+  gd_make_frames(genes, n, frames.data());
+  double maxd = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int k = 3; k < 6; ++k) maxd = std::max(maxd, std::fabs(genes[6 * static_cast<size_t>(i) + k]));
+  const size_t fb = sizeof(gd_pose_frame) * n, ub = sizeof(uint32_t) * words, cb = sizeof(int) * words;
+  // the compacted universe is at most min(pairs, sum of sizes); size it after the scan
+  s = ensure_scratch(ctx, al(fb) + al(bits_b) + al(ub) + 2 * al(cb) + al(sizeof(int)), 0);
+  if (s != GD_OK) return s;
+  char *base = static_cast<char *>(ctx->d_scratch);
+  gd_pose_frame *d_frames = reinterpret_cast<gd_pose_frame *>(base);
+  uint32_t *d_bits = reinterpret_cast<uint32_t *>(base + al(fb));
+  uint32_t *d_u = reinterpret_cast<uint32_t *>(base + al(fb) + al(bits_b));
+  int *d_cnt = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub));
+  int *d_base = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub) + al(cb));
+  int *d_total = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub) + 2 * al(cb));
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(d_frames, frames.data(), fb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bits, 0, bits_b, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps setup");
+  BitsParams p{};
+  p.r32 = t->d_r32;
+  p.rx = t->d_rx;
+  p.ry = t->d_ry;
+  p.rz = t->d_rz;
+  p.rg_off = t->d_rg_off;
+  p.rg_sph = t->d_rg_sph;
+  p.rg_chain = t->d_rg_chain;
+  p.lx = t->d_lx;
+  p.ly = t->d_ly;
+  p.lz = t->d_lz;
+  p.lg_off = t->d_lg_off;
+  p.lg_sph = t->d_lg_sph;
+  p.lg_chain = t->d_lg_chain;
+  p.GR = t->GR;
+  p.GL = t->GL;
+  p.cx = cx->cx;
+  p.cy = cx->cy;
+  p.cz = cx->cz;
+  p.ox = cx->ox;
+  p.oy = cx->oy;
+  p.oz = cx->oz;
+  p.frames = d_frames;
+  p.n = n;
+  p.t_le = thr.contact_le;
+  p.t32 = static_cast<float>(thr.contact_le);
+  {
+    // FP32 error bound of d2 near the cutoff (as for the scoring guard bands)
+    const double u = std::ldexp(1.0, -24), c = cfg.contact_distance;
+    const double M = std::max(cx->rec_extent, cx->lig_radius + maxd +
+                                                  std::max({std::fabs(cx->cx - cx->ox), std::fabs(cx->cy - cx->oy),
+                                                            std::fabs(cx->cz - cx->oz)})) + 1.0;
+    const double err = 2.0 * c * std::sqrt(3.0) * (2.0 * M * u + c * u) + 4.0 * c * c * u;
+    p.guard = static_cast<float>(4.0 * err + 1e-6);
+  }
+  p.reach = static_cast<float>(cfg.contact_distance) + 0.05f;
+  p.bits = d_bits;
+  p.words = words;
+  if (pairs > 0 && n > 0) {
+    const long long items = static_cast<long long>(n) * t->GL;
+    const int grid = static_cast<int>(std::min<long long>((items + kContactWarps - 1) / kContactWarps,
+                                                          static_cast<long long>(ctx->sm_count) * 16));
+    k_contact_bits<<<grid, kContactWarps * 32, 0, st>>>(p);
+  }
+  const int g2 = static_cast<int>(std::min<long long>((words + 255) / 256, static_cast<long long>(ctx->sm_count) * 8));
+  k_union<<<std::max(g2, 1), 256, 0, st>>>(d_bits, n, words, d_u, d_cnt);
+  k_scan<<<1, 1024, 0, st>>>(d_cnt, words, d_base, d_total);
+  int U = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&U, d_total, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps");
+  trace("cluster (device): contacts + union", std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+  const int W = std::max(1, (U + 63) / 64);
+  const int aw = (n + 31) / 32;
+  const size_t compact_b = sizeof(unsigned long long) * static_cast<size_t>(W) * n, sz_b = sizeof(int) * n,
+               adj_b = sizeof(uint32_t) * static_cast<size_t>(n) * aw;
+  void *extra = nullptr;
+  s = dev_alloc(ctx, al(compact_b) + al(sz_b) + al(adj_b), &extra);
+  if (s != GD_OK) return s;
+  unsigned long long *d_compact = static_cast<unsigned long long *>(extra);
+  int *d_sizes = reinterpret_cast<int *>(static_cast<char *>(extra) + al(compact_b));
+  uint32_t *d_adj = reinterpret_cast<uint32_t *>(static_cast<char *>(extra) + al(compact_b) + al(sz_b));
+  e = cudaMemsetAsync(extra, 0, al(compact_b) + al(sz_b) + al(adj_b), st);
+  if (e == cudaSuccess) {
+    const long long tot = static_cast<long long>(n) * words;
+    const int g3 = static_cast<int>(std::min<long long>((tot + 255) / 256, static_cast<long long>(ctx->sm_count) * 32));
+    k_compact<<<std::max(g3, 1), 256, 0, st>>>(d_bits, d_u, d_base, n, words, W, d_compact, d_sizes);
+    FccParams fp{};
+    fp.bits = d_compact;
+    fp.sizes = d_sizes;
+    fp.n = n;
+    fp.W = W;
+    fp.c = cfg.fcc_cutoff;
+    fp.cs = cfg.fcc_cutoff * cfg.strictness;
+    fp.adj = d_adj;
+    fp.adj_words = aw;
+    dim3 grid((n + kFT - 1) / kFT, (n + kFT - 1) / kFT);
+    k_fcc<<<grid, 256, 0, st>>>(fp);
+    e = cudaGetLastError();
+  }
+  std::vector<uint32_t> adj(static_cast<size_t>(n) * aw);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(adj.data(), d_adj, adj_b, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  dev_free(ctx, extra, al(compact_b) + al(sz_b) + al(adj_b));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC on the device");
+  trace("cluster (device): compact + fcc", std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+  *n_clusters = greedy_clusters(adj, n, aw, cfg.min_cluster_size, centers, sizes, members);
+  return GD_OK;
+}
+
 }  // namespace gd
 
 using namespace gd;
@@ -690,8 +976,11 @@ gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cl
   *n_clusters = 0;
   if (n == 0) return GD_OK;  // cluster_structures on no structures
   cudaSetDevice(ctx->device);
+  gd_status s = cluster_device(cx, genes, n, c, n_clusters, centers, sizes, members);
+  if (s != GD_ERR_STATE) return s;
+  // multi-chain molecules or shared residues: contact keys on the host path
   std::vector<int64_t> k, o;
-  gd_status s = pose_contacts_host(cx, genes, n, c.contact_distance, k, o);
+  s = pose_contacts_host(cx, genes, n, c.contact_distance, k, o);
   if (s != GD_OK) return s;
   return cluster_sets(ctx, k.data(), o.data(), n, c, n_clusters, centers, sizes, members);
 }

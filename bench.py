@@ -137,6 +137,12 @@ def cpu_sample(c, lig, genes, n_sample, threads):
     return n_sample / (time.perf_counter() - t0)
 
 
+def variant_name(tune: int) -> str:
+    """GD_TUNE_F32_SLOTS value -> 'S<slots per lane>xA<receptor rows per step>'."""
+    a = 4 if tune & 64 else (2 if tune & 16 else 1)
+    return f"S{tune % 16}xA{a}"
+
+
 def replica_throughput(t_step: float, units: int, world: int, device: str = "cpu"):
     """Replicas-only scaling: every rank scores its own `units` poses; the job
     takes as long as the slowest rank, and all ranks' poses count.
@@ -367,7 +373,7 @@ def main():
 
     # --- slots-per-lane sweep (a small autotune on a pose sample) ---
     tune = {}
-    for slots in (4, 8, 16 + 4, 16 + 6, 16 + 8, 32 + 4, 32 + 16 + 4):  # see GD_TUNE_F32_SLOTS
+    for slots in (4, 16 + 4, 64 + 2, 64 + 4):  # see GD_TUNE_F32_SLOTS
         ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
         ns_t = min(NP, 16384)
         launch(gd.GD_PREC_F32, ns_t)
@@ -448,10 +454,8 @@ def main():
             "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES,
                     "d2h_bytes_per_step": NP * 48},
             "gpu_launches": args.steps,
-            "autotune": {"f32_slots": best_slots % 16, "receptor_atoms_per_step": 1 + (best_slots // 16) % 2,
-                         "min_ctas_per_sm": 6 if best_slots >= 32 else 4,
-                         "poses_per_s_by_variant": {f"S{k % 16}xA{1 + (k // 16) % 2}xB{6 if k >= 32 else 4}": v
-                                                    for k, v in tune.items()}},
+            "autotune": {"variant": variant_name(best_slots),
+                         "poses_per_s_by_variant": {variant_name(k): v for k, v in tune.items()}},
             "pair_evals_per_s": pairs * value,
             "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,
                            "tflops": FLOP_PER_PAIR * pairs * plain / 1e12,

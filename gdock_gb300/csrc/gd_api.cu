@@ -313,13 +313,13 @@ const char *gd_last_error(const gd_context *ctx) { return ctx ? ctx->last_error.
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (knob == GD_TUNE_F32_SLOTS) {
-    static const int kValid[] = {0, 4, 8, 16 + 4, 16 + 6, 16 + 8, 32 + 4, 32 + 16 + 4};
+    static const int kValid[] = {0, 4, 16 + 4, 64 + 2, 64 + 4};
     bool ok = false;
     for (int v : kValid) ok = ok || v == value;
     if (!ok)
       return fail(ctx, GD_ERR_INVALID_ARG,
-                  "F32 tuning: one of 4, 8, 20, 22, 24, 36, 52 (slots + 16 for two atoms per step + 32 for the "
-                  "higher-occupancy register cap)");
+                  "F32 tuning: one of 4, 20, 66, 68 (ligand slots per lane + 16 or 64 for two or four "
+                  "receptor rows per step)");
     ctx->tune_f32_slots = value;
     return GD_OK;
   }
@@ -412,27 +412,6 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
     ext = std::max({ext, std::fabs(rec->x[i] - o[0]), std::fabs(rec->y[i] - o[1]), std::fabs(rec->z[i] - o[2])});
   }
   cx->rec_extent = ext;
-  // culling spheres of 8-atom receptor blocks: centre (FP32 frame) and
-  // radius + 15 A + margin, so that a block further than this from a ligand
-  // atom holds no pair with any nonzero term
-  std::vector<float4> rsph(std::max(cx->nr_pad / 8, 1), make_float4(0.f, 0.f, 0.f, -1.0e30f));
-  for (int b = 0; b * 8 < rec->n; ++b) {
-    const int a0 = b * 8, a1 = std::min(rec->n, a0 + 8);
-    double c3[3] = {0, 0, 0};
-    for (int i = a0; i < a1; ++i) {
-      c3[0] += rec->x[i] - o[0];
-      c3[1] += rec->y[i] - o[1];
-      c3[2] += rec->z[i] - o[2];
-    }
-    for (double &v : c3) v /= (a1 - a0);
-    double r = 0.0;
-    for (int i = a0; i < a1; ++i) {
-      const double dx = rec->x[i] - o[0] - c3[0], dy = rec->y[i] - o[1] - c3[1], dz = rec->z[i] - o[2] - c3[2];
-      r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
-    }
-    rsph[b] = make_float4(static_cast<float>(c3[0]), static_cast<float>(c3[1]), static_cast<float>(c3[2]),
-                          static_cast<float>(r * 1.0001 + 0.01 + 15.0));
-  }
   std::vector<double> lx(lig->x, lig->x + lig->n), ly(lig->y, lig->y + lig->n), lz(lig->z, lig->z + lig->n);
   std::vector<double> lq(lig->charge, lig->charge + lig->n);
   std::vector<int> lser(lig->serial, lig->serial + lig->n);
@@ -469,7 +448,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
 
   gd_status s;
   if ((s = upload(cx, rp32, &cx->rec_pos32)) != GD_OK || (s = upload(cx, rp64, &cx->rec_pos64)) != GD_OK ||
-      (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rsph, &cx->rec_sph32)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
+      (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
       (s = upload(cx, lx, &cx->lig_x)) != GD_OK || (s = upload(cx, ly, &cx->lig_y)) != GD_OK ||
       (s = upload(cx, lz, &cx->lig_z)) != GD_OK || (s = upload(cx, lq, &cx->lig_q)) != GD_OK ||
       (s = upload(cx, ltype, &cx->lig_type)) != GD_OK || (s = upload(cx, lser, &cx->lig_serial)) != GD_OK ||

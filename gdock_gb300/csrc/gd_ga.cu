@@ -417,7 +417,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     }
     BatchLaunch *bl = nullptr;
     if (prec == GD_PREC_F32) {
-      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4, &bl);
+      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune, &bl);
       if (s != GD_OK) goto done;
     }
     GaStepParams P{};
@@ -755,7 +755,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
     if (S->dirty || !S->bl) {
       if (S->bl) batch_free(ctx, S->bl);
       S->bl = nullptr;
-      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4, &S->bl);
+      s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune, &S->bl);
       S->dirty = false;
     }
     if (s == GD_OK) s = batch_launch(ctx, S->bl, st);

@@ -24,6 +24,9 @@ constexpr uint32_t kSpinLimit = 1u << 26;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 // Distinct (epsilon, Rmin/2) atom types a complex may hold.
 constexpr int kMaxTypes = 64;
+// FP32 scoring variant when none is set: 4 ligand slots per lane, 4 receptor
+// rows per step (GD_TUNE_F32_SLOTS encoding)
+constexpr int kDefaultF32Tune = 64 + 4;
 
 // device error codes written to the context's error word
 enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };
@@ -56,7 +59,6 @@ struct ScoreParams {
   // receptor, sorted by atom type, padded to a multiple of kTile
   const float4 *rec_pos32;  // (x-O, y-O, z-O, 332.0636*q) FP32
   const D4 *rec_pos64; // (x, y, z, q) FP64
-  const float4 *rec_sph32;  // per 8-atom block: (centre - O, radius + 15 A reach)
   const int2 *rec_meta;     // (type, serial)
   const double *rec_desolv; // [nr * 11] energy contribution at burial count 0..10
   int nr, n_tiles;
@@ -109,7 +111,7 @@ struct gd_context {
   void *d_batch = nullptr;
   size_t d_batch_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int tune_f32_slots = 0;  // 0: automatic
+  int tune_f32_slots = 0;  // 0: automatic (kDefaultF32Tune)
 };
 
 struct gd_complex {
@@ -124,7 +126,6 @@ struct gd_complex {
   // device arrays
   float4 *rec_pos32 = nullptr;
   D4 *rec_pos64 = nullptr;
-  float4 *rec_sph32 = nullptr;
   int2 *rec_meta = nullptr;
   double *rec_desolv = nullptr;
   double *lig_x = nullptr, *lig_y = nullptr, *lig_z = nullptr, *lig_q = nullptr;

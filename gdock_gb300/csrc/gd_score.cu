@@ -244,7 +244,6 @@ ScoreParams make_params(gd_complex *cx, const gd_pose_frame *d_frames, const dou
   ScoreParams p{};
   p.rec_pos32 = cx->rec_pos32;
   p.rec_pos64 = cx->rec_pos64;
-  p.rec_sph32 = cx->rec_sph32;
   p.rec_meta = cx->rec_meta;
   p.rec_desolv = cx->rec_desolv;
   p.nr = cx->nr;
@@ -292,7 +291,7 @@ gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const doub
   const bool serial = cx->serial_overlap, clamp = cx->need_clamp;
   if (prec == GD_PREC_F32)
     return launch_score_batch_f32(ctx, std::vector<ScoreParams>{p}, serial, clamp,
-                                  ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4, stream);
+                                  ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune, stream);
   cudaError_t e;
   const size_t smem = smem_layout<D4>(p.nt, p.nr, kNT, sizeof(D4)).total;
   const int S = std::max(1, std::min(4, (p.nl + kNT - 1) / kNT));

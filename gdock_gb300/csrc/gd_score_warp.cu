@@ -10,15 +10,17 @@
 //      copies in registers (S slots of 32 consecutive atoms, one per lane) and
 //      a bounding sphere per slot;
 //   3. streams the receptor through its own ring of shared-memory stages, each
-//      filled by one bulk (TMA) copy of 64 atoms + 8 culling spheres and
-//      guarded by a per-warp mbarrier;
-//   4. per 8-atom receptor block, finds the slots whose sphere is within the
-//      15 A cutoff reach (all other pairs contribute exactly nothing) and
-//      evaluates those pairs four receptor atoms at a time (independent
-//      FP32 chains for ILP): soft-core LJ, Coulomb, burial counts, guard band;
-//   5. re-decides in FP64 any pair whose FP32 d2 lies within the guard band of
+//      filled by one bulk (TMA) copy of 64 atoms and guarded by a per-warp
+//      mbarrier;
+//   4. row test: each lane takes one (receptor atom, slot) row of an 8 x 4
+//      round and keeps it when the atom lies within the 15 A reach of the
+//      slot's sphere (every pair of a dropped row contributes exactly
+//      nothing); kept rows go to per-slot lists in shared memory;
+//   5. evaluates the kept rows four at a time (independent FP32 chains):
+//      soft-core LJ, Coulomb, burial counts, guard band;
+//   6. re-decides in FP64 any pair whose FP32 d2 lies within the guard band of
 //      a cutoff (1, 8, 12, 15 A), so all decisions equal the FP64 ones;
-//   6. reduces in FP64: per-lane Kahan partials, warp sums, desolvation from
+//   7. reduces in FP64: per-lane Kahan partials, warp sums, desolvation from
 //      the exact burial counts, AIR in restraint order (bit-identical), and
 //      writes the six-field record (src/chromosome.rs:110-127).
 #include <algorithm>
@@ -36,7 +38,10 @@ namespace {
 constexpr int kWarps = 4;      // warps per CTA (independent)
 constexpr int kSeg = 64;       // receptor atoms per ring stage
 constexpr int kWS = 4;         // ring stages per warp
-constexpr int kBlk = 8;        // receptor atoms per culling sphere
+constexpr int kBlk = 8;        // receptor atoms per row-test round (lane = slot * 8 + atom)
+constexpr int kMaxS = 4;       // ligand slots per lane, at most (one row-test round covers 8 atoms x 4 slots)
+constexpr int kList = kSeg + 4;  // row-list entries per slot: a segment's atoms + padding for 4 rows per step
+constexpr int kFar = kWS * kSeg; // shared-memory index of the far-away dummy receptor atom
 constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
 
 struct BatchParams {
@@ -54,7 +59,7 @@ struct BatchParams {
 };
 
 struct WarpSmem {
-  size_t pos, meta, sph, bars, desc, frame, blob, cnt, total;
+  size_t pos, meta, list, bars, desc, frame, blob, rc, cnt, total;
 };
 
 __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
@@ -62,11 +67,14 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   size_t o = 0;
   auto al = [&](size_t a) { o = (o + a - 1) / a * a; };
   L.pos = o;
-  o += sizeof(float4) * kWS * kSeg;
+  o += sizeof(float4) * (kWS * kSeg + 1);  // + the far dummy atom
+  al(16);
   L.meta = o;
-  o += sizeof(int2) * kWS * kSeg;
-  L.sph = o;
-  o += sizeof(float4) * kWS * (kSeg / kBlk);
+  o += sizeof(int2) * (kWS * kSeg + 1);
+  al(16);
+  L.list = o;
+  o += sizeof(uint16_t) * kMaxS * kList;
+  al(16);
   L.bars = o;
   o += 8 * kWS;
   al(16);
@@ -77,6 +85,8 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   o += sizeof(gd_pose_frame);
   L.blob = o;
   o += sizeof(float4) * 8;
+  L.rc = o;
+  o += sizeof(int) * kSeg;
   L.cnt = o;
   o += smem_cnt;
   al(128);
@@ -85,14 +95,12 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
 }
 
 __device__ __forceinline__ void issue_seg(long long q, int seg, const ScoreParams &p, float4 *s_pos, int2 *s_meta,
-                                          float4 *s_sph, uint64_t *s_bar) {
+                                          uint64_t *s_bar) {
   const int st = static_cast<int>(q % kWS);
-  constexpr uint32_t kBytes = kSeg * (sizeof(float4) + sizeof(int2)) + (kSeg / kBlk) * sizeof(float4);
+  constexpr uint32_t kBytes = kSeg * (sizeof(float4) + sizeof(int2));
   mbar_expect_tx(&s_bar[st], kBytes);
   bulk_g2s(&s_pos[st * kSeg], p.rec_pos32 + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(float4), &s_bar[st]);
   bulk_g2s(&s_meta[st * kSeg], p.rec_meta + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(int2), &s_bar[st]);
-  bulk_g2s(&s_sph[st * (kSeg / kBlk)], p.rec_sph32 + static_cast<size_t>(seg) * (kSeg / kBlk),
-           (kSeg / kBlk) * sizeof(float4), &s_bar[st]);
 }
 
 // acc += v when |t| < lim (one predicated add)
@@ -202,11 +210,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   unsigned char *base = smem + static_cast<size_t>(wib) * L.total;
   float4 *s_pos = reinterpret_cast<float4 *>(base + L.pos);
   int2 *s_meta = reinterpret_cast<int2 *>(base + L.meta);
-  float4 *s_sph = reinterpret_cast<float4 *>(base + L.sph);
+  uint16_t *s_list = reinterpret_cast<uint16_t *>(base + L.list);  // kept rows per slot, as stage indices
   uint64_t *s_bar = reinterpret_cast<uint64_t *>(base + L.bars);
   ScoreParams *s_desc = reinterpret_cast<ScoreParams *>(base + L.desc);
   gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(base + L.frame);
   float4 *s_blob = reinterpret_cast<float4 *>(base + L.blob);
+  int *s_rc = reinterpret_cast<int *>(base + L.rc);  // receptor burial counts of the current segment
   const int gwarp = static_cast<int>(blockIdx.x) * kWarps + wib;
   uint8_t *cnt = bp.smem_cnt ? reinterpret_cast<uint8_t *>(base + L.cnt)
                              : bp.gcounts + static_cast<size_t>(gwarp) * bp.gcount_stride;
@@ -214,11 +223,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   if (lane == 0) {
     for (int s = 0; s < kWS; ++s) mbar_init(&s_bar[s], 1);
     fence_mbar_init();
+    s_pos[kFar] = make_float4(1.0e9f, 1.0e9f, 1.0e9f, 0.0f);  // far from real and idle ligand lanes
+    s_meta[kFar] = make_int2(0, 0);
   }
   for (int i = lane; i < bp.max_nr; i += 32) cnt[i] = 0;
+  for (int i = lane; i < kSeg; i += 32) s_rc[i] = 0;
   __syncwarp();
 
+  static_assert(S >= 1 && S <= kMaxS, "one row-test round covers at most four slots");
   constexpr int kChunk = 32 * S;
+  const int my_s = lane >> 3, my_a = lane & 7;
+  const unsigned my_group = 0xffu << (8 * my_s), lt_mask = (1u << lane) - 1u;
   long long q = 0;  // ring uses of this warp so far
   for (;;) {
     unsigned long long item = 0;
@@ -251,8 +266,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     const long long Qi = static_cast<long long>(nchunks) * nseg;
     const long long q0 = q;
     if (lane == 0)
-      for (long long k = 0; k < Qi && k < kWS; ++k) issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_sph, s_bar);
+      for (long long k = 0; k < Qi && k < kWS; ++k) issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_bar);
     const float gv = p.guard_v, ge = p.guard_e, gdd = p.guard_d;
+    // a row (receptor atom, ligand slot) whose atom lies farther than this
+    // from the slot's bounding sphere has every FP32 d2 beyond the elec
+    // cutoff and its guard band: all its terms, counts and guard tests are 0
+    const float reach = sqrtf(225.01f + 2.0f * ge) + 0.01f;
     const float2 *tab = reinterpret_cast<const float2 *>(p.tab32);
     double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
     bool failed = false;
@@ -275,7 +294,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           lt[s] = p.lig_type[j];
           lser[s] = SERIAL ? p.lig_serial[j] : 0;
         } else {
-          lx[s] = ly[s] = lz[s] = 1.0e9f;  // far away: no term, no count, no guard hit
+          // far from every receptor atom, including the padding at +1e9
+          lx[s] = ly[s] = lz[s] = -1.0e9f;
           lq[s] = 0.0f;
           lt[s] = 0;
           lser[s] = 0;
@@ -300,6 +320,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         if (lane == 0) s_blob[s] = make_float4(cx, cy, cz, on_mask ? rr * 1.0001f + 0.01f : -1.0e30f);
       }
       __syncwarp();
+      // phase-1 role of this lane: row (slot my_s, atom my_a of each 8-atom round)
+      const float4 myb = my_s < S ? s_blob[my_s] : make_float4(0.0f, 0.0f, 0.0f, -1.0e30f);
+      const float mlim = myb.w + reach;
+      const float mlim2 = (myb.w >= 0.0f) ? mlim * mlim : -1.0f;  // empty slot: no row kept
       float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
       for (int g = 0; g < nseg; ++g, ++q) {
         const int st = static_cast<int>(q % kWS);
@@ -310,76 +334,83 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         }
         const int gbase = g * kSeg;
         const int na = min(kSeg, p.nr - gbase);
-        float av = 0.0f, ae = 0.0f;
+        const int sbase = st * kSeg;
+
+        // Phase 1: lane (slot, atom) tests one row against the slot's sphere;
+        // kept rows go to per-slot lists, padded with the far dummy atom.
+        int n_mine = 0;  // rows of this lane's slot
         for (int b0 = 0; b0 < na; b0 += kBlk) {
-          const float4 sp = s_sph[st * (kSeg / kBlk) + b0 / kBlk];  // (centre, radius + cutoff reach)
-          unsigned act = 0;
+          const float4 ra = s_pos[sbase + b0 + my_a];  // atoms past nr are padding far away
+          const float dx = ra.x - myb.x, dy = ra.y - myb.y, dz = ra.z - myb.z;
+          const bool keep = dx * dx + dy * dy + dz * dz < mlim2;
+          const unsigned M = __ballot_sync(kFull, keep);
+          if (keep) s_list[my_s * kList + n_mine + __popc(M & my_group & lt_mask)] = static_cast<uint16_t>(sbase + b0 + my_a);
+          n_mine += __popc(M & my_group);
+        }
+        if (my_s < S && my_a < kAtoms) s_list[my_s * kList + n_mine + my_a] = static_cast<uint16_t>(kFar);
+        __syncwarp();
+
+        // Phase 2: every term of the kept rows, kAtoms rows per step
+        float av = 0.0f, ae = 0.0f;
 #pragma unroll
-          for (int s = 0; s < S; ++s) {
-            const float4 bl = s_blob[s];
-            const float dx = sp.x - bl.x, dy = sp.y - bl.y, dz = sp.z - bl.z;
-            const float lim = sp.w + bl.w;
-            act |= (lim > 0.0f && dx * dx + dy * dy + dz * dz < lim * lim) ? (1u << s) : 0u;
-          }
-          if (act == 0) continue;
-          const int bend = min(b0 + kBlk, na);
+        for (int s = 0; s < S; ++s) {
+          const int n = __shfl_sync(kFull, n_mine, s * 8);
+          const int j = ch * kChunk + s * 32 + lane;
+          const uint16_t *lst = s_list + s * kList;
 #pragma unroll 1
-          for (int h = b0; h < bend; h += kAtoms) {
+          for (int k0 = 0; k0 < n; k0 += kAtoms) {
+            int ix[kAtoms];
             float4 r[kAtoms];
             int rt[kAtoms], rs[kAtoms], rc[kAtoms];
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
+              ix[i] = lst[k0 + i];
+              r[i] = s_pos[ix[i]];
+              const int2 mt = s_meta[ix[i]];
+              rt[i] = mt.x;
+              rs[i] = mt.y;
               rc[i] = 0;
-              if (h + i < bend) {
-                r[i] = s_pos[st * kSeg + h + i];
-                const int2 m = s_meta[st * kSeg + h + i];
-                rt[i] = m.x;
-                rs[i] = m.y;
-              } else {
-                r[i] = make_float4(-1.0e9f, -1.0e9f, -1.0e9f, 0.0f);
-                rt[i] = 0;
-                rs[i] = 0;
-              }
             }
             bool amb = false;
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-              if (!(act & (1u << s))) continue;
-#pragma unroll
-              for (int i = 0; i < kAtoms; ++i)
-                pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], gv, ge, gdd,
-                                      av, ae, lcnt[s], rc[i], amb);
-            }
+            for (int i = 0; i < kAtoms; ++i)
+              pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], gv, ge, gdd,
+                                    av, ae, lcnt[s], rc[i], amb);
             if (__any_sync(kFull, amb)) {
 #pragma unroll
               for (int i = 0; i < kAtoms; ++i) {
-#pragma unroll
-                for (int s = 0; s < S; ++s) {
-                  const int j = ch * kChunk + s * 32 + lane;
-                  if (h + i >= bend || j >= p.nl || !(act & (1u << s))) continue;
-                  if (!near_band(d2f(r[i], lx[s], ly[s], lz[s]), gv, ge, gdd)) continue;
-                  const FixOut fo = fix_pair<SERIAL, CLAMP>(p, f, pose, j, r[i], gbase + h + i, rt[i], rs[i], lx[s],
-                                                            ly[s], lz[s], lq[s], lt[s], lser[s]);
-                  av += fo.dv;
-                  ae += fo.de;
-                  lcnt[s] += fo.dl;
-                  rc[i] += fo.dl;
-                }
+                if (ix[i] == kFar || j >= p.nl) continue;
+                if (!near_band(d2f(r[i], lx[s], ly[s], lz[s]), gv, ge, gdd)) continue;
+                const FixOut fo = fix_pair<SERIAL, CLAMP>(p, f, pose, j, r[i], gbase + ix[i] - sbase, rt[i], rs[i],
+                                                          lx[s], ly[s], lz[s], lq[s], lt[s], lser[s]);
+                av += fo.dv;
+                ae += fo.de;
+                lcnt[s] += fo.dl;
+                rc[i] += fo.dl;
               }
             }
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
               const int tot = __reduce_add_sync(kFull, rc[i]);
-              if (lane == 0 && tot) bump_count(cnt, gbase + h + i, tot);
+              if (lane == 0 && tot) s_rc[ix[i] - sbase] += tot;  // the far atom never counts
             }
           }
         }
         kahan_add(sv, cv, av);
         kahan_add(se, ce, ae);
         __syncwarp();
+        // receptor burial counts of this segment into the per-item counters
+        for (int i = lane; i < na; i += 32) {
+          const int c = s_rc[i];
+          if (c) {
+            bump_count(cnt, gbase + i, c);
+            s_rc[i] = 0;
+          }
+        }
+        __syncwarp();
         const long long k = q - q0;  // index of this use within the item
         if (lane == 0 && k + kWS < Qi)
-          issue_seg(q + kWS, static_cast<int>((k + kWS) % nseg), p, s_pos, s_meta, s_sph, s_bar);
+          issue_seg(q + kWS, static_cast<int>((k + kWS) % nseg), p, s_pos, s_meta, s_bar);
       }
       if (failed) break;
 #pragma unroll
@@ -453,7 +484,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 // Kernel variants.  The common case (no equal receptor/ligand serials, no
 // clamp needed) has a tuning grid of slots per lane S, receptor atoms per
 // inner step A and minimum CTAs per SM (register cap); the rare cases run
-// one variant.  The tuning value encodes S + 16*(A-1) + 32*(MINB > 4).
+// one variant.  The tuning value encodes S + 16 (A = 2) or + 64 (A = 4).
 template <typename F>
 cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
   if (serial || clamp) {
@@ -463,12 +494,10 @@ cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
   }
   switch (tune) {
     case 4: return f(k_score_f32w<4, 1, 4, false, false>);
-    case 8: return f(k_score_f32w<8, 1, 4, false, false>);
-    case 16 + 6: return f(k_score_f32w<6, 2, 4, false, false>);
-    case 16 + 8: return f(k_score_f32w<8, 2, 4, false, false>);
-    case 32 + 4: return f(k_score_f32w<4, 1, 6, false, false>);
-    case 32 + 16 + 4: return f(k_score_f32w<4, 2, 6, false, false>);
-    default: return f(k_score_f32w<4, 2, 4, false, false>);  // 16 + 4
+    case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false>);
+    case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false>);
+    case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false>);
+    default: return f(k_score_f32w<4, 4, 4, false, false>);  // 64 + 4
   }
 }
 
@@ -730,7 +759,7 @@ extern "C" gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pos
   gd_status s = noalloc_scratch(ctx, &scratch);
   if (s != GD_OK) return s;
   const std::vector<ScoreParams> descs{make_params(cx, d_frames, nullptr, n, d_out, max_displacement)};
-  const int slots = ctx->tune_f32_slots ? ctx->tune_f32_slots : 16 + 4;
+  const int slots = ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune;
   BatchPlan pl;
   s = plan_batch(ctx, descs, cx->serial_overlap, cx->need_clamp, slots, &pl);
   if (s != GD_OK) return s;

@@ -3,6 +3,7 @@
 // entry points.  No call throws across the ABI; every failure becomes a
 // gd_status with a message in gd_last_error().
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -381,7 +382,9 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
       const double eps = std::sqrt(t_eps[a] * t_eps[b]);
       const double r6 = powi6(t_rmin[a] + t_rmin[b]);
       tab64[a * nt + b] = TypePair64{r6, 0.5 * r6, eps, 0.0};
-      tab32[a * nt + b] = TypePair32{static_cast<float>(r6), static_cast<float>(eps)};
+      const double inv2 = r6 > 0.0 ? 2.0 / r6 : 0.0;
+      tab32[a * nt + b] = TypePair32{r6 > 0.0 && inv2 < FLT_MAX ? static_cast<float>(inv2) : FLT_MAX,
+                                     static_cast<float>(4.0 * eps)};
       if (eps > 50.0) cx->need_clamp = true;
     }
 

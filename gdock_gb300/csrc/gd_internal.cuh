@@ -38,9 +38,10 @@ struct GaJobState {
   double last_best;
 };
 
-// Per-pair parameters of one type pair, FP32 form: R6 = (Rmin_i + Rmin_j)^6,
-// eps = sqrt(eps_i eps_j).
-struct TypePair32 { float r6, eps; };
+// Per-pair parameters of one type pair, FP32 form, for the soft-core LJ
+// rewritten as eps (q^2 - 2q) = 4 eps x (x - 1) with q = 2x and
+// x = 1 / (r^6 * 2/R6 + 1), R6 = (Rmin_i + Rmin_j)^6, eps = sqrt(eps_i eps_j).
+struct TypePair32 { float inv2, eps4; };  // 2/R6 (FLT_MAX when R6 = 0), 4 eps
 // FP64 form: R6, alpha*R6 (alpha = 0.5), eps.
 struct TypePair64 { double r6, hr6, eps, pad; };
 

@@ -120,19 +120,22 @@ __device__ __forceinline__ float d2f(const float4 &r, float lx, float ly, float 
   return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
-// soft-core LJ in FP32 (src/fitness.rs:57-70): eps*(q^2 - 2q), q = R6/(r^6 + R6/2)
+// soft-core LJ in FP32 (src/fitness.rs:57-70): eps*(q^2 - 2q) with
+// q = R6/(r^6 + R6/2), evaluated as 4 eps x (x - 1), x = q/2 = 1/(r^6 2/R6 + 1)
 template <bool CLAMP>
 __device__ __forceinline__ float vdw_term(float d2, float2 tp) {
   const float r6 = d2 * d2 * d2;
-  const float q = tp.x * rcp_approx(__fmaf_rn(0.5f, tp.x, r6));
-  float v = (q * (q - 2.0f)) * tp.y;
+  const float x = rcp_approx(__fmaf_rn(r6, tp.x, 1.0f));
+  float v = (x * (x - 1.0f)) * tp.y;
   if (CLAMP) v = v < -50.0f ? -50.0f : (v > 500.0f ? 500.0f : v);
   return v;
 }
 
+// One pair's FP32 terms.  The Coulomb sum accumulates q_r / d2 (scaled by
+// the lane's ligand charge once per segment).
 template <bool SERIAL, bool CLAMP>
 __device__ __forceinline__ void pair32(const float4 &r, int rtrow, int rser, const float2 *tab, float lx, float ly,
-                                       float lz, float lq, int lt, int lser, float gv, float ge, float gdd, float &av,
+                                       float lz, int lt, int lser, float gv, float ge, float gdd, float &av,
                                        float &ae, int &lc, int &rc, bool &amb) {
   const float d2 = d2f(r, lx, ly, lz);
   const float v = vdw_term<CLAMP>(d2, __ldg(&tab[rtrow + lt]));
@@ -142,7 +145,7 @@ __device__ __forceinline__ void pair32(const float4 &r, int rtrow, int rser, con
   } else {
     add_if_abs_lt(av, tv, 72.0f, v);
   }
-  const float e = (r.w * lq) * rcp_approx(d2);
+  const float e = r.w * rcp_approx(d2);
   const float te = __fsub_rn(d2, 113.0f);  // 1 < d2 < 225  <=>  |te| < 112
   add_if_abs_lt(ae, te, 112.0f, e);
   count_if_lt64(lc, rc, d2);
@@ -190,7 +193,7 @@ __device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, const gd_pose_f
     o.dv = pv64 ? v : -v;
   }
   if (pe64 != pe32) {
-    const float e = (r.w * lq) * rcp_approx(d2);
+    const float e = (r.w * rcp_approx(d2)) * lq;
     o.de = pe64 ? e : -e;
   }
   if (pd64 != pd32) o.dl = pd64 ? 1 : -1;
@@ -351,9 +354,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         __syncwarp();
 
         // Phase 2: every term of the kept rows, kAtoms rows per step
-        float av = 0.0f, ae = 0.0f;
+        float av = 0.0f, ae = 0.0f;  // ae: corrections from FP64 re-decisions (charge included)
 #pragma unroll
         for (int s = 0; s < S; ++s) {
+          float aes = 0.0f;  // sum of q_r / d2 over this slot's kept pairs
           const int n = __shfl_sync(kFull, n_mine, s * 8);
           const int j = ch * kChunk + s * 32 + lane;
           const uint16_t *lst = s_list + s * kList;
@@ -374,8 +378,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             bool amb = false;
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i)
-              pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lq[s], lt[s], lser[s], gv, ge, gdd,
-                                    av, ae, lcnt[s], rc[i], amb);
+              pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lt[s], lser[s], gv, ge, gdd, av,
+                                    aes, lcnt[s], rc[i], amb);
             if (__any_sync(kFull, amb)) {
 #pragma unroll
               for (int i = 0; i < kAtoms; ++i) {
@@ -389,12 +393,20 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
                 rc[i] += fo.dl;
               }
             }
+            // receptor burial counts of the step's rows: lane i adds row i's
+            // total (distinct atoms; the far atom never counts)
+            int my_t = 0, my_ix = kFar;
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
               const int tot = __reduce_add_sync(kFull, rc[i]);
-              if (lane == 0 && tot) s_rc[ix[i] - sbase] += tot;  // the far atom never counts
+              if (lane == i) {
+                my_t = tot;
+                my_ix = ix[i];
+              }
             }
+            if (my_t) s_rc[my_ix - sbase] += my_t;
           }
+          ae = __fmaf_rn(aes, lq[s], ae);
         }
         kahan_add(sv, cv, av);
         kahan_add(se, ce, ae);

@@ -231,6 +231,62 @@ static gd_status upload(gd_complex *cx, const std::vector<T> &h, T **d) {
   return GD_OK;
 }
 
+// Ligand atoms grouped into spatially compact runs of 32 (one FP32 scoring
+// slot each): repeatedly take the remaining atom farthest from the remaining
+// atoms' centroid and its 31 nearest remaining atoms.  The ligand is rigid, so
+// tight groups keep their small bounding spheres in every pose and the
+// kernel's row test drops more rows.  Deterministic (ties by index).
+// Returns order[k] = original index of the atom at slot position k.
+static std::vector<int> slot_order(const double *x, const double *y, const double *z, int n) {
+  std::vector<int> order;
+  order.reserve(n);
+  if (n > 65536) {  // quadratic grouping: keep chain order for very large ligands
+    for (int j = 0; j < n; ++j) order.push_back(j);
+    return order;
+  }
+  std::vector<int> rest(n);
+  for (int j = 0; j < n; ++j) rest[j] = j;
+  std::vector<std::pair<double, int>> d;
+  while (!rest.empty()) {
+    double c[3] = {0, 0, 0};
+    for (int j : rest) {
+      c[0] += x[j];
+      c[1] += y[j];
+      c[2] += z[j];
+    }
+    for (double &v : c) v /= static_cast<double>(rest.size());
+    int far = rest[0];
+    double best = -1.0;
+    for (int j : rest) {
+      const double dx = x[j] - c[0], dy = y[j] - c[1], dz = z[j] - c[2];
+      const double e = dx * dx + dy * dy + dz * dz;
+      if (e > best) {
+        best = e;
+        far = j;
+      }
+    }
+    d.clear();
+    for (int j : rest) {
+      const double dx = x[j] - x[far], dy = y[j] - y[far], dz = z[j] - z[far];
+      d.emplace_back(dx * dx + dy * dy + dz * dz, j);
+    }
+    const size_t take = std::min<size_t>(32, d.size());
+    std::nth_element(d.begin(), d.begin() + (take - 1), d.end());
+    std::vector<int> grp;
+    for (size_t k = 0; k < take; ++k) grp.push_back(d[k].second);
+    std::sort(grp.begin(), grp.end());
+    order.insert(order.end(), grp.begin(), grp.end());
+    std::vector<char> used(n, 0);
+    for (int j : grp) used[j] = 1;
+    std::vector<int> keep;
+    keep.reserve(rest.size() - take);
+    for (int j : rest)
+      if (!used[j]) keep.push_back(j);
+    rest.swap(keep);
+  }
+  return order;
+}
+
 static void centroid(const double *x, const double *y, const double *z, int n, double *c) {
   double sx = -0.0, sy = -0.0, sz = -0.0;  // left folds, as Molecule::center_of_mass
   for (int i = 0; i < n; ++i) sx += x[i];
@@ -415,13 +471,24 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
     ext = std::max({ext, std::fabs(rec->x[i] - o[0]), std::fabs(rec->y[i] - o[1]), std::fabs(rec->z[i] - o[2])});
   }
   cx->rec_extent = ext;
-  std::vector<double> lx(lig->x, lig->x + lig->n), ly(lig->y, lig->y + lig->n), lz(lig->z, lig->z + lig->n);
-  std::vector<double> lq(lig->charge, lig->charge + lig->n);
-  std::vector<int> lser(lig->serial, lig->serial + lig->n);
+  // ligand on the device in slot order (sums are order-free; restraint and
+  // model indices go through the permutation)
+  const std::vector<int> perm = slot_order(lig->x, lig->y, lig->z, lig->n);
+  std::vector<int> inv(lig->n);
+  std::vector<double> lx(lig->n), ly(lig->n), lz(lig->n), lq(lig->n);
+  std::vector<int> lser(lig->n), ltp(lig->n);
   std::vector<double> ldes(static_cast<size_t>(std::max(lig->n, 1)) * 11, 0.0);
   double rad = 0.0;
-  for (int j = 0; j < lig->n; ++j) {
-    desolv_row(lig->element[j], lig->vdw_radius[j], &ldes[static_cast<size_t>(j) * 11]);
+  for (int k = 0; k < lig->n; ++k) {
+    const int j = perm[k];
+    inv[j] = k;
+    lx[k] = lig->x[j];
+    ly[k] = lig->y[j];
+    lz[k] = lig->z[j];
+    lq[k] = lig->charge[j];
+    lser[k] = lig->serial[j];
+    ltp[k] = ltype[j];
+    desolv_row(lig->element[j], lig->vdw_radius[j], &ldes[static_cast<size_t>(k) * 11]);
     const double dx = lig->x[j] - c[0], dy = lig->y[j] - c[1], dz = lig->z[j] - c[2];
     rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
   }
@@ -444,7 +511,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
     const int b = first_ca(lig, restraint_pairs[2 * k + 1]);
     if (a >= 0 && b >= 0) {
       rr.push_back(D4{rec->x[a], rec->y[a], rec->z[a], 0.0});
-      rl.push_back(b);
+      rl.push_back(inv[b]);
     }
   }
   cx->K = static_cast<int>(rl.size());
@@ -454,10 +521,10 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
       (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
       (s = upload(cx, lx, &cx->lig_x)) != GD_OK || (s = upload(cx, ly, &cx->lig_y)) != GD_OK ||
       (s = upload(cx, lz, &cx->lig_z)) != GD_OK || (s = upload(cx, lq, &cx->lig_q)) != GD_OK ||
-      (s = upload(cx, ltype, &cx->lig_type)) != GD_OK || (s = upload(cx, lser, &cx->lig_serial)) != GD_OK ||
+      (s = upload(cx, ltp, &cx->lig_type)) != GD_OK || (s = upload(cx, lser, &cx->lig_serial)) != GD_OK ||
       (s = upload(cx, ldes, &cx->lig_desolv)) != GD_OK || (s = upload(cx, tab32, &cx->tab32)) != GD_OK ||
       (s = upload(cx, tab64, &cx->tab64)) != GD_OK || (s = upload(cx, rr, &cx->restr_rec)) != GD_OK ||
-      (s = upload(cx, rl, &cx->restr_lig)) != GD_OK) {
+      (s = upload(cx, rl, &cx->restr_lig)) != GD_OK || (s = upload(cx, perm, &cx->lig_perm)) != GD_OK) {
     gd_complex_destroy(cx);
     return s;
   }
@@ -465,9 +532,9 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   cx->h_rx.assign(rec->x, rec->x + rec->n);
   cx->h_ry.assign(rec->y, rec->y + rec->n);
   cx->h_rz.assign(rec->z, rec->z + rec->n);
-  cx->h_lx = lx;
-  cx->h_ly = ly;
-  cx->h_lz = lz;
+  cx->h_lx.assign(lig->x, lig->x + lig->n);
+  cx->h_ly.assign(lig->y, lig->y + lig->n);
+  cx->h_lz.assign(lig->z, lig->z + lig->n);
   cx->h_rchain.assign(rec->chain, rec->chain + rec->n);
   cx->h_lchain.assign(lig->chain, lig->chain + lig->n);
   cx->h_relem.assign(rec->element, rec->element + rec->n);

@@ -88,7 +88,7 @@ static __device__ __forceinline__ void transform_atom(const gd_pose_frame &f, do
 static __device__ __forceinline__ void ligand_atom(const ScoreParams &p, const gd_pose_frame &f, int pose, int j,
                                             double &X, double &Y, double &Z) {
   if (p.models) {
-    const double *m = p.models + (static_cast<size_t>(pose) * p.nl + j) * 3;
+    const double *m = p.models + (static_cast<size_t>(pose) * p.nl + p.lig_perm[j]) * 3;  // models: original order
     X = m[0];
     Y = m[1];
     Z = m[2];

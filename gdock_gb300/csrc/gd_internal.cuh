@@ -63,7 +63,8 @@ struct ScoreParams {
   const int2 *rec_meta;     // (type, serial)
   const double *rec_desolv; // [nr * 11] energy contribution at burial count 0..10
   int nr, n_tiles;
-  // ligand, original order
+  // ligand in slot order (spatially compact runs of 32 atoms)
+  const int *lig_perm;      // slot position -> original atom index
   const double *lig_x, *lig_y, *lig_z;
   const double *lig_q;
   const int *lig_type, *lig_serial;
@@ -77,7 +78,7 @@ struct ScoreParams {
   int need_clamp;           // some |eps_ij| may exceed the [-50, 500] clamp
   // restraints: receptor CA coordinates and ligand CA atom index
   const D4 *restr_rec; // (x, y, z, -) of the receptor CA
-  const int *restr_lig;     // ligand CA index
+  const int *restr_lig;     // ligand CA index (slot order)
   int K;
   double wv, we, wd, wa;
   Thresholds thr;
@@ -136,6 +137,7 @@ struct gd_complex {
   gd::TypePair64 *tab64 = nullptr;
   D4 *restr_rec = nullptr;
   int *restr_lig = nullptr;
+  int *lig_perm = nullptr;  // slot position -> original ligand atom index
   std::vector<void *> allocs;
   uint64_t bytes = 0;
   // host copies used by clustering

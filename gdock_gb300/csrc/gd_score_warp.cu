@@ -40,7 +40,7 @@ constexpr int kSeg = 64;       // receptor atoms per ring stage
 constexpr int kWS = 4;         // ring stages per warp
 constexpr int kBlk = 8;        // receptor atoms per row-test round (lane = slot * 8 + atom)
 constexpr int kMaxS = 4;       // ligand slots per lane, at most (one row-test round covers 8 atoms x 4 slots)
-constexpr int kList = kSeg + 4;  // row-list entries per slot: a segment's atoms + padding for 4 rows per step
+constexpr int kList = kSeg + 8;  // row-list entries per slot: a segment's atoms + two paddings of 4 rows
 constexpr int kFar = kWS * kSeg; // shared-memory index of the far-away dummy receptor atom
 constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
 
@@ -59,7 +59,7 @@ struct BatchParams {
 };
 
 struct WarpSmem {
-  size_t pos, meta, list, bars, desc, frame, blob, rc, cnt, total;
+  size_t pos, meta, list, fixq, lfix, bars, desc, frame, blob, rc, cnt, total;
 };
 
 __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
@@ -74,6 +74,12 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   al(16);
   L.list = o;
   o += sizeof(uint16_t) * kMaxS * kList;
+  al(16);
+  L.fixq = o;
+  o += sizeof(uint16_t) * kMaxS * kList;  // at most one entry per step of a segment
+  al(16);
+  L.lfix = o;
+  o += sizeof(int) * kMaxS * 32;
   al(16);
   L.bars = o;
   o += 8 * kWS;
@@ -153,6 +159,17 @@ __device__ __forceinline__ void pair32(const float4 &r, int rtrow, int rser, con
         (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
 }
 
+// One pair of a far row (no pair within the vdW cutoff): Coulomb only, the
+// same FP32 expressions and decision as pair32().
+__device__ __forceinline__ void pair32_elec(const float4 &r, float lx, float ly, float lz, float ge, float &ae,
+                                            bool &amb) {
+  const float d2 = d2f(r, lx, ly, lz);
+  const float e = r.w * rcp_approx(d2);
+  const float te = __fsub_rn(d2, 113.0f);
+  add_if_abs_lt(ae, te, 112.0f, e);
+  amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge);
+}
+
 __device__ __forceinline__ bool near_band(float d2, float gv, float ge, float gdd) {
   const float tv = __fsub_rn(d2, 72.0f), te = __fsub_rn(d2, 113.0f);
   return (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < gv) |
@@ -165,13 +182,12 @@ struct FixOut {
   int dl;
 };
 
-// FP64 re-decision of one flagged pair: recomputes the FP32 d2 and decisions
-// bit-identically to pair32() and returns the corrections where the exact
-// decision differs.  Out of line: it runs for a handful of pairs per pose.
+// FP64 re-decision of one flagged pair (exact ligand coordinates X, Y, Z):
+// recomputes the FP32 d2 and decisions bit-identically to pair32() and
+// returns the corrections where the exact decision differs.
 template <bool SERIAL, bool CLAMP>
-__device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, const gd_pose_frame &f, int pose, int j, float4 r,
-                                        int ridx, int rtrow, int rser, float lx, float ly, float lz, float lq, int lt,
-                                        int lser) {
+__device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, double X, double Y, double Z, float4 r, int ridx,
+                                        int rtrow, int rser, float lx, float ly, float lz, float lq, int lt, int lser) {
   FixOut o{0.0f, 0.0f, 0};
   const float d2 = d2f(r, lx, ly, lz);
   const float tv = __fsub_rn(d2, 72.0f);
@@ -180,8 +196,6 @@ __device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, const gd_pose_f
   if (SERIAL) pv32 = pv32 && (rser != lser);
   const bool pe32 = fabsf(te) < 112.0f;
   const bool pd32 = d2 < 64.0f;
-  double X, Y, Z;
-  ligand_atom(p, f, pose, j, X, Y, Z);
   const D4 r64 = p.rec_pos64[ridx];
   const double d2x = exact_d2(r64.x, r64.y, r64.z, X, Y, Z);
   bool pv64 = d2x > 0.0 && d2x < p.thr.vdw_lt;
@@ -214,6 +228,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   float4 *s_pos = reinterpret_cast<float4 *>(base + L.pos);
   int2 *s_meta = reinterpret_cast<int2 *>(base + L.meta);
   uint16_t *s_list = reinterpret_cast<uint16_t *>(base + L.list);  // kept rows per slot, as stage indices
+  uint16_t *s_fixq = reinterpret_cast<uint16_t *>(base + L.fixq);  // flagged steps: list position | slot << 8
+  int *s_lfix = reinterpret_cast<int *>(base + L.lfix);            // ligand burial corrections per slot and lane
   uint64_t *s_bar = reinterpret_cast<uint64_t *>(base + L.bars);
   ScoreParams *s_desc = reinterpret_cast<ScoreParams *>(base + L.desc);
   gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(base + L.frame);
@@ -231,6 +247,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   }
   for (int i = lane; i < bp.max_nr; i += 32) cnt[i] = 0;
   for (int i = lane; i < kSeg; i += 32) s_rc[i] = 0;
+  for (int i = lane; i < kMaxS * 32; i += 32) s_lfix[i] = 0;
   __syncwarp();
 
   static_assert(S >= 1 && S <= kMaxS, "one row-test round covers at most four slots");
@@ -275,6 +292,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     // from the slot's bounding sphere has every FP32 d2 beyond the elec
     // cutoff and its guard band: all its terms, counts and guard tests are 0
     const float reach = sqrtf(225.01f + 2.0f * ge) + 0.01f;
+    // ... and one farther than this has every FP32 d2 beyond the vdW cutoff
+    // and its band (so beyond the desolvation one too): Coulomb terms only
+    const float reach_v = sqrtf(144.01f + 2.0f * gv) + 0.01f;
     const float2 *tab = reinterpret_cast<const float2 *>(p.tab32);
     double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
     bool failed = false;
@@ -327,7 +347,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       const float4 myb = my_s < S ? s_blob[my_s] : make_float4(0.0f, 0.0f, 0.0f, -1.0e30f);
       const float mlim = myb.w + reach;
       const float mlim2 = (myb.w >= 0.0f) ? mlim * mlim : -1.0f;  // empty slot: no row kept
+      const float mnear = myb.w + reach_v, mnear2 = mnear * mnear;
       float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
+      int nfix = 0;  // flagged steps of the current segment
       for (int g = 0; g < nseg; ++g, ++q) {
         const int st = static_cast<int>(q % kWS);
         const bool ok = __all_sync(kFull, mbar_wait(&s_bar[st], static_cast<uint32_t>((q / kWS) & 1)));
@@ -339,18 +361,28 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         const int na = min(kSeg, p.nr - gbase);
         const int sbase = st * kSeg;
 
-        // Phase 1: lane (slot, atom) tests one row against the slot's sphere;
-        // kept rows go to per-slot lists, padded with the far dummy atom.
-        int n_mine = 0;  // rows of this lane's slot
+        // Phase 1: lane (slot, atom) tests one row against the slot's sphere.
+        // Kept rows go to the slot's list: far rows (Coulomb only) from the
+        // front, near rows from the back; each run is padded with the far
+        // dummy atom to whole steps.
+        int nf_mine = 0, nn_mine = 0;  // far / near rows of this lane's slot
+        uint16_t *my_list = s_list + my_s * kList;
         for (int b0 = 0; b0 < na; b0 += kBlk) {
           const float4 ra = s_pos[sbase + b0 + my_a];  // atoms past nr are padding far away
           const float dx = ra.x - myb.x, dy = ra.y - myb.y, dz = ra.z - myb.z;
-          const bool keep = dx * dx + dy * dy + dz * dz < mlim2;
-          const unsigned M = __ballot_sync(kFull, keep);
-          if (keep) s_list[my_s * kList + n_mine + __popc(M & my_group & lt_mask)] = static_cast<uint16_t>(sbase + b0 + my_a);
-          n_mine += __popc(M & my_group);
+          const float dc2 = dx * dx + dy * dy + dz * dz;
+          const bool keep = dc2 < mlim2, nearr = dc2 < mnear2;
+          const unsigned Mf = __ballot_sync(kFull, keep && !nearr), Mn = __ballot_sync(kFull, keep && nearr);
+          const uint16_t idx = static_cast<uint16_t>(sbase + b0 + my_a);
+          if (keep && !nearr) my_list[nf_mine + __popc(Mf & my_group & lt_mask)] = idx;
+          if (keep && nearr) my_list[kList - 1 - nn_mine - __popc(Mn & my_group & lt_mask)] = idx;
+          nf_mine += __popc(Mf & my_group);
+          nn_mine += __popc(Mn & my_group);
         }
-        if (my_s < S && my_a < kAtoms) s_list[my_s * kList + n_mine + my_a] = static_cast<uint16_t>(kFar);
+        if (my_s < S && my_a < kAtoms) {
+          my_list[nf_mine + my_a] = static_cast<uint16_t>(kFar);
+          my_list[kList - 1 - nn_mine - my_a] = static_cast<uint16_t>(kFar);
+        }
         __syncwarp();
 
         // Phase 2: every term of the kept rows, kAtoms rows per step
@@ -358,11 +390,29 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 #pragma unroll
         for (int s = 0; s < S; ++s) {
           float aes = 0.0f;  // sum of q_r / d2 over this slot's kept pairs
-          const int n = __shfl_sync(kFull, n_mine, s * 8);
-          const int j = ch * kChunk + s * 32 + lane;
+          const int nf = __shfl_sync(kFull, nf_mine, s * 8), nn = __shfl_sync(kFull, nn_mine, s * 8);
           const uint16_t *lst = s_list + s * kList;
+          // far rows: Coulomb only
 #pragma unroll 1
-          for (int k0 = 0; k0 < n; k0 += kAtoms) {
+          for (int k0 = 0; k0 < nf; k0 += kAtoms) {
+            int ix[kAtoms];
+            float4 r[kAtoms];
+#pragma unroll
+            for (int i = 0; i < kAtoms; ++i) {
+              ix[i] = lst[k0 + i];
+              r[i] = s_pos[ix[i]];
+            }
+            bool amb = false;
+#pragma unroll
+            for (int i = 0; i < kAtoms; ++i) pair32_elec(r[i], lx[s], ly[s], lz[s], ge, aes, amb);
+            if (__any_sync(kFull, amb)) {
+              if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
+              ++nfix;
+            }
+          }
+          // near rows: every term; the first step may start in the padding
+#pragma unroll 1
+          for (int k0 = kList - (nn + kAtoms - 1) / kAtoms * kAtoms; k0 < kList; k0 += kAtoms) {
             int ix[kAtoms];
             float4 r[kAtoms];
             int rt[kAtoms], rs[kAtoms], rc[kAtoms];
@@ -381,17 +431,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
               pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lt[s], lser[s], gv, ge, gdd, av,
                                     aes, lcnt[s], rc[i], amb);
             if (__any_sync(kFull, amb)) {
-#pragma unroll
-              for (int i = 0; i < kAtoms; ++i) {
-                if (ix[i] == kFar || j >= p.nl) continue;
-                if (!near_band(d2f(r[i], lx[s], ly[s], lz[s]), gv, ge, gdd)) continue;
-                const FixOut fo = fix_pair<SERIAL, CLAMP>(p, f, pose, j, r[i], gbase + ix[i] - sbase, rt[i], rs[i],
-                                                          lx[s], ly[s], lz[s], lq[s], lt[s], lser[s]);
-                av += fo.dv;
-                ae += fo.de;
-                lcnt[s] += fo.dl;
-                rc[i] += fo.dl;
-              }
+              if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
+              ++nfix;
             }
             // receptor burial counts of the step's rows: lane i adds row i's
             // total (distinct atoms; the far atom never counts)
@@ -408,6 +449,38 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           }
           ae = __fmaf_rn(aes, lq[s], ae);
         }
+        __syncwarp();
+        // FP64 re-decisions of the flagged steps' pairs in the guard band
+#pragma unroll 1
+        for (int t = 0; t < nfix; ++t) {
+          const int e = s_fixq[t], k0 = e & 255, s = e >> 8;
+          const int j = ch * kChunk + s * 32 + lane;
+          if (j >= p.nl) continue;
+          double X, Y, Z;
+          ligand_atom(p, f, pose, j, X, Y, Z);
+          // the lane's FP32 coordinates, as in the chunk set-up
+          const float fx = static_cast<float>(X - p.ox), fy = static_cast<float>(Y - p.oy),
+                      fz = static_cast<float>(Z - p.oz);
+          const float fq = static_cast<float>(p.lig_q[j]);
+          const int ft = p.lig_type[j], fs = SERIAL ? p.lig_serial[j] : 0;
+#pragma unroll 1
+          for (int i = 0; i < kAtoms; ++i) {
+            const int ixi = s_list[s * kList + k0 + i];
+            if (ixi == kFar) continue;
+            const float4 ri = s_pos[ixi];
+            if (!near_band(d2f(ri, fx, fy, fz), gv, ge, gdd)) continue;
+            const int2 mt = s_meta[ixi];
+            const FixOut fo = fix_pair<SERIAL, CLAMP>(p, X, Y, Z, ri, gbase + ixi - sbase, mt.x, mt.y, fx, fy, fz, fq,
+                                                      ft, fs);
+            av += fo.dv;
+            ae += fo.de;
+            if (fo.dl) {
+              s_lfix[s * 32 + lane] += fo.dl;
+              atomicAdd(&s_rc[ixi - sbase], fo.dl);
+            }
+          }
+        }
+        nfix = 0;
         kahan_add(sv, cv, av);
         kahan_add(se, ce, ae);
         __syncwarp();
@@ -425,8 +498,11 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           issue_seg(q + kWS, static_cast<int>((k + kWS) % nseg), p, s_pos, s_meta, s_bar);
       }
       if (failed) break;
+      __syncwarp();
 #pragma unroll
       for (int s = 0; s < S; ++s) {
+        lcnt[s] += s_lfix[s * 32 + lane];  // burial corrections of FP64 re-decisions
+        s_lfix[s * 32 + lane] = 0;
         const int j = ch * kChunk + s * 32 + lane;
         if (j < p.nl) desolv_t += p.lig_desolv[static_cast<size_t>(j) * 11 + min(lcnt[s], 10)];
       }

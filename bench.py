@@ -271,7 +271,13 @@ def run_c4(args):
             srv.wait(jid, 600.0)
         t_all = time.perf_counter() - t0
         st = srv.stats()
-        gens = [srv.result(j)[0].generations for j in ids]
+        res = [srv.result(j)[0] for j in ids]
+        bad = [(j, r.status, r.error) for j, r in zip(ids, res) if r.status != _lib.GD_JOB_DONE]
+        if bad:
+            srv.stop()
+            raise SystemExit(f"served jobs did not finish: (job, status, error) {bad[:8]}; "
+                             f"last error: {ctx.lib.gd_last_error(ctx.h).decode()}")
+        gens = [r.generations for r in res]
         srv.stop()
         sweep.append({"rate_jobs_per_s": rate, "jobs": per_rate, "jobs_per_s": per_rate / t_all,
                       "latency_p50_s": st.latency_p50_s, "latency_p99_s": st.latency_p99_s,

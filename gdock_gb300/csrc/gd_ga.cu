@@ -581,6 +581,8 @@ struct gd_server {
   int64_t next_id = 1;
   std::thread worker;
   bool running = false;
+  gd_status failed = GD_OK;  // the worker stopped on this error: no job runs any more
+  std::string fail_msg;      // the context's error message at that moment
   // statistics
   int64_t completed = 0, poses_scored = 0, generations_run = 0;
   std::vector<double> latencies;
@@ -879,6 +881,10 @@ gd_status gd_server_submit(gd_server *S, const gd_atoms *rec, const gd_atoms *li
   job->seed = seed;
   job->t_submit = Clock::now();
   std::lock_guard<std::mutex> lock(S->mu);
+  if (S->failed != GD_OK) {
+    delete job;
+    return gd::fail(S->ctx, GD_ERR_STATE, "the server stopped on an error: " + S->fail_msg);
+  }
   job->id = S->next_id++;
   if (!S->started_clock) {
     S->t_first = job->t_submit;
@@ -918,13 +924,21 @@ gd_status gd_server_start(gd_server *S) {
         }
       }
       int active = 0;
-      if (gd::server_tick(S, &active) != GD_OK) {
+      const gd_status ts = gd::server_tick(S, &active);
+      if (ts != GD_OK) {
+        // every resident and queued job fails with the tick's status; later
+        // submissions are refused (see gd_server_submit)
         std::lock_guard<std::mutex> lock(S->mu);
+        S->failed = ts;
+        S->fail_msg = gd_last_error(S->ctx);
+        const auto now = gd::Clock::now();
         for (auto &kv : S->jobs)
           if (kv.second->status == GD_JOB_RUNNING || kv.second->status == GD_JOB_QUEUED) {
             kv.second->status = GD_JOB_FAILED;
-            kv.second->error = GD_ERR_CUDA;
+            kv.second->error = ts;
+            kv.second->t_done = now;
           }
+        S->queue.clear();
         S->cv.notify_all();
         break;
       }

@@ -374,6 +374,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           const bool keep = dc2 < mlim2, nearr = dc2 < mnear2;
           const unsigned Mf = __ballot_sync(kFull, keep && !nearr), Mn = __ballot_sync(kFull, keep && nearr);
           const uint16_t idx = static_cast<uint16_t>(sbase + b0 + my_a);
+          // at most na <= kSeg rows per slot: far rows fill [0, nf), near rows
+          // (kList - nn, kList - 1], with room for both paddings in between
           if (keep && !nearr) my_list[nf_mine + __popc(Mf & my_group & lt_mask)] = idx;
           if (keep && nearr) my_list[kList - 1 - nn_mine - __popc(Mn & my_group & lt_mask)] = idx;
           nf_mine += __popc(Mf & my_group);
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             bool amb = false;
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) pair32_elec(r[i], lx[s], ly[s], lz[s], ge, aes, amb);
-            if (__any_sync(kFull, amb)) {
+            if (__any_sync(kFull, amb)) {  // at most one entry per step: nfix <= 4 * 18 per segment
               if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
               ++nfix;
             }
@@ -430,7 +432,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             for (int i = 0; i < kAtoms; ++i)
               pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lt[s], lser[s], gv, ge, gdd, av,
                                     aes, lcnt[s], rc[i], amb);
-            if (__any_sync(kFull, amb)) {
+            if (__any_sync(kFull, amb)) {  // at most one entry per step: nfix <= 4 * 18 per segment
               if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
               ++nfix;
             }
@@ -445,7 +447,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
                 my_ix = ix[i];
               }
             }
-            if (my_t) s_rc[my_ix - sbase] += my_t;
+            if (my_t) s_rc[my_ix - sbase] += my_t;  // a counted row is a real atom of this stage
           }
           ae = __fmaf_rn(aes, lq[s], ae);
         }
@@ -589,8 +591,14 @@ cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
   }
 }
 
+// The dynamic shared memory of a CTA can exceed the 48 KB default (receptors
+// near kCntSmemMax keep their burial counters there): the kernel's limit is
+// raised before the occupancy query, which otherwise reports an invalid
+// configuration.
 cudaError_t occupancy_var(int tune, bool serial, bool clamp, size_t smem, int *per_sm) {
   return with_variant(tune, serial, clamp, [&](auto kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, kWarps * 32, smem);
   });
 }

@@ -158,6 +158,49 @@ def test_cutoff_boundaries_f32_matches_f64(oracle):
         assert abs(e32[name][0] - e64[name][0]) <= 1e-5 * max(1.0, abs(e64[name][0])), name
 
 
+def test_elec_cutoff_band_in_far_rows(oracle):
+    """A compact ligand slot about 15 A from a receptor atom (beyond the vdW
+    reach, so its row takes the Coulomb-only path) with atoms within a few
+    ulps of the 15 A elec cutoff: the FP32 form must match the FP64 one."""
+    rec = make_mol([tatom(0, 0, 0, "O", charge=0.8, serial=1)])
+    pts = []
+    rng = np.random.default_rng(7)
+    for k in range(32):
+        u = np.array([1.0, 2.0, 2.0]) / 3.0 + rng.normal(0.0, 0.01, 3)
+        u /= np.linalg.norm(u)
+        d = 15.0 * (1 + (k % 7 - 3) * 2.0 ** -52)
+        pts.append(tatom(*(d * u), "N", charge=-0.7, serial=100 + k))
+    lig = make_mol(pts)
+    cx = gd.Complex(rec, lig, [])
+    xyz = lig.xyz()[None]
+    e64 = cx.score_models(xyz, gd.GD_PREC_F64)
+    e32 = cx.score_models(xyz, gd.GD_PREC_F32)
+    ref = oracle.score_models(rec, lig, [], xyz)
+    check(e64, ref, F64_TOL)
+    assert abs(e32["elec"][0] - e64["elec"][0]) <= 1e-5 * max(1.0, abs(e64["elec"][0]))
+    assert e32["vdw"][0] == 0.0 and e64["vdw"][0] == 0.0
+
+
+def test_receptor_near_shared_counter_limit():
+    """A receptor just under the shared-memory burial-counter limit (4,096
+    atoms) needs more than 48 KB of dynamic shared memory per CTA: the FP32
+    kernel must launch on a fresh context and agree with the FP64 form."""
+    c = synth.make_complex(470, 40, 5, seed=3)
+    assert 3600 < len(c.receptor) <= 4096
+    ctx = gd.Context(0)
+    try:
+        lig = gd.position_ligand(c.receptor, c.ligand)
+        cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+        genes = synth.quaternion_genes(np.random.default_rng(5), 64, half_box=10.0)
+        e64 = cx.score_poses(genes, gd.GD_PREC_F64)
+        e32 = cx.score_poses(genes, gd.GD_PREC_F32)
+        for name in ("vdw", "elec", "desolv", "air"):
+            assert np.allclose(e32[name], e64[name], rtol=1e-5, atol=1e-5), name
+        cx.close()
+    finally:
+        ctx.close()
+
+
 def test_deterministic(c1):
     lig = positioned(c1)
     genes = synth.random_genes(np.random.default_rng(9), 20)

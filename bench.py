@@ -158,9 +158,9 @@ def within_cutoff_fraction(c, lig, genes, n_sample=16, cutoff=15.0):
 
 
 def variant_name(tune: int) -> str:
-    """GD_TUNE_F32_SLOTS value -> 'S<slots per lane>xA<receptor rows per step>'."""
+    """GD_TUNE_F32_SLOTS value -> 'S<slots per lane>xA<receptor rows per step>xB<min CTAs per SM>'."""
     a = 4 if tune & 64 else (2 if tune & 16 else 1)
-    return f"S{tune % 16}xA{a}"
+    return f"S{tune % 16}xA{a}xB{5 if tune & 256 else 4}"
 
 
 def replica_throughput(t_step: float, units: int, world: int, device: str = "cpu"):
@@ -399,7 +399,7 @@ def main():
 
     # --- slots-per-lane sweep (a small autotune on a pose sample) ---
     tune = {}
-    for slots in (4, 16 + 4, 64 + 2, 64 + 4):  # see GD_TUNE_F32_SLOTS
+    for slots in (16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4):  # see GD_TUNE_F32_SLOTS
         ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
         ns_t = min(NP, 16384)
         launch(gd.GD_PREC_F32, ns_t)

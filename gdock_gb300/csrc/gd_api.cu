@@ -370,13 +370,13 @@ const char *gd_last_error(const gd_context *ctx) { return ctx ? ctx->last_error.
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (knob == GD_TUNE_F32_SLOTS) {
-    static const int kValid[] = {0, 4, 16 + 4, 64 + 2, 64 + 4};
+    static const int kValid[] = {0, 4, 16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4};
     bool ok = false;
     for (int v : kValid) ok = ok || v == value;
     if (!ok)
       return fail(ctx, GD_ERR_INVALID_ARG,
-                  "F32 tuning: one of 4, 20, 66, 68 (ligand slots per lane + 16 or 64 for two or four "
-                  "receptor rows per step)");
+                  "F32 tuning: one of 4, 20, 66, 68, 322, 324 (ligand slots per lane + 16 or 64 for two or "
+                  "four receptor rows per step, + 256 for the five-CTA register cap)");
     ctx->tune_f32_slots = value;
     return GD_OK;
   }

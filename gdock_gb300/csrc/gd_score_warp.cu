@@ -37,7 +37,7 @@ namespace {
 
 constexpr int kWarps = 4;      // warps per CTA (independent)
 constexpr int kSeg = 64;       // receptor atoms per ring stage
-constexpr int kWS = 4;         // ring stages per warp
+constexpr int kWS = 2;         // ring stages per warp (a stage takes microseconds to process: two hide the copy)
 constexpr int kBlk = 8;        // receptor atoms per row-test round (lane = slot * 8 + atom)
 constexpr int kMaxS = 4;       // ligand slots per lane, at most (one row-test round covers 8 atoms x 4 slots)
 constexpr int kList = kSeg + 8;  // row-list entries per slot: a segment's atoms + two paddings of 4 rows
@@ -574,7 +574,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 // Kernel variants.  The common case (no equal receptor/ligand serials, no
 // clamp needed) has a tuning grid of slots per lane S, receptor atoms per
 // inner step A and minimum CTAs per SM (register cap); the rare cases run
-// one variant.  The tuning value encodes S + 16 (A = 2) or + 64 (A = 4).
+// one variant.  The tuning value encodes S + 16 (A = 2) or + 64 (A = 4),
+// + 256 for the register cap of five resident CTAs per SM.
 template <typename F>
 cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
   if (serial || clamp) {
@@ -586,6 +587,8 @@ cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
     case 4: return f(k_score_f32w<4, 1, 4, false, false>);
     case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false>);
     case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false>);
+    case 256 + 64 + 2: return f(k_score_f32w<2, 4, 5, false, false>);
+    case 256 + 64 + 4: return f(k_score_f32w<4, 4, 5, false, false>);
     case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false>);
     default: return f(k_score_f32w<4, 4, 4, false, false>);  // 64 + 4
   }

@@ -25,8 +25,8 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;
 // Distinct (epsilon, Rmin/2) atom types a complex may hold.
 constexpr int kMaxTypes = 64;
 // FP32 scoring variant when none is set: 4 ligand slots per lane, 4 receptor
-// rows per step (GD_TUNE_F32_SLOTS encoding)
-constexpr int kDefaultF32Tune = 64 + 4;
+// rows per step, five resident CTAs per SM (GD_TUNE_F32_SLOTS encoding)
+constexpr int kDefaultF32Tune = 256 + 64 + 4;
 
 // device error codes written to the context's error word
 enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };

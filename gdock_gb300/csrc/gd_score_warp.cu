@@ -588,9 +588,8 @@ cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
     case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false>);
     case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false>);
     case 256 + 64 + 2: return f(k_score_f32w<2, 4, 5, false, false>);
-    case 256 + 64 + 4: return f(k_score_f32w<4, 4, 5, false, false>);
     case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false>);
-    default: return f(k_score_f32w<4, 4, 4, false, false>);  // 64 + 4
+    default: return f(k_score_f32w<4, 4, 5, false, false>);  // 256 + 64 + 4 = kDefaultF32Tune
   }
 }
 

@@ -275,7 +275,7 @@ def run_c4(args):
     ctx = gd.Context(0)
     pool = _uneven_complexes(48, 44)
     ga = _lib.ga_default_cfg(pop_size=150, max_generations=200, early_stopping=1)
-    rates = [float(r) for r in os.environ.get("GD_C4_RATES", "2,8,32").split(",")]
+    rates = [float(r) for r in os.environ.get("GD_C4_RATES", "1,8,32,200").split(",")]
     per_rate = int(os.environ.get("GD_C4_JOBS", "32"))
     sweep = []
     for rate in rates:
@@ -310,7 +310,8 @@ def run_c4(args):
             "value": best["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "Poisson arrivals of synthetic complexes (C3 sizes), GA pop 150, early "
+            "config": {"workload": "Poisson arrivals of synthetic complexes (C3 sizes) swept over "
+                                   f"{rates} jobs/s, {per_rate} jobs per rate, GA pop 150, early "
                                    "stopping after 10 stagnant generations, cap 200", "slots": 64},
             "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64}
     print(json.dumps(line), flush=True)

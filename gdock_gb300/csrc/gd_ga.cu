@@ -587,6 +587,8 @@ struct gd_server {
   int64_t completed = 0, poses_scored = 0, generations_run = 0;
   std::vector<double> latencies;
   gd::Clock::time_point t_first;
+  // host time per tick phase (GD_TRACE prints the totals when the server is destroyed)
+  double t_admit = 0, t_load = 0, t_prepare = 0, t_gpu = 0, t_retire = 0;
   bool started_clock = false;
 };
 
@@ -698,8 +700,10 @@ gd_status server_tick(gd_server *S, int *active_out) {
     const gd_atoms ra = job->rec.view(), la = job->lig.view();
     gd_complex *cx = nullptr;
     const uint64_t before = ctx->in_use;
+    const auto ta = Clock::now();
     s = gd_complex_create(ctx, &ra, &la, job->pairs.empty() ? nullptr : job->pairs.data(),
                           static_cast<int32_t>(job->pairs.size() / 2), &job->w, &cx);
+    S->t_admit += std::chrono::duration<double>(Clock::now() - ta).count();
     if (s == GD_ERR_OOM) break;  // wait for a resident job to finish
     const uint64_t bytes = ctx->in_use - before;
     if (s == GD_OK && S->cfg.hbm_budget && S->job_bytes + bytes > S->cfg.hbm_budget && S->job_bytes > 0) {
@@ -724,7 +728,9 @@ gd_status server_tick(gd_server *S, int *active_out) {
     }
     S->job_bytes += bytes;
     S->dirty = true;
+    const auto tl = Clock::now();
     s = server_load_slot(S, free_slot, job);
+    S->t_load += std::chrono::duration<double>(Clock::now() - tl).count();
     if (s != GD_OK) return s;
   }
   int active = 0;
@@ -749,6 +755,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
   }
   cudaStream_t st = ctx->stream;
   const int total = J * n;
+  const auto tg = Clock::now();
   k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "frames kernel");
@@ -757,7 +764,9 @@ gd_status server_tick(gd_server *S, int *active_out) {
     if (S->dirty || !S->bl) {
       if (S->bl) batch_free(ctx, S->bl);
       S->bl = nullptr;
+      const auto tp = Clock::now();
       s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune, &S->bl);
+      S->t_prepare += std::chrono::duration<double>(Clock::now() - tp).count();
       S->dirty = false;
     }
     if (s == GD_OK) s = batch_launch(ctx, S->bl, st);
@@ -791,6 +800,8 @@ gd_status server_tick(gd_server *S, int *active_out) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "server tick");
   s = check_device_error(ctx);
   if (s != GD_OK) return s;
+  S->t_gpu += std::chrono::duration<double>(Clock::now() - tg).count();
+  const auto tr = Clock::now();
   S->generations_run += 1;
   S->poses_scored += static_cast<int64_t>(active) * n;
   // 3. retire finished jobs
@@ -828,6 +839,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
     S->latencies.push_back(std::chrono::duration<double>(job->t_done - job->t_submit).count());
     S->cv.notify_all();
   }
+  S->t_retire += std::chrono::duration<double>(Clock::now() - tr).count();
   return GD_OK;
 }
 
@@ -1038,6 +1050,11 @@ gd_status gd_server_get_stats(gd_server *S, gd_server_stats *out) {
 gd_status gd_server_destroy(gd_server *S) {
   if (!S) return GD_ERR_INVALID_ARG;
   gd_server_stop(S);
+  gd::trace("server: admit (complex create)", S->t_admit);
+  gd::trace("server: load (draws + uploads)", S->t_load);
+  gd::trace("server: batch prepare", S->t_prepare);
+  gd::trace("server: kernels + sync (incl. prepare)", S->t_gpu);
+  gd::trace("server: retire", S->t_retire);
   cudaSetDevice(S->ctx->device);
   cudaStreamSynchronize(S->ctx->stream);
   for (auto *j : S->slot_job)

@@ -59,7 +59,7 @@ struct BatchParams {
 };
 
 struct WarpSmem {
-  size_t pos, meta, list, fixq, lfix, bars, desc, frame, blob, rc, cnt, total;
+  size_t pos, meta, list, fixq, lfix, bars, desc, frame, blob, box, rc, cnt, total;
 };
 
 __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
@@ -91,6 +91,8 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   o += sizeof(gd_pose_frame);
   L.blob = o;
   o += sizeof(float4) * 8;
+  L.box = o;
+  o += sizeof(float4) * 2 * kMaxS;
   L.rc = o;
   o += sizeof(int) * kSeg;
   L.cnt = o;
@@ -234,6 +236,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   ScoreParams *s_desc = reinterpret_cast<ScoreParams *>(base + L.desc);
   gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(base + L.frame);
   float4 *s_blob = reinterpret_cast<float4 *>(base + L.blob);
+  float4 *s_box = reinterpret_cast<float4 *>(base + L.box);  // per slot: (centre, hx), (hy, hz, -, -)
   int *s_rc = reinterpret_cast<int *>(base + L.rc);  // receptor burial counts of the current segment
   const int gwarp = static_cast<int>(blockIdx.x) * kWarps + wib;
   uint8_t *cnt = bp.smem_cnt ? reinterpret_cast<uint8_t *>(base + L.cnt)
@@ -295,6 +298,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     // ... and one farther than this has every FP32 d2 beyond the vdW cutoff
     // and its band (so beyond the desolvation one too): Coulomb terms only
     const float reach_v = sqrtf(144.01f + 2.0f * gv) + 0.01f;
+    const float reach2 = reach * reach, reach_v2 = reach_v * reach_v;
     const float2 *tab = reinterpret_cast<const float2 *>(p.tab32);
     double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
     bool failed = false;
@@ -340,7 +344,31 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
                       : 0.0f;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) rr = fmaxf(rr, __shfl_xor_sync(kFull, rr, o));
-        if (lane == 0) s_blob[s] = make_float4(cx, cy, cz, on_mask ? rr * 1.0001f + 0.01f : -1.0e30f);
+        // axis-aligned bounding box of the same atoms (half-widths widened
+        // like the radius so that FP32 rounding never shrinks it)
+        float lo_x = on ? lx[s] : 3.0e38f, lo_y = on ? ly[s] : 3.0e38f, lo_z = on ? lz[s] : 3.0e38f;
+        float hi_x = on ? lx[s] : -3.0e38f, hi_y = on ? ly[s] : -3.0e38f, hi_z = on ? lz[s] : -3.0e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          lo_x = fminf(lo_x, __shfl_xor_sync(kFull, lo_x, o));
+          lo_y = fminf(lo_y, __shfl_xor_sync(kFull, lo_y, o));
+          lo_z = fminf(lo_z, __shfl_xor_sync(kFull, lo_z, o));
+          hi_x = fmaxf(hi_x, __shfl_xor_sync(kFull, hi_x, o));
+          hi_y = fmaxf(hi_y, __shfl_xor_sync(kFull, hi_y, o));
+          hi_z = fmaxf(hi_z, __shfl_xor_sync(kFull, hi_z, o));
+        }
+        if (lane == 0) {
+          s_blob[s] = make_float4(cx, cy, cz, on_mask ? rr * 1.0001f + 0.01f : -1.0e30f);
+          if (on_mask) {
+            s_box[2 * s] = make_float4(0.5f * (lo_x + hi_x), 0.5f * (lo_y + hi_y), 0.5f * (lo_z + hi_z),
+                                       0.5f * (hi_x - lo_x) * 1.0001f + 0.01f);
+            s_box[2 * s + 1] = make_float4(0.5f * (hi_y - lo_y) * 1.0001f + 0.01f,
+                                           0.5f * (hi_z - lo_z) * 1.0001f + 0.01f, 0.0f, 0.0f);
+          } else {
+            s_box[2 * s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            s_box[2 * s + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          }
+        }
       }
       __syncwarp();
       // phase-1 role of this lane: row (slot my_s, atom my_a of each 8-atom round)
@@ -371,7 +399,14 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           const float4 ra = s_pos[sbase + b0 + my_a];  // atoms past nr are padding far away
           const float dx = ra.x - myb.x, dy = ra.y - myb.y, dz = ra.z - myb.z;
           const float dc2 = dx * dx + dy * dy + dz * dz;
-          const bool keep = dc2 < mlim2, nearr = dc2 < mnear2;
+          // distance from the atom to the slot's box: a second lower bound on
+          // every pair distance of the row (either bound may drop the row or
+          // make it far)
+          const float4 bx0 = s_box[2 * (my_s & (kMaxS - 1))], bx1 = s_box[2 * (my_s & (kMaxS - 1)) + 1];
+          const float ex = fmaxf(fabsf(ra.x - bx0.x) - bx0.w, 0.0f), ey = fmaxf(fabsf(ra.y - bx0.y) - bx1.x, 0.0f),
+                      ez = fmaxf(fabsf(ra.z - bx0.z) - bx1.y, 0.0f);
+          const float db2 = ex * ex + ey * ey + ez * ez;
+          const bool keep = dc2 < mlim2 && db2 < reach2, nearr = dc2 < mnear2 && db2 < reach_v2;
           const unsigned Mf = __ballot_sync(kFull, keep && !nearr), Mn = __ballot_sync(kFull, keep && nearr);
           const uint16_t idx = static_cast<uint16_t>(sbase + b0 + my_a);
           // at most na <= kSeg rows per slot: far rows fill [0, nf), near rows

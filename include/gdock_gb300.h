@@ -256,14 +256,16 @@ typedef struct gd_server_stats {
 gd_status gd_server_default_cfg(gd_server_cfg *cfg);
 gd_status gd_server_create(gd_context *ctx, const gd_server_cfg *cfg, gd_server **out);
 gd_status gd_server_destroy(gd_server *s);
-/* Queue a job (inputs copied); thread-safe. */
+/* Queue a job (inputs copied); thread-safe.  Refused with GD_ERR_STATE once
+ * the server's own thread has stopped on an error (gd_last_error names it). */
 gd_status gd_server_submit(gd_server *s, const gd_atoms *receptor, const gd_atoms *ligand,
                            const int32_t *restraint_pairs, int32_t n_pairs, const gd_weights *w, uint64_t seed,
                            int64_t *job_id);
 /* One tick on the caller's thread (admit, one generation, retire). */
 gd_status gd_server_step(gd_server *s, int32_t *resident_jobs);
 /* Run ticks on the server's own thread until gd_server_stop (which drains
- * queued and resident jobs first). */
+ * queued and resident jobs first).  A tick that fails stops the thread: every
+ * resident and queued job ends GD_JOB_FAILED with the tick's status. */
 gd_status gd_server_start(gd_server *s);
 gd_status gd_server_stop(gd_server *s);
 gd_status gd_server_wait(gd_server *s, int64_t job_id, double timeout_s, int32_t *status);

@@ -183,10 +183,14 @@ struct FccParams {
 constexpr int kFT = 64;   // pose tile
 constexpr int kFW = 16;   // words per staged chunk
 
+// The common count of a pose pair is symmetric: only tiles on or above the
+// diagonal run, and an off-diagonal tile decides both directions of each pair.
 __global__ void __launch_bounds__(256) k_fcc(const FccParams p) {
+  if (blockIdx.y > blockIdx.x) return;
   __shared__ unsigned long long sa[kFT][kFW + 1];
   __shared__ unsigned long long sb[kFT][kFW + 1];
   const int i0 = blockIdx.y * kFT, j0 = blockIdx.x * kFT;
+  const bool diag = blockIdx.y == blockIdx.x;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 pairs each
   int cnt[4][4];
 #pragma unroll
@@ -227,14 +231,16 @@ __global__ void __launch_bounds__(256) k_fcc(const FccParams p) {
       // calculate_fcc (src/clustering.rs:122-132) and the first test of
       // create_elements (src/clustering.rs:171); the second test for the
       // pair (j, i) is the same condition, evaluated in that pair's thread.
-      bool edge = false;
+      bool edge = false, back = false;
       if (si > 0 && sj > 0) {
         const double common = static_cast<double>(cnt[a][b]);
         const double fcc = common / static_cast<double>(si);
         const double fcc_v = common / static_cast<double>(sj);
-        edge = fcc >= p.c && fcc_v >= p.cs;
+        edge = fcc >= p.c && fcc_v >= p.cs;  // i -> j
+        back = fcc_v >= p.c && fcc >= p.cs;  // j -> i: the same ratios, roles swapped
       }
       if (edge) atomicOr(&p.adj[static_cast<size_t>(i) * p.adj_words + (j >> 5)], 1u << (j & 31));
+      if (back && !diag) atomicOr(&p.adj[static_cast<size_t>(j) * p.adj_words + (i >> 5)], 1u << (i & 31));
     }
   }
 }
@@ -556,29 +562,28 @@ gd_status get_topo(gd_complex *cx, ClusterTopo **t) {
 }
 
 // Greedy clustering of cluster_elements (src/clustering.rs:183-254) over an
-// adjacency bit matrix, then the size filter (src/clustering.rs:289-292).
+// adjacency bit matrix (row e, bit m: edge e -> m), then the size filter
+// (src/clustering.rs:289-292).
+//  - count[e] = unused neighbours of e (its self-edge included, as in the
+//    reference); the centre is the unused element with the largest count,
+//    lower index on ties.
+//  - A cluster holds the centre and its unused neighbours, so its size is at
+//    most count + 1 (+1 only without a self-edge, i.e. an empty contact set).
+//    Counts never grow, so once the best count + 1 is below min_size every
+//    later cluster would be dropped by the size filter: the loop stops there
+//    without changing the kept clusters or their order.
+//  - After a cluster M is formed, every unused e loses |N(e) & M|, taken
+//    from the bit rows (per member bit for small M, popcounts for large M).
 int greedy_clusters(const std::vector<uint32_t> &adj, int n, int words, int min_size, int32_t *centers, int32_t *sizes,
                     int32_t *members) {
   std::vector<int> count(n, 0);
-  std::vector<std::vector<int>> in_edges(n);  // e with edge e -> m
   for (int e = 0; e < n; ++e)
-    for (int w = 0; w < words; ++w) {
-      uint32_t v = adj[static_cast<size_t>(e) * words + w];
-      count[e] += __builtin_popcount(v);
-      while (v) {
-        const int b = __builtin_ctz(v);
-        v &= v - 1;
-        in_edges[w * 32 + b].push_back(e);
-      }
-    }
+    for (int w = 0; w < words; ++w) count[e] += __builtin_popcount(adj[static_cast<size_t>(e) * words + w]);
   std::vector<char> used(n, 0);
+  std::vector<uint32_t> mbits(words, 0);
   struct Cl { int center, first, size; };
   std::vector<Cl> cls;
   std::vector<int> mem;
-  auto mark = [&](int m) {
-    used[m] = 1;
-    for (int e : in_edges[m]) --count[e];
-  };
   for (;;) {
     int center = -1, best = -1;
     for (int e = 0; e < n; ++e)
@@ -586,26 +591,42 @@ int greedy_clusters(const std::vector<uint32_t> &adj, int n, int words, int min_
         best = count[e];
         center = e;
       }
-    if (center < 0) break;
+    if (center < 0 || best + 1 < min_size) break;
     const int first = static_cast<int>(mem.size());
     mem.push_back(center);
-    std::vector<int> nb;
+    const uint32_t *row = &adj[static_cast<size_t>(center) * words];
     for (int w = 0; w < words; ++w) {
-      uint32_t v = adj[static_cast<size_t>(center) * words + w];
+      uint32_t v = row[w];
       while (v) {
         const int b = __builtin_ctz(v);
         v &= v - 1;
         const int m = w * 32 + b;
-        if (m != center && !used[m]) nb.push_back(m);
+        if (m != center && !used[m]) mem.push_back(m);
       }
     }
-    for (int m : nb) {
-      mem.push_back(m);
-      mark(m);
+    const int size = static_cast<int>(mem.size()) - first;
+    for (int k = first; k < first + size; ++k) used[mem[k]] = 1;
+    // counts of the remaining elements lose their edges into the cluster
+    if (size < words) {
+      for (int k = first; k < first + size; ++k) {
+        const int m = mem[k], mw = m >> 5;
+        const uint32_t mb = 1u << (m & 31);
+        for (int e = 0; e < n; ++e)
+          if (!used[e] && (adj[static_cast<size_t>(e) * words + mw] & mb)) --count[e];
+      }
+    } else {
+      std::fill(mbits.begin(), mbits.end(), 0u);
+      for (int k = first; k < first + size; ++k) mbits[mem[k] >> 5] |= 1u << (mem[k] & 31);
+      for (int e = 0; e < n; ++e) {
+        if (used[e]) continue;
+        const uint32_t *re = &adj[static_cast<size_t>(e) * words];
+        int c = 0;
+        for (int w = 0; w < words; ++w) c += __builtin_popcount(re[w] & mbits[w]);
+        count[e] -= c;
+      }
     }
-    mark(center);
     std::sort(mem.begin() + first, mem.end());
-    cls.push_back(Cl{center, first, static_cast<int>(mem.size()) - first});
+    cls.push_back(Cl{center, first, size});
   }
   std::stable_sort(cls.begin(), cls.end(), [](const Cl &a, const Cl &b) { return a.size > b.size; });
   int k = 0, mo = 0;
@@ -903,7 +924,8 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   if (e == cudaSuccess) e = cudaMemcpyAsync(&U, d_total, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps");
-  trace("cluster (device): contacts + union", std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+  const auto t_union = std::chrono::steady_clock::now();
+  trace("cluster (device): contacts + union", std::chrono::duration<double>(t_union - pt_all.t0).count());
   const int W = std::max(1, (U + 63) / 64);
   const int aw = (n + 31) / 32;
   const size_t compact_b = sizeof(unsigned long long) * static_cast<size_t>(W) * n, sz_b = sizeof(int) * n,
@@ -937,8 +959,10 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   dev_free(ctx, extra, al(compact_b) + al(sz_b) + al(adj_b));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC on the device");
-  trace("cluster (device): compact + fcc", std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+  const auto t_fcc = std::chrono::steady_clock::now();
+  trace("cluster (device): compact + fcc", std::chrono::duration<double>(t_fcc - t_union).count());
   *n_clusters = greedy_clusters(adj, n, aw, cfg.min_cluster_size, centers, sizes, members);
+  trace("cluster (device): greedy (host)", std::chrono::duration<double>(std::chrono::steady_clock::now() - t_fcc).count());
   return GD_OK;
 }
 

@@ -70,6 +70,24 @@ def test_cluster_edge_cases(oracle):
             assert got == oracle.cluster(sets, min_size=ms), trial
 
 
+def test_cluster_large_dense_groups(oracle):
+    """Groups of near-identical contact sets give clusters larger than a row
+    of the adjacency bit matrix (the popcount update) next to small ones."""
+    rng = np.random.default_rng(11)
+    protos = [np.unique(rng.integers(0, 400, 60)) for _ in range(3)]
+    sets = []
+    for k in range(330):
+        base = protos[k % 3] if k < 300 else np.unique(rng.integers(0, 400, int(rng.integers(0, 40))))
+        keep = base[rng.random(base.size) > 0.1]
+        extra = rng.integers(0, 400, 3)
+        sets.append(np.unique(np.concatenate([keep, extra])).astype(np.int64))
+    for ms in (1, 4, 50):
+        cfg = gd.ClusteringConfig(min_cluster_size=ms)
+        got = [(r.center_idx, r.members) for r in gd.cluster_sets(sets, cfg)]
+        assert got == oracle.cluster(sets, min_size=ms), ms
+    assert max(len(m) for _, m in got) > 330 // 32
+
+
 def test_multichain_receptor_contacts(oracle):
     """A receptor of two chains: receptor-only inter-chain contacts count in
     every pose's set (src/clustering.rs:82-91)."""

@@ -380,12 +380,18 @@ gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
     ctx->tune_f32_slots = value;
     return GD_OK;
   }
+  if (knob == GD_TUNE_SPLIT) {
+    if (value < 0 || value > 2) return fail(ctx, GD_ERR_INVALID_ARG, "split tuning: 0 (automatic), 1 (never), 2 (always)");
+    ctx->tune_split = value;
+    return GD_OK;
+  }
   return fail(ctx, GD_ERR_INVALID_ARG, "unknown tuning knob");
 }
 
 int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob) {
   if (!ctx) return -1;
   if (knob == GD_TUNE_F32_SLOTS) return ctx->tune_f32_slots;
+  if (knob == GD_TUNE_SPLIT) return ctx->tune_split;
   return -1;
 }
 

@@ -114,6 +114,7 @@ struct gd_context {
   size_t d_batch_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int tune_f32_slots = 0;  // 0: automatic (kDefaultF32Tune)
+  int tune_split = 0;      // GD_TUNE_SPLIT: 0 automatic, 1 whole poses, 2 always split
 };
 
 struct gd_complex {

@@ -56,6 +56,14 @@ struct BatchParams {
   int max_nr;                     // largest receptor of the batch
   int warp_smem;                  // bytes of shared memory per warp
   int *err;
+  // split mode: a work item is one ligand chunk of a pose; the chunk that
+  // finishes a pose last reduces its per-chunk partials
+  int split;
+  const long long *pose_start;    // first batch-wide pose index of each complex
+  int max_chunks;
+  double *part;                   // [pose][chunk][vdw, elec, ligand desolvation][32 lanes]
+  unsigned *pcount;               // [pose][max_nr] receptor burial counts
+  int *pdone;                     // [pose] chunks finished
 };
 
 struct WarpSmem {
@@ -221,7 +229,7 @@ __device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
   cnt[i] = static_cast<uint8_t>(c > 255 ? 255 : (c < 0 ? 0 : c));
 }
 
-template <int S, int kAtoms, int MINB, bool SERIAL, bool CLAMP>
+template <int S, int kAtoms, int MINB, bool SERIAL, bool CLAMP, bool SPLIT>
 __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchParams bp) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -248,7 +256,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     s_pos[kFar] = make_float4(1.0e9f, 1.0e9f, 1.0e9f, 0.0f);  // far from real and idle ligand lanes
     s_meta[kFar] = make_int2(0, 0);
   }
-  for (int i = lane; i < bp.max_nr; i += 32) cnt[i] = 0;
+  if (!SPLIT)
+    for (int i = lane; i < bp.max_nr; i += 32) cnt[i] = 0;
   for (int i = lane; i < kSeg; i += 32) s_rc[i] = 0;
   for (int i = lane; i < kMaxS * 32; i += 32) s_lfix[i] = 0;
   __syncwarp();
@@ -270,7 +279,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       if (bp.item_start[mid] <= static_cast<long long>(item)) lo = mid;
       else hi = mid - 1;
     }
-    const int pose = static_cast<int>(static_cast<long long>(item) - bp.item_start[lo]);
+    const long long kk = static_cast<long long>(item) - bp.item_start[lo];
     __syncwarp();
     {
       const uint64_t *src = reinterpret_cast<const uint64_t *>(bp.descs + lo);
@@ -280,13 +289,18 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     __syncwarp();
     const ScoreParams &p = *s_desc;
     if (p.skip && *p.skip) continue;  // this complex is finished (e.g. a converged GA job)
+    const int nchunks = (p.nl + kChunk - 1) / kChunk;
+    // split mode: item = (pose, chunk); otherwise item = pose, all chunks
+    const int pose = static_cast<int>(SPLIT ? kk / nchunks : kk);
+    const int ch0 = SPLIT ? static_cast<int>(kk % nchunks) : 0;
+    const int ch1 = SPLIT ? ch0 + 1 : nchunks;
+    const long long gp = SPLIT ? bp.pose_start[lo] + pose : 0;
     if (!p.models && lane < 16)
       reinterpret_cast<double *>(s_frame)[lane] = reinterpret_cast<const double *>(p.frames + pose)[lane];
     __syncwarp();
     const gd_pose_frame &f = *s_frame;
     const int nseg = (p.nr + kSeg - 1) / kSeg;
-    const int nchunks = (p.nl + kChunk - 1) / kChunk;
-    const long long Qi = static_cast<long long>(nchunks) * nseg;
+    const long long Qi = static_cast<long long>(ch1 - ch0) * nseg;
     const long long q0 = q;
     if (lane == 0)
       for (long long k = 0; k < Qi && k < kWS; ++k) issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_bar);
@@ -303,7 +317,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
     bool failed = false;
 
-    for (int ch = 0; ch < nchunks && !failed; ++ch) {
+    for (int ch = ch0; ch < ch1 && !failed; ++ch) {
       float lx[S], ly[S], lz[S], lq[S];
       int lt[S], lser[S], lcnt[S];
 #pragma unroll
@@ -525,7 +539,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         for (int i = lane; i < na; i += 32) {
           const int c = s_rc[i];
           if (c) {
-            bump_count(cnt, gbase + i, c);
+            if (SPLIT) atomicAdd(&bp.pcount[gp * bp.max_nr + gbase + i], static_cast<unsigned>(c));
+            else bump_count(cnt, gbase + i, c);
             s_rc[i] = 0;
           }
         }
@@ -536,15 +551,28 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       }
       if (failed) break;
       __syncwarp();
+      // the chunk's per-lane partials; both modes add them in chunk order,
+      // so split and whole-pose items give bit-identical energies
+      double dch = 0.0;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         lcnt[s] += s_lfix[s * 32 + lane];  // burial corrections of FP64 re-decisions
         s_lfix[s * 32 + lane] = 0;
         const int j = ch * kChunk + s * 32 + lane;
-        if (j < p.nl) desolv_t += p.lig_desolv[static_cast<size_t>(j) * 11 + min(lcnt[s], 10)];
+        if (j < p.nl) dch += p.lig_desolv[static_cast<size_t>(j) * 11 + min(lcnt[s], 10)];
       }
-      vdw_t += static_cast<double>(sv) - static_cast<double>(cv);
-      elec_t += static_cast<double>(se) - static_cast<double>(ce);
+      const double vch = static_cast<double>(sv) - static_cast<double>(cv);
+      const double ech = static_cast<double>(se) - static_cast<double>(ce);
+      if (SPLIT) {
+        double *pt = bp.part + (static_cast<size_t>(gp) * bp.max_chunks + ch) * 96;
+        pt[lane] = vch;
+        pt[32 + lane] = ech;
+        pt[64 + lane] = dch;
+      } else {
+        vdw_t += vch;
+        elec_t += ech;
+        desolv_t += dch;
+      }
     }
     if (failed) {
       // a bulk copy did not land in time: record it, wait (bounded) for the
@@ -557,11 +585,32 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       __syncwarp();
       return;
     }
-    // receptor burial -> desolvation; reset the counters for the next item
-    for (int i = lane; i < p.nr; i += 32) {
-      const int c = cnt[i];
-      desolv_t += p.rec_desolv[static_cast<size_t>(i) * 11 + (c < 10 ? c : 10)];
-      cnt[i] = 0;
+    if (SPLIT) {
+      // publish this chunk; the warp that completes the pose reduces it
+      __threadfence();
+      __syncwarp();
+      int done = 0;
+      if (lane == 0) done = atomicAdd(&bp.pdone[gp], 1);
+      done = __shfl_sync(kFull, done, 0);
+      if (done != nchunks - 1) continue;
+      __threadfence();
+      for (int c = 0; c < nchunks; ++c) {
+        const double *pt = bp.part + (static_cast<size_t>(gp) * bp.max_chunks + c) * 96;
+        vdw_t += __ldcg(pt + lane);
+        elec_t += __ldcg(pt + 32 + lane);
+        desolv_t += __ldcg(pt + 64 + lane);
+      }
+      for (int i = lane; i < p.nr; i += 32) {
+        const unsigned c = __ldcg(&bp.pcount[gp * bp.max_nr + i]);
+        desolv_t += p.rec_desolv[static_cast<size_t>(i) * 11 + (c < 10u ? c : 10u)];
+      }
+    } else {
+      // receptor burial -> desolvation; reset the counters for the next item
+      for (int i = lane; i < p.nr; i += 32) {
+        const int c = cnt[i];
+        desolv_t += p.rec_desolv[static_cast<size_t>(i) * 11 + (c < 10 ? c : 10)];
+        cnt[i] = 0;
+      }
     }
     vdw_t = warp_sum(vdw_t);
     elec_t = warp_sum(elec_t);
@@ -606,6 +655,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   }
 }
 
+// Split-mode kernel (a work item is one ligand chunk of a pose): one variant,
+// 4 slots and 4 rows per step, used for launches with fewer poses than warps.
+constexpr int kSplitTune = -1;
+
 // Kernel variants.  The common case (no equal receptor/ligand serials, no
 // clamp needed) has a tuning grid of slots per lane S, receptor atoms per
 // inner step A and minimum CTAs per SM (register cap); the rare cases run
@@ -613,18 +666,19 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 // + 256 for the register cap of five resident CTAs per SM.
 template <typename F>
 cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
+  if (tune == kSplitTune) return f(k_score_f32w<4, 4, 4, false, false, true>);
   if (serial || clamp) {
-    if (serial && clamp) return f(k_score_f32w<4, 1, 4, true, true>);
-    if (serial) return f(k_score_f32w<4, 1, 4, true, false>);
-    return f(k_score_f32w<4, 1, 4, false, true>);
+    if (serial && clamp) return f(k_score_f32w<4, 1, 4, true, true, false>);
+    if (serial) return f(k_score_f32w<4, 1, 4, true, false, false>);
+    return f(k_score_f32w<4, 1, 4, false, true, false>);
   }
   switch (tune) {
-    case 4: return f(k_score_f32w<4, 1, 4, false, false>);
-    case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false>);
-    case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false>);
-    case 256 + 64 + 2: return f(k_score_f32w<2, 4, 5, false, false>);
-    case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false>);
-    default: return f(k_score_f32w<4, 4, 5, false, false>);  // 256 + 64 + 4 = kDefaultF32Tune
+    case 4: return f(k_score_f32w<4, 1, 4, false, false, false>);
+    case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false, false>);
+    case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false, false>);
+    case 256 + 64 + 2: return f(k_score_f32w<2, 4, 5, false, false, false>);
+    case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false, false>);
+    default: return f(k_score_f32w<4, 4, 5, false, false, false>);  // 256 + 64 + 4 = kDefaultF32Tune
   }
 }
 
@@ -667,69 +721,149 @@ static std::vector<ScoreParams> lpt_order(const std::vector<ScoreParams> &descs)
 struct BatchPlan {
   int tune, smem_cnt, max_nr, grid;
   size_t smem;
-  std::vector<long long> start;
+  std::vector<long long> start;       // work-item prefix per complex
+  std::vector<long long> pose_start;  // pose prefix per complex
+  int split = 0, max_chunks = 1;
+  size_t part_b = 0, cnt_b = 0, done_b = 0;  // split-mode scratch
 };
 
+constexpr size_t kSplitScratchMax = size_t(512) << 20;
+
+static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+// Whole poses per work item fill the GPU when there are at least as many
+// poses as resident warps.  With fewer (one GA generation of a few jobs, one
+// docking run's population) each pose is split into its ligand chunks so that
+// every warp has work; the energies are bit-identical either way.
 static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
-                            int slots, BatchPlan *pl) {
+                            int slots, bool allow_split, BatchPlan *pl) {
   const int ncx = static_cast<int>(descs.size());
+  const int chunk_split = 32 * 4;  // the split kernel's chunk of ligand atoms
   pl->start.assign(ncx + 1, 0);
+  pl->pose_start.assign(ncx + 1, 0);
   pl->max_nr = 0;
+  pl->max_chunks = 1;
   for (int c = 0; c < ncx; ++c) {
-    pl->start[c + 1] = pl->start[c] + descs[c].n_poses;
+    pl->pose_start[c + 1] = pl->pose_start[c] + descs[c].n_poses;
     pl->max_nr = std::max(pl->max_nr, descs[c].nr);
+    pl->max_chunks = std::max(pl->max_chunks, (descs[c].nl + chunk_split - 1) / chunk_split);
   }
-  pl->smem_cnt = pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0;
-  pl->smem = warp_layout(pl->smem_cnt).total * kWarps;
+  const long long poses = pl->pose_start[ncx];
   pl->tune = slots;
+  auto fit = [&](int smem_cnt, int *per_sm) -> cudaError_t {
+    pl->smem_cnt = smem_cnt;
+    pl->smem = warp_layout(smem_cnt).total * kWarps;
+    cudaError_t e = occupancy_var(pl->tune, serial, clamp, pl->smem, per_sm);
+    if (e == cudaSuccess && *per_sm < 1) e = cudaErrorInvalidConfiguration;
+    return e;
+  };
   int per_sm = 0;
-  cudaError_t e = occupancy_var(pl->tune, serial, clamp, pl->smem, &per_sm);
-  if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
+  cudaError_t e = fit(pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0, &per_sm);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
+  const long long warps = static_cast<long long>(per_sm) * ctx->sm_count * kWarps;
+  const size_t part_b = static_cast<size_t>(poses) * pl->max_chunks * 96 * sizeof(double);
+  const size_t cnt_b = static_cast<size_t>(poses) * pl->max_nr * sizeof(unsigned);
+  const bool fits = al256(part_b) + al256(cnt_b) <= kSplitScratchMax;
+  pl->split = 0;
+  if (allow_split && fits && poses > 0 && pl->max_chunks > 1 && !serial && !clamp)
+    pl->split = ctx->tune_split == 2 || (ctx->tune_split == 0 && poses < warps);
+  if (pl->split) {
+    pl->part_b = part_b;
+    pl->cnt_b = cnt_b;
+    pl->done_b = static_cast<size_t>(poses) * sizeof(int);
+    pl->tune = kSplitTune;
+    e = fit(0, &per_sm);  // burial counters live in the split scratch
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
+  } else {
+    pl->part_b = pl->cnt_b = pl->done_b = 0;
+  }
+  for (int c = 0; c < ncx; ++c) {
+    const long long per_pose = pl->split ? (descs[c].nl + chunk_split - 1) / chunk_split : 1;
+    pl->start[c + 1] = pl->start[c] + static_cast<long long>(descs[c].n_poses) * per_pose;
+  }
   const long long items = pl->start[ncx];
   pl->grid = static_cast<int>(std::max<long long>(
       1, std::min<long long>((items + kWarps - 1) / kWarps, static_cast<long long>(per_sm) * ctx->sm_count)));
   return GD_OK;
 }
 
-// Upload descriptors and prefix sums to `arg` (device), clear the work
-// counter, and launch.
-static gd_status run_batch(gd_context *ctx, const std::vector<ScoreParams> &descs, const BatchPlan &pl, bool serial,
-                           bool clamp, char *arg, uint8_t *gcounts, size_t gstride, cudaStream_t stream) {
+// Layout of the argument block: descriptors, item prefix, work counter, pose
+// prefix, per-warp global burial counters (large receptors, whole-pose
+// items), split-mode partials, burial counts and chunk counters.
+struct ArgLayout {
+  size_t desc, start, queue, pstart, gcounts, part, pcount, pdone, total;
+};
+
+static ArgLayout arg_layout(int ncx, const BatchPlan &pl, size_t gcount_bytes) {
+  ArgLayout L{};
+  size_t o = 0;
+  L.desc = o;
+  o += al256(sizeof(ScoreParams) * ncx);
+  L.start = o;
+  o += al256(sizeof(long long) * (ncx + 1));
+  L.queue = o;
+  o += al256(sizeof(unsigned long long));
+  L.pstart = o;
+  o += al256(sizeof(long long) * (ncx + 1));
+  L.gcounts = o;
+  o += al256(gcount_bytes);
+  L.part = o;
+  o += al256(pl.part_b);
+  L.pcount = o;
+  o += al256(pl.cnt_b);
+  L.pdone = o;
+  o += al256(pl.done_b);
+  L.total = o;
+  return L;
+}
+
+static size_t gcount_stride(const BatchPlan &pl) {
+  return (pl.smem_cnt || pl.split) ? 0 : ((pl.max_nr + 127) / 128) * 128;
+}
+
+static gd_status upload_args(gd_context *ctx, const std::vector<ScoreParams> &descs, const BatchPlan &pl,
+                             const ArgLayout &L, char *arg, cudaStream_t stream, bool sync) {
   const int ncx = static_cast<int>(descs.size());
-  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-  const size_t db = sizeof(ScoreParams) * ncx, sb = sizeof(long long) * (ncx + 1);
-  ScoreParams *d_desc = reinterpret_cast<ScoreParams *>(arg);
-  long long *d_start = reinterpret_cast<long long *>(arg + al(db));
-  unsigned long long *d_queue = reinterpret_cast<unsigned long long *>(arg + al(db) + al(sb));
   // staged from pageable memory: the copy has left the host buffer when the
   // call returns, so back-to-back launches cannot race on it
-  std::vector<char> h(al(db) + sb);
-  std::memcpy(h.data(), descs.data(), db);
-  std::memcpy(h.data() + al(db), pl.start.data(), sb);
-  cudaError_t e = cudaMemcpyAsync(arg, h.data(), h.size(), cudaMemcpyHostToDevice, stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned long long), stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring setup");
+  std::vector<char> h(L.gcounts);
+  std::memcpy(h.data() + L.desc, descs.data(), sizeof(ScoreParams) * ncx);
+  std::memcpy(h.data() + L.start, pl.start.data(), sizeof(long long) * (ncx + 1));
+  std::memcpy(h.data() + L.pstart, pl.pose_start.data(), sizeof(long long) * (ncx + 1));
+  const cudaError_t e = sync ? cudaMemcpy(arg, h.data(), h.size(), cudaMemcpyHostToDevice)
+                             : cudaMemcpyAsync(arg, h.data(), h.size(), cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring arguments");
+  return GD_OK;
+}
+
+// Reset the work counter (and the split-mode counters) and launch.
+static gd_status launch_args(gd_context *ctx, int ncx, const BatchPlan &pl, const ArgLayout &L, char *arg,
+                             bool serial, bool clamp, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(arg + L.queue, 0, sizeof(unsigned long long), stream);
+  if (e == cudaSuccess && pl.split) e = cudaMemsetAsync(arg + L.pcount, 0, L.total - L.pcount, stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring reset");
   BatchParams bp{};
-  bp.descs = d_desc;
-  bp.item_start = d_start;
+  bp.descs = reinterpret_cast<const ScoreParams *>(arg + L.desc);
+  bp.item_start = reinterpret_cast<const long long *>(arg + L.start);
   bp.ncx = ncx;
   bp.total = pl.start[ncx];
-  bp.queue = d_queue;
-  bp.gcounts = gcounts;
-  bp.gcount_stride = static_cast<int>(gstride);
+  bp.queue = reinterpret_cast<unsigned long long *>(arg + L.queue);
+  const size_t gs = gcount_stride(pl);
+  bp.gcounts = gs ? reinterpret_cast<uint8_t *>(arg + L.gcounts) : nullptr;
+  bp.gcount_stride = static_cast<int>(gs);
   bp.smem_cnt = pl.smem_cnt;
   bp.max_nr = pl.max_nr;
   bp.warp_smem = static_cast<int>(warp_layout(pl.smem_cnt).total);
   bp.err = ctx->d_err;
+  bp.split = pl.split;
+  bp.pose_start = reinterpret_cast<const long long *>(arg + L.pstart);
+  bp.max_chunks = pl.max_chunks;
+  bp.part = pl.split ? reinterpret_cast<double *>(arg + L.part) : nullptr;
+  bp.pcount = pl.split ? reinterpret_cast<unsigned *>(arg + L.pcount) : nullptr;
+  bp.pdone = pl.split ? reinterpret_cast<int *>(arg + L.pdone) : nullptr;
   e = launch_var(pl.tune, bp, serial, clamp, pl.smem, pl.grid, stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
   return GD_OK;
-}
-
-static size_t arg_bytes(int ncx) {
-  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-  return al(sizeof(ScoreParams) * ncx) + al(sizeof(long long) * (ncx + 1)) + al(sizeof(unsigned long long));
 }
 
 // Score the poses of several complexes in one persistent launch (FP32 form).
@@ -740,27 +874,26 @@ gd_status launch_score_batch_f32(gd_context *ctx, const std::vector<ScoreParams>
   const int ncx = static_cast<int>(descs.size());
   if (ncx == 0) return GD_OK;
   BatchPlan pl;
-  gd_status s = plan_batch(ctx, descs, serial, clamp, slots, &pl);
+  gd_status s = plan_batch(ctx, descs, serial, clamp, slots, true, &pl);
   if (s != GD_OK) return s;
   if (pl.start[ncx] == 0) return GD_OK;
-  const size_t gstride = pl.smem_cnt ? 0 : ((pl.max_nr + 127) / 128) * 128;
-  const size_t gb = gstride * static_cast<size_t>(pl.grid) * kWarps;
-  s = ensure_batch_scratch(ctx, arg_bytes(ncx) + gb);
+  const ArgLayout L = arg_layout(ncx, pl, gcount_stride(pl) * static_cast<size_t>(pl.grid) * kWarps);
+  s = ensure_batch_scratch(ctx, L.total);
   if (s != GD_OK) return s;
   char *arg = static_cast<char *>(ctx->d_batch);
-  return run_batch(ctx, descs, pl, serial, clamp, arg, reinterpret_cast<uint8_t *>(arg + arg_bytes(ncx)), gstride,
-                   stream);
+  s = upload_args(ctx, descs, pl, L, arg, stream, false);
+  if (s != GD_OK) return s;
+  return launch_args(ctx, ncx, pl, L, arg, serial, clamp, stream);
 }
 
-
 // A batched scoring launch whose argument block is uploaded once and whose
-// launch (work-counter reset + kernel) can be replayed, e.g. inside a
-// captured CUDA graph.
+// launch (counter resets + kernel) can be replayed, e.g. inside a captured
+// CUDA graph.
 struct BatchLaunch {
   BatchPlan plan;
+  ArgLayout layout{};
   bool serial = false, clamp = false;
   char *d_arg = nullptr;
-  size_t bytes = 0, gstride = 0;
   int ncx = 0;
 };
 
@@ -772,29 +905,23 @@ gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs_i
   b->serial = serial;
   b->clamp = clamp;
   b->ncx = static_cast<int>(descs.size());
-  gd_status s = plan_batch(ctx, descs, serial, clamp, slots, &b->plan);
+  gd_status s = plan_batch(ctx, descs, serial, clamp, slots, true, &b->plan);
   if (s != GD_OK) {
     delete b;
     return s;
   }
-  b->gstride = b->plan.smem_cnt ? 0 : ((b->plan.max_nr + 127) / 128) * 128;
-  b->bytes = arg_bytes(b->ncx) + b->gstride * static_cast<size_t>(b->plan.grid) * kWarps;
+  b->layout = arg_layout(b->ncx, b->plan, gcount_stride(b->plan) * static_cast<size_t>(b->plan.grid) * kWarps);
   void *p = nullptr;
-  s = dev_alloc(ctx, b->bytes, &p);
+  s = dev_alloc(ctx, b->layout.total, &p);
   if (s != GD_OK) {
     delete b;
     return s;
   }
   b->d_arg = static_cast<char *>(p);
-  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-  const size_t db = sizeof(ScoreParams) * b->ncx, sb = sizeof(long long) * (b->ncx + 1);
-  std::vector<char> h(al(db) + sb);
-  std::memcpy(h.data(), descs.data(), db);
-  std::memcpy(h.data() + al(db), b->plan.start.data(), sb);
-  const cudaError_t e = cudaMemcpy(b->d_arg, h.data(), h.size(), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
+  s = upload_args(ctx, descs, b->plan, b->layout, b->d_arg, nullptr, true);
+  if (s != GD_OK) {
     batch_free(ctx, b);
-    return cuda_fail(ctx, e, "batched scoring arguments");
+    return s;
   }
   *out = b;
   return GD_OK;
@@ -802,33 +929,12 @@ gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs_i
 
 gd_status batch_launch(gd_context *ctx, BatchLaunch *b, cudaStream_t stream) {
   if (b->plan.start[b->ncx] == 0) return GD_OK;
-  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-  const size_t db = sizeof(ScoreParams) * b->ncx, sb = sizeof(long long) * (b->ncx + 1);
-  char *arg = b->d_arg;
-  unsigned long long *d_queue = reinterpret_cast<unsigned long long *>(arg + al(db) + al(sb));
-  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned long long), stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring queue reset");
-  BatchParams bp{};
-  bp.descs = reinterpret_cast<const ScoreParams *>(arg);
-  bp.item_start = reinterpret_cast<const long long *>(arg + al(db));
-  bp.ncx = b->ncx;
-  bp.total = b->plan.start[b->ncx];
-  bp.queue = d_queue;
-  bp.gcounts = reinterpret_cast<uint8_t *>(arg + arg_bytes(b->ncx));
-  bp.gcount_stride = static_cast<int>(b->gstride);
-  bp.smem_cnt = b->plan.smem_cnt;
-  bp.max_nr = b->plan.max_nr;
-  bp.warp_smem = static_cast<int>(warp_layout(b->plan.smem_cnt).total);
-  bp.err = ctx->d_err;
-  const BatchPlan &pl = b->plan;
-  e = launch_var(pl.tune, bp, b->serial, b->clamp, pl.smem, pl.grid, stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
-  return GD_OK;
+  return launch_args(ctx, b->ncx, b->plan, b->layout, b->d_arg, b->serial, b->clamp, stream);
 }
 
 void batch_free(gd_context *ctx, BatchLaunch *b) {
   if (!b) return;
-  if (b->d_arg) dev_free(ctx, b->d_arg, b->bytes);
+  if (b->d_arg) dev_free(ctx, b->d_arg, b->layout.total);
   delete b;
 }
 
@@ -883,7 +989,7 @@ extern "C" gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pos
     return fail(ctx, GD_ERR_INVALID_ARG,
                 "receptor has " + std::to_string(cx->nr) + " atoms; scoring without allocation handles at most " +
                     std::to_string(kCntSmemMax));
-  static_assert(sizeof(ScoreParams) + 2 * sizeof(long long) + sizeof(unsigned long long) + 512 <= kNoAllocScratchBytes,
+  static_assert(4 * 256 + 2 * 256 + sizeof(ScoreParams) <= kNoAllocScratchBytes,
                 "no-allocation scratch too small for one complex");
   if (n == 0) return GD_OK;
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -894,11 +1000,17 @@ extern "C" gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pos
   const std::vector<ScoreParams> descs{make_params(cx, d_frames, nullptr, n, d_out, max_displacement)};
   const int slots = ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune;
   BatchPlan pl;
-  s = plan_batch(ctx, descs, cx->serial_overlap, cx->need_clamp, slots, &pl);
+  s = plan_batch(ctx, descs, cx->serial_overlap, cx->need_clamp, slots, false, &pl);
   if (s != GD_OK) return s;
-  // counters live in shared memory (receptor <= kCntSmemMax atoms): no global counters
-  return run_batch(ctx, descs, pl, cx->serial_overlap, cx->need_clamp, static_cast<char *>(scratch), nullptr, 0,
-                   stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
+  // whole-pose items with counters in shared memory (receptor <= kCntSmemMax
+  // atoms): the argument block is all the scratch there is
+  const ArgLayout L = arg_layout(1, pl, 0);
+  if (L.total > kNoAllocScratchBytes) return fail(ctx, GD_ERR_STATE, "no-allocation scratch too small");
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  char *arg = static_cast<char *>(scratch);
+  s = upload_args(ctx, descs, pl, L, arg, st, false);
+  if (s != GD_OK) return s;
+  return launch_args(ctx, 1, pl, L, arg, cx->serial_overlap, cx->need_clamp, st);
 }
 
 namespace gd {

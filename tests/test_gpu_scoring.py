@@ -201,6 +201,31 @@ def test_receptor_near_shared_counter_limit():
         ctx.close()
 
 
+def test_split_items_bit_identical():
+    """Poses split into ligand chunks (small launches) give exactly the
+    energies of whole-pose work items, for single-chunk and many-chunk
+    ligands and for receptors above the shared-counter limit."""
+    from gdock_gb300 import _lib
+    cases = [synth.make_complex(50, 76, 6, seed=11), synth.make_complex(120, 20, 4, seed=5),
+             synth.make_complex(560, 90, 8, seed=9)]
+    ctx = gd.Context(0)
+    try:
+        for c in cases:
+            lig = gd.position_ligand(c.receptor, c.ligand)
+            cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+            genes = synth.quaternion_genes(np.random.default_rng(3), 40, half_box=8.0)
+            out = {}
+            for mode in (1, 2):
+                ctx.set_tuning(_lib.GD_TUNE_SPLIT, mode)
+                out[mode] = cx.score_poses(genes, gd.GD_PREC_F32)
+            ctx.set_tuning(_lib.GD_TUNE_SPLIT, 0)
+            for name in FIELDS:
+                assert np.array_equal(out[1][name], out[2][name]), (len(c.receptor), len(lig), name)
+            cx.close()
+    finally:
+        ctx.close()
+
+
 def test_deterministic(c1):
     lig = positioned(c1)
     genes = synth.random_genes(np.random.default_rng(9), 20)

@@ -282,8 +282,9 @@ def run_c4(args):
         srv = gd.Server(ctx, max_slots=64, ga=ga)
         srv.start()
         rng = np.random.default_rng(int(rate * 100))
+        jobs = max(per_rate, int(rate))  # at least one second of arrivals
         ids, t0 = [], time.perf_counter()
-        for i in range(per_rate):
+        for i in range(jobs):
             r, l, p = pool[i % len(pool)]
             ids.append(srv.submit(r, l, p, seed=1000 + i))
             time.sleep(float(rng.exponential(1.0 / rate)))
@@ -299,7 +300,7 @@ def run_c4(args):
                              f"last error: {ctx.lib.gd_last_error(ctx.h).decode()}")
         gens = [r.generations for r in res]
         srv.stop()
-        sweep.append({"rate_jobs_per_s": rate, "jobs": per_rate, "jobs_per_s": per_rate / t_all,
+        sweep.append({"rate_jobs_per_s": rate, "jobs": jobs, "jobs_per_s": jobs / t_all,
                       "latency_p50_s": st.latency_p50_s, "latency_p99_s": st.latency_p99_s,
                       "mean_generations": float(np.mean(gens)), "poses_scored": int(st.poses_scored)})
         srv.close()
@@ -311,7 +312,7 @@ def run_c4(args):
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "Poisson arrivals of synthetic complexes (C3 sizes) swept over "
-                                   f"{rates} jobs/s, {per_rate} jobs per rate, GA pop 150, early "
+                                   f"{rates} jobs/s, max({per_rate}, rate x 1 s) jobs per rate, GA pop 150, early "
                                    "stopping after 10 stagnant generations, cap 200", "slots": 64},
             "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64}
     print(json.dumps(line), flush=True)

@@ -561,6 +561,9 @@ struct Job {
   std::vector<double> genes, history;
   std::vector<gd_pose_energy> energies;
   int error = GD_OK;
+  // host draws (made on the submitting thread, uploaded at admission)
+  std::vector<double> d_init, d_cu, d_mu, d_mz;
+  std::vector<int> d_tour, d_perm;
 };
 
 }  // namespace
@@ -644,35 +647,56 @@ gd_status server_alloc(gd_server *S) {
 }
 
 // Upload a job's draws and initial state into slot j.
+// The job's draws for all generations, in the reference's consumption order
+// (src/population.rs:74-158); pure host work, done when the job is submitted.
+void draw_job(const gd_ga_cfg &c, Job *job) {
+  const int n = c.pop_size, m = n, G = std::max(c.max_generations, 1);
+  const size_t gT = static_cast<size_t>(c.tournament_size) * n, gC = 6 * static_cast<size_t>(n / 2),
+               gM = 6 * static_cast<size_t>(m);
+  job->d_init.resize(static_cast<size_t>(n) * 6);
+  job->d_cu.resize(gC * G);
+  job->d_mu.resize(gM * G);
+  job->d_mz.resize(gM * G);
+  job->d_tour.resize(gT * G);
+  job->d_perm.resize(static_cast<size_t>(n) * G);
+  gd_ga_draw(&c, job->seed, c.max_generations, job->d_init.data(), job->d_tour.data(), job->d_perm.data(),
+             job->d_cu.data(), job->d_mu.data(), job->d_mz.data());
+}
+
 gd_status server_load_slot(gd_server *S, int j, Job *job) {
   const gd_ga_cfg &c = S->cfg.ga;
   GaRun &R = S->arena;
   const int n = c.pop_size, m = n, G = c.max_generations;
   const size_t gT = static_cast<size_t>(c.tournament_size) * n, gC = 6 * static_cast<size_t>(n / 2),
                gM = 6 * static_cast<size_t>(m);
-  std::vector<double> genes(static_cast<size_t>(n) * 6), cu(gC * std::max(G, 1)), mu(gM * std::max(G, 1)),
-      mz(gM * std::max(G, 1));
-  std::vector<int> tour(gT * std::max(G, 1)), perm(static_cast<size_t>(n) * std::max(G, 1));
-  gd_ga_draw(&c, job->seed, G, genes.data(), tour.data(), perm.data(), cu.data(), mu.data(), mz.data());
   const size_t Gs = static_cast<size_t>(G);
   cudaStream_t st = S->ctx->stream;
-  cudaError_t e = cudaMemcpyAsync(R.genes + static_cast<size_t>(j) * n * 6, genes.data(), sizeof(double) * genes.size(),
-                                  cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(R.genes + static_cast<size_t>(j) * n * 6, job->d_init.data(),
+                                  sizeof(double) * job->d_init.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && G > 0) {
-    e = cudaMemcpyAsync(R.tour + j * Gs * gT, tour.data(), sizeof(int) * gT * Gs, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(R.tour + j * Gs * gT, job->d_tour.data(), sizeof(int) * gT * Gs, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(R.perm + j * Gs * n, perm.data(), sizeof(int) * n * Gs, cudaMemcpyHostToDevice, st);
+      e = cudaMemcpyAsync(R.perm + j * Gs * n, job->d_perm.data(), sizeof(int) * n * Gs, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(R.cross_u + j * Gs * gC, cu.data(), sizeof(double) * gC * Gs, cudaMemcpyHostToDevice, st);
+      e = cudaMemcpyAsync(R.cross_u + j * Gs * gC, job->d_cu.data(), sizeof(double) * gC * Gs, cudaMemcpyHostToDevice,
+                          st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(R.mut_u + j * Gs * gM, mu.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice, st);
+      e = cudaMemcpyAsync(R.mut_u + j * Gs * gM, job->d_mu.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice,
+                          st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(R.mut_z + j * Gs * gM, mz.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice, st);
+      e = cudaMemcpyAsync(R.mut_z + j * Gs * gM, job->d_mz.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice,
+                          st);
   }
   GaJobState s0{0, 0, 0, 0, 1.7976931348623157e308};
   if (e == cudaSuccess) e = cudaMemcpyAsync(R.state + j, &s0, sizeof(s0), cudaMemcpyHostToDevice, st);
-  // pageable sources: staged before the calls return
+  // pageable sources: staged before the calls return, so the host draws can go
   if (e != cudaSuccess) return cuda_fail(S->ctx, e, "server slot upload");
+  std::vector<double>().swap(job->d_cu);
+  std::vector<double>().swap(job->d_mu);
+  std::vector<double>().swap(job->d_mz);
+  std::vector<int>().swap(job->d_tour);
+  std::vector<int>().swap(job->d_perm);
+  std::vector<double>().swap(job->d_init);
   return GD_OK;
 }
 
@@ -891,7 +915,8 @@ gd_status gd_server_submit(gd_server *S, const gd_atoms *rec, const gd_atoms *li
   job->pairs.assign(pairs, pairs + 2 * static_cast<size_t>(n_pairs));
   job->w = w ? *w : gd_weights{0.4, 0.05, 3.4, 1.0};
   job->seed = seed;
-  job->t_submit = Clock::now();
+  job->t_submit = Clock::now();  // latency counts the draws below
+  gd::draw_job(S->cfg.ga, job);  // on the caller's thread, not the server's
   std::lock_guard<std::mutex> lock(S->mu);
   if (S->failed != GD_OK) {
     delete job;

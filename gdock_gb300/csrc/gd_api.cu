@@ -5,13 +5,14 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <functional>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
 #include <thread>
-#include <unordered_set>
+#include <cstdint>
 #include <utility>
 
 #include "gd_internal.cuh"
@@ -216,20 +217,38 @@ static bool atoms_ok(const gd_atoms *a) {
          a->chain && a->element && a->is_ca;
 }
 
-template <typename T>
-static gd_status upload(gd_complex *cx, const std::vector<T> &h, T **d) {
-  void *p = nullptr;
-  gd_status s = dev_alloc(cx->ctx, sizeof(T) * std::max<size_t>(h.size(), 1), &p);
-  if (s != GD_OK) return s;
-  cx->allocs.push_back(p);
-  cx->bytes += sizeof(T) * std::max<size_t>(h.size(), 1);
-  *d = static_cast<T *>(p);
-  if (!h.empty()) {
-    cudaError_t e = cudaMemcpy(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_fail(cx->ctx, e, "cudaMemcpy (complex upload)");
+// All device arrays of a complex in one allocation and one copy (admitting a
+// docking job costs one cudaMalloc and one cudaMemcpy, not one per array).
+struct UploadPack {
+  struct Item {
+    const void *src;
+    size_t bytes, off;
+    std::function<void(char *)> bind;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  template <typename T>
+  void add(const std::vector<T> &h, T **d) {
+    const size_t off = total;
+    items.push_back(Item{h.empty() ? nullptr : h.data(), sizeof(T) * h.size(), off,
+                         [d, off](char *base) { *d = reinterpret_cast<T *>(base + off); }});
+    total += (sizeof(T) * std::max<size_t>(h.size(), 1) + 255) / 256 * 256;
   }
-  return GD_OK;
-}
+  gd_status commit(gd_complex *cx) {
+    void *p = nullptr;
+    gd_status s = dev_alloc(cx->ctx, total, &p);
+    if (s != GD_OK) return s;
+    cx->allocs.push_back(p);
+    cx->bytes += total;
+    std::vector<char> h(total, 0);
+    for (const Item &it : items)
+      if (it.bytes) std::memcpy(h.data() + it.off, it.src, it.bytes);
+    const cudaError_t e = cudaMemcpy(p, h.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(cx->ctx, e, "cudaMemcpy (complex upload)");
+    for (const Item &it : items) it.bind(static_cast<char *>(p));
+    return GD_OK;
+  }
+};
 
 // Ligand atoms grouped into spatially compact runs of 32 (one FP32 scoring
 // slot each): repeatedly take the remaining atom farthest from the remaining
@@ -246,7 +265,9 @@ static std::vector<int> slot_order(const double *x, const double *y, const doubl
   }
   std::vector<int> rest(n);
   for (int j = 0; j < n; ++j) rest[j] = j;
+  std::vector<char> taken(n, 0);
   std::vector<std::pair<double, int>> d;
+  d.reserve(n);
   while (!rest.empty()) {
     double c[3] = {0, 0, 0};
     for (int j : rest) {
@@ -272,17 +293,16 @@ static std::vector<int> slot_order(const double *x, const double *y, const doubl
     }
     const size_t take = std::min<size_t>(32, d.size());
     std::nth_element(d.begin(), d.begin() + (take - 1), d.end());
-    std::vector<int> grp;
-    for (size_t k = 0; k < take; ++k) grp.push_back(d[k].second);
-    std::sort(grp.begin(), grp.end());
-    order.insert(order.end(), grp.begin(), grp.end());
-    std::vector<char> used(n, 0);
-    for (int j : grp) used[j] = 1;
-    std::vector<int> keep;
-    keep.reserve(rest.size() - take);
+    const size_t o0 = order.size();
+    for (size_t k = 0; k < take; ++k) {
+      order.push_back(d[k].second);
+      taken[d[k].second] = 1;
+    }
+    std::sort(order.begin() + o0, order.end());
+    size_t w = 0;
     for (int j : rest)
-      if (!used[j]) keep.push_back(j);
-    rest.swap(keep);
+      if (!taken[j]) rest[w++] = j;
+    rest.resize(w);
   }
   return order;
 }
@@ -500,8 +520,17 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   }
   cx->lig_radius = rad;
   {
-    std::unordered_set<int32_t> rs(rec->serial, rec->serial + rec->n);
-    for (int j = 0; j < lig->n && !cx->serial_overlap; ++j) cx->serial_overlap = rs.count(lig->serial[j]) > 0;
+    // equal receptor/ligand serials (vdW pairs skipped): disjoint serial
+    // ranges, the usual case, settle it without a search
+    int32_t rlo = INT32_MAX, rhi = INT32_MIN, llo = INT32_MAX, lhi = INT32_MIN;
+    for (int i = 0; i < rec->n; ++i) rlo = std::min(rlo, rec->serial[i]), rhi = std::max(rhi, rec->serial[i]);
+    for (int j = 0; j < lig->n; ++j) llo = std::min(llo, lig->serial[j]), lhi = std::max(lhi, lig->serial[j]);
+    if (rec->n > 0 && lig->n > 0 && rlo <= lhi && llo <= rhi) {
+      std::vector<int32_t> rs(rec->serial, rec->serial + rec->n);
+      std::sort(rs.begin(), rs.end());
+      for (int j = 0; j < lig->n && !cx->serial_overlap; ++j)
+        cx->serial_overlap = std::binary_search(rs.begin(), rs.end(), lig->serial[j]);
+    }
   }
 
   // restraints: first CA with each residue number (src/restraints.rs:44-77)
@@ -523,14 +552,24 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   cx->K = static_cast<int>(rl.size());
 
   gd_status s;
-  if ((s = upload(cx, rp32, &cx->rec_pos32)) != GD_OK || (s = upload(cx, rp64, &cx->rec_pos64)) != GD_OK ||
-      (s = upload(cx, rmeta, &cx->rec_meta)) != GD_OK || (s = upload(cx, rdes, &cx->rec_desolv)) != GD_OK ||
-      (s = upload(cx, lx, &cx->lig_x)) != GD_OK || (s = upload(cx, ly, &cx->lig_y)) != GD_OK ||
-      (s = upload(cx, lz, &cx->lig_z)) != GD_OK || (s = upload(cx, lq, &cx->lig_q)) != GD_OK ||
-      (s = upload(cx, ltp, &cx->lig_type)) != GD_OK || (s = upload(cx, lser, &cx->lig_serial)) != GD_OK ||
-      (s = upload(cx, ldes, &cx->lig_desolv)) != GD_OK || (s = upload(cx, tab32, &cx->tab32)) != GD_OK ||
-      (s = upload(cx, tab64, &cx->tab64)) != GD_OK || (s = upload(cx, rr, &cx->restr_rec)) != GD_OK ||
-      (s = upload(cx, rl, &cx->restr_lig)) != GD_OK || (s = upload(cx, perm, &cx->lig_perm)) != GD_OK) {
+  UploadPack pack;
+  pack.add(rp32, &cx->rec_pos32);
+  pack.add(rp64, &cx->rec_pos64);
+  pack.add(rmeta, &cx->rec_meta);
+  pack.add(rdes, &cx->rec_desolv);
+  pack.add(lx, &cx->lig_x);
+  pack.add(ly, &cx->lig_y);
+  pack.add(lz, &cx->lig_z);
+  pack.add(lq, &cx->lig_q);
+  pack.add(ltp, &cx->lig_type);
+  pack.add(lser, &cx->lig_serial);
+  pack.add(ldes, &cx->lig_desolv);
+  pack.add(tab32, &cx->tab32);
+  pack.add(tab64, &cx->tab64);
+  pack.add(rr, &cx->restr_rec);
+  pack.add(rl, &cx->restr_lig);
+  pack.add(perm, &cx->lig_perm);
+  if ((s = pack.commit(cx)) != GD_OK) {
     gd_complex_destroy(cx);
     return s;
   }

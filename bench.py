@@ -235,6 +235,7 @@ def run_c3(args):
     import gdock_gb300 as gd
     from gdock_gb300 import _lib
     ctx = gd.Context(0)
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
     jobs = _uneven_complexes(64, 33)
     G, pop = 50, 150
     cxs = [gd.Complex(r, l, p, ctx=ctx) for r, l, p in jobs]
@@ -273,6 +274,7 @@ def run_c4(args):
     import gdock_gb300 as gd
     from gdock_gb300 import _lib
     ctx = gd.Context(0)
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
     pool = _uneven_complexes(48, 44)
     ga = _lib.ga_default_cfg(pop_size=150, max_generations=200, early_stopping=1)
     rates = [float(r) for r in os.environ.get("GD_C4_RATES", "1,8,32,200").split(",")]
@@ -322,6 +324,7 @@ def run_c5(args):
     import gdock_gb300 as gd
     from gdock_gb300 import _lib, position_ligand, synth
     ctx = gd.Context(0)
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
     c = synth.make_complex(2000, 500, 30, seed=55)
     lig = position_ligand(c.receptor, c.ligand)
     cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
@@ -358,6 +361,8 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
                     help="c2: single-complex scoring (default); c3: batched uneven GA; c4: served jobs; "
                          "c5: large complex")
+    ap.add_argument("--split", default="auto", choices=["auto", "never", "always"],
+                    help="work items of the FP32 kernel (GD_TUNE_SPLIT): whole poses or ligand chunks")
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
     args = ap.parse_args()

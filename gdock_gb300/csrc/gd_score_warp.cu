@@ -731,10 +731,11 @@ constexpr size_t kSplitScratchMax = size_t(512) << 20;
 
 static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
 
-// Whole poses per work item fill the GPU when there are at least as many
-// poses as resident warps.  With fewer (one GA generation of a few jobs, one
-// docking run's population) each pose is split into its ligand chunks so that
-// every warp has work; the energies are bit-identical either way.
+// Whole poses per work item keep the GPU evenly busy when there are many
+// poses per resident warp.  With fewer than four per warp (one GA generation
+// of a few jobs, one docking run's population, a few thousand poses of a large
+// complex) the last poses leave most warps idle, so each pose is split into
+// its ligand chunks; the energies are bit-identical either way.
 static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
                             int slots, bool allow_split, BatchPlan *pl) {
   const int ncx = static_cast<int>(descs.size());
@@ -766,7 +767,7 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   const bool fits = al256(part_b) + al256(cnt_b) <= kSplitScratchMax;
   pl->split = 0;
   if (allow_split && fits && poses > 0 && pl->max_chunks > 1 && !serial && !clamp)
-    pl->split = ctx->tune_split == 2 || (ctx->tune_split == 0 && poses < warps);
+    pl->split = ctx->tune_split == 2 || (ctx->tune_split == 0 && poses < 4 * warps);
   if (pl->split) {
     pl->part_b = part_b;
     pl->cnt_b = cnt_b;

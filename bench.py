@@ -157,8 +157,11 @@ def within_cutoff_fraction(c, lig, genes, n_sample=16, cutoff=15.0):
     return hit / tot
 
 
-def variant_name(tune: int) -> str:
-    """GD_TUNE_F32_SLOTS value -> 'S<slots per lane>xA<receptor rows per step>xB<min CTAs per SM>'."""
+def variant_name(tune: int, split: int = 0) -> str:
+    """(GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT) -> 'S<slots per lane>xA<receptor rows per step>xB<min CTAs per SM>',
+    or 'split' for ligand chunks as work items."""
+    if split == 2:
+        return "split"
     a = 4 if tune & 64 else (2 if tune & 16 else 1)
     return f"S{tune % 16}xA{a}xB{5 if tune & 256 else 4}"
 
@@ -386,6 +389,8 @@ def main():
 
     c, lig, genes = workload(NP)
     ctx = gd.Context(local)
+    split_mode = {"auto": 0, "never": 1, "always": 2}[args.split]
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, split_mode)
     cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
     lib = ctx.lib
     frames_h = _lib.make_frames(genes)
@@ -404,11 +409,17 @@ def main():
         ctx.check(lib.gd_score_frames_device(cx.h, frames.data_ptr(), n, prec, max_disp, out.data_ptr(),
                                              stream.cuda_stream))
 
-    # --- slots-per-lane sweep (a small autotune on a pose sample) ---
+    # --- kernel-variant sweep (a small autotune on a pose sample); the last
+    # candidate is split mode (ligand chunks as work items), which any
+    # variant value selects once GD_TUNE_SPLIT forces it ---
     tune = {}
-    for slots in (16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4):  # see GD_TUNE_F32_SLOTS
+    candidates = [(v, split_mode) for v in (16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4)]
+    if split_mode == 0:
+        candidates.append((256 + 64 + 4, 2))
+    for slots, split in candidates:  # see GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT
         ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
-        ns_t = min(NP, 16384)
+        ctx.set_tuning(_lib.GD_TUNE_SPLIT, split)
+        ns_t = min(NP, 32768)
         launch(gd.GD_PREC_F32, ns_t)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -416,9 +427,10 @@ def main():
         launch(gd.GD_PREC_F32, ns_t)
         e1.record(stream)
         e1.synchronize()
-        tune[slots] = ns_t / (e0.elapsed_time(e1) / 1e3)
-    best_slots = max(tune, key=tune.get)
+        tune[(slots, split)] = ns_t / (e0.elapsed_time(e1) / 1e3)
+    best_slots, best_split = max(tune, key=tune.get)
     ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, best_slots)
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, best_split)
     ctx.sync()
 
     # --- device-resident throughput (value) ---
@@ -488,8 +500,8 @@ def main():
             "e2e": {"value": e2e, "unit": "poses/s", "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES,
                     "d2h_bytes_per_step": NP * 48},
             "gpu_launches": args.steps,
-            "autotune": {"variant": variant_name(best_slots),
-                         "poses_per_s_by_variant": {variant_name(k): v for k, v in tune.items()}},
+            "autotune": {"variant": variant_name(best_slots, best_split),
+                         "poses_per_s_by_variant": {variant_name(*k): v for k, v in tune.items()}},
             "pair_evals_per_s": pairs * value,
             "plain_fp64": {"value": plain, "unit": "poses/s", "sample_poses": ns,
                            "tflops": FLOP_PER_PAIR * pairs * plain / 1e12,

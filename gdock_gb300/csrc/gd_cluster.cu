@@ -51,6 +51,7 @@ struct ClusterTopo {
   int *d_rg_off = nullptr, *d_lg_off = nullptr;
   float4 *d_rg_sph = nullptr;   // (centre - O, radius) FP32
   D4 *d_lg_sph = nullptr;  // (centre in the positioned frame, radius)
+  D4 *d_lb_sph = nullptr;  // per block of kLigBlock ligand residues: sphere enclosing theirs
   uint8_t *d_rg_chain = nullptr, *d_lg_chain = nullptr;
   std::vector<void *> allocs;
   uint64_t bytes = 0;
@@ -59,6 +60,16 @@ struct ClusterTopo {
 namespace {
 
 constexpr int kMaxGroupAtoms = 64;
+
+// Under GD_TRACE: wait for the stream and print the time since `t` (then
+// reset it), so that device phases can be told apart.  No-op otherwise.
+void trace_step(const char *name, cudaStream_t st, std::chrono::steady_clock::time_point &t) {
+  if (!trace_on()) return;
+  cudaStreamSynchronize(st);
+  const auto now = std::chrono::steady_clock::now();
+  trace(name, std::chrono::duration<double>(now - t).count());
+  t = now;
+}
 
 struct PhaseTimer {
   const char *name;
@@ -108,6 +119,8 @@ struct ContactParams {
 };
 
 constexpr int kContactWarps = 8;
+constexpr int kLigBlock = 8;    // ligand residues per contact-bitmap work item
+constexpr int kCandMax = 1024;  // receptor residue candidates kept per block
 
 __global__ void __launch_bounds__(kContactWarps * 32) k_contacts_rl(const ContactParams p) {
   __shared__ double s_xyz[kContactWarps][3][kMaxGroupAtoms];
@@ -264,6 +277,7 @@ struct BitsParams {
   const double *lx, *ly, *lz;
   const int *lg_off;
   const D4 *lg_sph;
+  const D4 *lb_sph;
   const uint8_t *lg_chain;
   int GR, GL;
   double cx, cy, cz, ox, oy, oz;
@@ -276,19 +290,52 @@ struct BitsParams {
   long long words;
 };
 
-// One warp per (pose, ligand residue): the residue's atoms are transformed
-// exactly and kept in FP64 and FP32; each lane tests receptor residues (culled
-// by bounding spheres), first in FP32, re-deciding in FP64 the atom pairs
-// whose FP32 d2 is within the guard band of the cutoff.
+// One warp per (pose, block of kLigBlock consecutive ligand residues).  The
+// block's enclosing sphere first selects the receptor residues within reach
+// of any of its residues (a shared-memory candidate list; all residues when
+// the list would overflow).  Then, residue by residue, the atoms are
+// transformed exactly and kept in FP64 and FP32, and each lane tests
+// candidate receptor residues (culled by bounding spheres), first in FP32,
+// re-deciding in FP64 the atom pairs whose FP32 d2 is within the guard band
+// of the cutoff.
 __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsParams p) {
   __shared__ double s_xyz[kContactWarps][3][kMaxGroupAtoms];
   __shared__ float4 s_f[kContactWarps][kMaxGroupAtoms];
+  __shared__ uint16_t s_cand[kContactWarps][kCandMax];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long items = static_cast<long long>(p.n) * p.GL;
+  const int nb = (p.GL + kLigBlock - 1) / kLigBlock;
+  const long long items = static_cast<long long>(p.n) * nb;
   for (long long it = static_cast<long long>(blockIdx.x) * kContactWarps + wib; it < items;
        it += static_cast<long long>(gridDim.x) * kContactWarps) {
-    const int pose = static_cast<int>(it / p.GL), lg = static_cast<int>(it % p.GL);
+    const int pose = static_cast<int>(it / nb), blk = static_cast<int>(it % nb);
     const gd_pose_frame f = p.frames[pose];
+    int ncand = 0;
+    {
+      const D4 bs = p.lb_sph[blk];
+      double BX, BY, BZ;
+      xform(f, p.cx, p.cy, p.cz, bs.x, bs.y, bs.z, BX, BY, BZ);
+      const float bcx = static_cast<float>(BX - p.ox), bcy = static_cast<float>(BY - p.oy),
+                  bcz = static_cast<float>(BZ - p.oz), brad = static_cast<float>(bs.w);
+      for (int r0 = 0; r0 < p.GR; r0 += 32) {
+        const int rg = r0 + lane;
+        bool near = false;
+        if (rg < p.GR) {
+          const float4 rs = p.rg_sph[rg];
+          const float dx = rs.x - bcx, dy = rs.y - bcy, dz = rs.z - bcz;
+          const float lim = rs.w + brad + p.reach;
+          near = dx * dx + dy * dy + dz * dz <= lim * lim;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, near);
+        const int pos = ncand + __popc(m & ((1u << lane) - 1u));
+        if (near && pos < kCandMax) s_cand[wib][pos] = static_cast<uint16_t>(rg);
+        ncand += __popc(m);
+      }
+      __syncwarp();
+    }
+    const bool every = ncand > kCandMax;  // list overflowed: scan every receptor residue
+    const int nscan = every ? p.GR : ncand;
+    const int lg_end = min(p.GL, (blk + 1) * kLigBlock);
+    for (int lg = blk * kLigBlock; lg < lg_end; ++lg) {
     const int a0 = p.lg_off[lg], na = min(p.lg_off[lg + 1] - a0, kMaxGroupAtoms);
     for (int a = lane; a < na; a += 32) {
       double X, Y, Z;
@@ -308,31 +355,73 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
     const float lrad = static_cast<float>(ls.w);
     const uint8_t lchain = p.lg_chain[lg];
     uint32_t *row = p.bits + static_cast<size_t>(pose) * p.words;
-    for (int rg = lane; rg < p.GR; rg += 32) {
-      if (p.rg_chain[rg] == lchain) continue;
-      const float4 rs = p.rg_sph[rg];
-      const float dx = rs.x - lcx, dy = rs.y - lcy, dz = rs.z - lcz;
-      const float lim = rs.w + lrad + p.reach;
-      if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
-      bool found = false;
-      for (int b = p.rg_off[rg]; b < p.rg_off[rg + 1] && !found; ++b) {
-        const float4 rb = p.r32[b];
-        for (int a = 0; a < na; ++a) {
-          const float4 la = s_f[wib][a];
-          const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
-          const float d2 = ex * ex + ey * ey + ez * ez;
-          if (d2 > p.t32 + p.guard) continue;
-          if (d2 < p.t32 - p.guard ||
-              d2_exact(p.rx[b], p.ry[b], p.rz[b], s_xyz[wib][0][a], s_xyz[wib][1][a], s_xyz[wib][2][a]) <= p.t_le) {
-            found = true;
-            break;
-          }
+    // lanes split a residue pair's atom pairs: lane = (receptor atom step,
+    // ligand atom a); na <= 32 gives per = 32 / na receptor atoms per round
+    const int per = na <= 32 ? 32 / na : 1;
+    const int my_a = na <= 32 ? lane % na : 0, my_b = na <= 32 ? lane / na : 0;
+    const bool lane_on = na <= 32 && lane < per * na;
+    for (int k0 = 0; k0 < nscan; k0 += 32) {
+      // 32 candidates at a time: the sphere test on one lane each
+      const int k = k0 + lane;
+      int rg = -1;
+      bool near = false;
+      if (k < nscan) {
+        rg = every ? k : s_cand[wib][k];
+        if (p.rg_chain[rg] != lchain) {
+          const float4 rs = p.rg_sph[rg];
+          const float dx = rs.x - lcx, dy = rs.y - lcy, dz = rs.z - lcz;
+          const float lim = rs.w + lrad + p.reach;
+          near = dx * dx + dy * dy + dz * dz <= lim * lim;
         }
       }
-      if (found) {
-        const long long idx = static_cast<long long>(rg) * p.GL + lg;
-        atomicOr(&row[idx >> 5], 1u << (idx & 31));
+      unsigned m = __ballot_sync(0xffffffffu, near);
+      while (m) {
+        // each near receptor residue: the whole warp over its atom pairs,
+        // stopping at the first contact
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const int r = __shfl_sync(0xffffffffu, rg, src);
+        const int b0 = p.rg_off[r], b1 = p.rg_off[r + 1];
+        bool found = false;
+        if (na <= 32) {
+          for (int bb = b0; bb < b1 && !found; bb += per) {
+            const int b = bb + my_b;
+            bool hit = false;
+            if (lane_on && b < b1) {
+              const float4 rb = p.r32[b];
+              const float4 la = s_f[wib][my_a];
+              const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
+              const float d2 = ex * ex + ey * ey + ez * ez;
+              if (d2 <= p.t32 + p.guard)
+                hit = d2 < p.t32 - p.guard || d2_exact(p.rx[b], p.ry[b], p.rz[b], s_xyz[wib][0][my_a],
+                                                      s_xyz[wib][1][my_a], s_xyz[wib][2][my_a]) <= p.t_le;
+            }
+            found = __any_sync(0xffffffffu, hit);
+          }
+        } else {
+          // a residue with more than 32 heavy atoms: lanes over its atoms
+          for (int b = b0; b < b1 && !found; ++b) {
+            const float4 rb = p.r32[b];
+            bool hit = false;
+            for (int a = lane; a < na; a += 32) {
+              const float4 la = s_f[wib][a];
+              const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
+              const float d2 = ex * ex + ey * ey + ez * ez;
+              if (d2 <= p.t32 + p.guard)
+                hit = hit || d2 < p.t32 - p.guard ||
+                      d2_exact(p.rx[b], p.ry[b], p.rz[b], s_xyz[wib][0][a], s_xyz[wib][1][a], s_xyz[wib][2][a]) <=
+                          p.t_le;
+            }
+            found = __any_sync(0xffffffffu, hit);
+          }
+        }
+        if (found && lane == 0) {
+          const long long idx = static_cast<long long>(r) * p.GL + lg;
+          atomicOr(&row[idx >> 5], 1u << (idx & 31));
+        }
       }
+    }
+    __syncwarp();
     }
     __syncwarp();
   }
@@ -533,7 +622,33 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
     lsph[g] = D4{c[0], c[1], c[2], r * (1 + 1e-6) + 1e-3};
     lch[g] = static_cast<uint8_t>(t->lg_key[g] >> 16);
   }
+  // blocks of kLigBlock consecutive ligand residues: a sphere enclosing the
+  // residues' spheres (with the same small widening)
+  const int nb = (t->GL + kLigBlock - 1) / kLigBlock;
+  std::vector<D4> lbsph(std::max(nb, 1), D4{0, 0, 0, 0});
+  for (int b = 0; b < nb; ++b) {
+    const int g0 = b * kLigBlock, g1 = std::min(t->GL, g0 + kLigBlock);
+    double c[3] = {0, 0, 0};
+    for (int g = g0; g < g1; ++g) {
+      c[0] += lsph[g].x;
+      c[1] += lsph[g].y;
+      c[2] += lsph[g].z;
+    }
+    for (double &v : c) v /= (g1 - g0);
+    double r = 0;
+    for (int g = g0; g < g1; ++g)
+      r = std::max(r, std::sqrt((lsph[g].x - c[0]) * (lsph[g].x - c[0]) + (lsph[g].y - c[1]) * (lsph[g].y - c[1]) +
+                                (lsph[g].z - c[2]) * (lsph[g].z - c[2])) +
+                          lsph[g].w);
+    lbsph[b] = D4{c[0], c[1], c[2], r * (1 + 1e-6) + 1e-3};
+  }
   gd_status s;
+  if ((s = topo_upload(ctx, t, lbsph, &t->d_lb_sph)) != GD_OK) {
+    for (void *p : t->allocs) cudaFree(p);
+    ctx->in_use -= std::min<uint64_t>(ctx->in_use, t->bytes);
+    delete t;
+    return s;
+  }
   if ((s = topo_upload(ctx, t, rx, &t->d_rx)) != GD_OK || (s = topo_upload(ctx, t, ry, &t->d_ry)) != GD_OK ||
       (s = topo_upload(ctx, t, rz, &t->d_rz)) != GD_OK || (s = topo_upload(ctx, t, lx, &t->d_lx)) != GD_OK ||
       (s = topo_upload(ctx, t, ly, &t->d_ly)) != GD_OK || (s = topo_upload(ctx, t, lz, &t->d_lz)) != GD_OK ||
@@ -859,6 +974,7 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
     for (int k = 3; k < 6; ++k) maxd = std::max(maxd, std::fabs(genes[6 * static_cast<size_t>(i) + k]));
   const size_t fb = sizeof(gd_pose_frame) * n, ub = sizeof(uint32_t) * words, cb = sizeof(int) * words;
   // the compacted universe is at most min(pairs, sum of sizes); size it after the scan
+  auto t_step = std::chrono::steady_clock::now();
   s = ensure_scratch(ctx, al(fb) + al(bits_b) + al(ub) + 2 * al(cb) + al(sizeof(int)), 0);
   if (s != GD_OK) return s;
   char *base = static_cast<char *>(ctx->d_scratch);
@@ -871,6 +987,7 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaMemcpyAsync(d_frames, frames.data(), fb, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bits, 0, bits_b, st);
+  trace_step("cluster (device):   scratch + frames + clear", st, t_step);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps setup");
   BitsParams p{};
   p.r32 = t->d_r32;
@@ -885,6 +1002,7 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   p.lz = t->d_lz;
   p.lg_off = t->d_lg_off;
   p.lg_sph = t->d_lg_sph;
+  p.lb_sph = t->d_lb_sph;
   p.lg_chain = t->d_lg_chain;
   p.GR = t->GR;
   p.GL = t->GL;
@@ -911,14 +1029,16 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   p.bits = d_bits;
   p.words = words;
   if (pairs > 0 && n > 0) {
-    const long long items = static_cast<long long>(n) * t->GL;
+    const long long items = static_cast<long long>(n) * ((t->GL + kLigBlock - 1) / kLigBlock);
     const int grid = static_cast<int>(std::min<long long>((items + kContactWarps - 1) / kContactWarps,
                                                           static_cast<long long>(ctx->sm_count) * 16));
     k_contact_bits<<<grid, kContactWarps * 32, 0, st>>>(p);
+    trace_step("cluster (device):   k_contact_bits", st, t_step);
   }
   const int g2 = static_cast<int>(std::min<long long>((words + 255) / 256, static_cast<long long>(ctx->sm_count) * 8));
   k_union<<<std::max(g2, 1), 256, 0, st>>>(d_bits, n, words, d_u, d_cnt);
   k_scan<<<1, 1024, 0, st>>>(d_cnt, words, d_base, d_total);
+  trace_step("cluster (device):   k_union + k_scan", st, t_step);
   int U = 0;
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(&U, d_total, sizeof(int), cudaMemcpyDeviceToHost, st);

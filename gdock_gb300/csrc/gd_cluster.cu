@@ -194,7 +194,7 @@ struct FccParams {
 };
 
 constexpr int kFT = 64;   // pose tile
-constexpr int kFW = 16;   // words per staged chunk
+constexpr int kFW = 18;   // words per staged chunk (groups of 3; row stride 19 words: no bank conflicts)
 
 // The common count of a pose pair is symmetric: only tiles on or above the
 // diagonal run, and an off-diagonal tile decides both directions of each pair.
@@ -218,17 +218,28 @@ __global__ void __launch_bounds__(256) k_fcc(const FccParams p) {
       sb[r][w] = (gj < p.n && gw < p.W) ? p.bits[static_cast<size_t>(gj) * p.W + gw] : 0ull;
     }
     __syncthreads();
-#pragma unroll 4
-    for (int w = 0; w < kFW; ++w) {
-      unsigned long long av[4], bv[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) av[a] = sa[ty + 16 * a][w];
-#pragma unroll
-      for (int b = 0; b < 4; ++b) bv[b] = sb[tx + 16 * b][w];
+    // three words at a time through a carry-save step: with l = x0^x1^x2 and
+    // h = majority(x0, x1, x2), popc(x0) + popc(x1) + popc(x2) =
+    // 2 popc(h) + popc(l): two popcounts (the XU pipe) instead of three
+#pragma unroll 1
+    for (int w = 0; w < kFW; w += 3) {
+      unsigned long long av[4][3], bv[4][3];
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) cnt[a][b] += __popcll(av[a] & bv[b]);
+        for (int i = 0; i < 3; ++i) av[a][i] = sa[ty + 16 * a][w + i];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) bv[b][i] = sb[tx + 16 * b][w + i];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const unsigned long long x0 = av[a][0] & bv[b][0], x1 = av[a][1] & bv[b][1], x2 = av[a][2] & bv[b][2];
+          const unsigned long long l = x0 ^ x1 ^ x2, h = (x0 & x1) | (x2 & (x0 ^ x1));
+          cnt[a][b] += 2 * __popcll(h) + __popcll(l);
+        }
     }
     __syncthreads();
   }

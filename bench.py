@@ -234,6 +234,58 @@ def _fp64_ga_cost(gd, _lib, ctx, jobs, pop, gens):
     return dt, pairs
 
 
+def run_c1(args):
+    """The small plain-method config: receptor 50 x ligand 76 residues, 6
+    restraints, GA pop 150 x 50 generations in FP64, then FCC clustering of the
+    final population; one dock per step.  The CPU leg runs the oracle's GA on
+    the same draws (gdock's own loop, threaded per pose) on the host cores."""
+    import gdock_gb300 as gd
+    from gdock_gb300 import _lib, position_ligand, synth
+    ctx = gd.Context(0)
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
+    c = synth.make_complex(50, 76, 6, seed=SEED)
+    lig = position_ligand(c.receptor, c.ligand)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    G, pop = 50, 150
+    cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=G, early_stopping=0, seed=7)
+    for _ in range(max(1, args.warmup)):
+        gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
+    times, times32 = [], []
+    res = None
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        res = gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
+        clusters = cx.cluster(res.genes[0])
+        times.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        r32 = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
+        cx.cluster(r32.genes[0])
+        times32.append(time.perf_counter() - t0)
+    t, t32 = float(np.median(times)), float(np.median(times32))
+    # CPU leg: the oracle's generation loop on the same draws, all host cores
+    from oracle import oracle as orc
+    draws = _lib.ga_draw(cfg, cfg.seed, G)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    g_cpu, e_cpu, _, _ = orc.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, nthreads=threads)
+    orc.cluster([orc.pose_contacts(c.receptor, lig, g) for g in g_cpu])
+    t_cpu = time.perf_counter() - t0
+    same = bool(np.array_equal(g_cpu, res.genes[0]))
+    line = {"metric": "docks/s (plain FP64 GA, pop 150 x 50 generations, then FCC clustering)",
+            "value": 1.0 / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": max(1, args.warmup),
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "synthetic receptor 50 residues x ligand 76 residues, 6 restraints, GA pop 150 "
+                                   "x 50 generations (fixed), FCC clustering of the final population",
+                       "receptor_atoms": len(c.receptor), "ligand_atoms": len(lig)},
+            "clusters": len(clusters),
+            "f32_graph_docks_per_s": 1.0 / t32,
+            "final_population_equals_oracle": same,
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "docks/s", "cores": threads, "kind": "port",
+                             "sample": "one full dock: the oracle's GA on the same draws, then its FCC clustering"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_c3(args):
     import gdock_gb300 as gd
     from gdock_gb300 import _lib
@@ -361,9 +413,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-sample", type=int, default=2048)
     ap.add_argument("--cpu-sample", type=int, default=32)
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
-                    help="c2: single-complex scoring (default); c3: batched uneven GA; c4: served jobs; "
-                         "c5: large complex")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c1: small plain FP64 GA + clustering; c2: single-complex scoring (default); "
+                         "c3: batched uneven GA; c4: served jobs; c5: large complex")
     ap.add_argument("--split", default="auto", choices=["auto", "never", "always"],
                     help="work items of the FP32 kernel (GD_TUNE_SPLIT): whole poses or ligand chunks")
     ap.add_argument("--poses", type=int, default=N_POSES,
@@ -373,7 +425,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "c2":
-        return {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
+        return {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
 
     import torch
     import torch.distributed as dist

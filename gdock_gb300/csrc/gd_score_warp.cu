@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     const int pose = static_cast<int>(SPLIT ? kk / nchunks : kk);
     const int ch0 = SPLIT ? static_cast<int>(kk % nchunks) : 0;
     const int ch1 = SPLIT ? ch0 + 1 : nchunks;
-    const long long gp = SPLIT ? bp.pose_start[lo] + pose : 0;
+    const int gp = SPLIT ? static_cast<int>(bp.pose_start[lo]) + pose : 0;  // poses of a launch fit an int
     if (!p.models && lane < 16)
       reinterpret_cast<double *>(s_frame)[lane] = reinterpret_cast<const double *>(p.frames + pose)[lane];
     __syncwarp();
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         for (int i = lane; i < na; i += 32) {
           const int c = s_rc[i];
           if (c) {
-            if (SPLIT) atomicAdd(&bp.pcount[gp * bp.max_nr + gbase + i], static_cast<unsigned>(c));
+            if (SPLIT) atomicAdd(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + gbase + i], static_cast<unsigned>(c));
             else bump_count(cnt, gbase + i, c);
             s_rc[i] = 0;
           }
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         desolv_t += __ldcg(pt + 64 + lane);
       }
       for (int i = lane; i < p.nr; i += 32) {
-        const unsigned c = __ldcg(&bp.pcount[gp * bp.max_nr + i]);
+        const unsigned c = __ldcg(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + i]);
         desolv_t += p.rec_desolv[static_cast<size_t>(i) * 11 + (c < 10u ? c : 10u)];
       }
     } else {
@@ -656,7 +656,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 }
 
 // Split-mode kernel (a work item is one ligand chunk of a pose): one variant,
-// 4 slots and 4 rows per step, used for launches with fewer poses than warps.
+// 4 slots and 4 rows per step, five CTAs per SM, used for launches with few
+// poses per warp.
 constexpr int kSplitTune = -1;
 
 // Kernel variants.  The common case (no equal receptor/ligand serials, no
@@ -666,7 +667,7 @@ constexpr int kSplitTune = -1;
 // + 256 for the register cap of five resident CTAs per SM.
 template <typename F>
 cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
-  if (tune == kSplitTune) return f(k_score_f32w<4, 4, 4, false, false, true>);
+  if (tune == kSplitTune) return f(k_score_f32w<4, 4, 5, false, false, true>);
   if (serial || clamp) {
     if (serial && clamp) return f(k_score_f32w<4, 1, 4, true, true, false>);
     if (serial) return f(k_score_f32w<4, 1, 4, true, false, false>);

@@ -491,9 +491,8 @@ def main():
     # candidate is split mode (ligand chunks as work items), which any
     # variant value selects once GD_TUNE_SPLIT forces it ---
     tune = {}
-    candidates = [(v, split_mode) for v in (16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4)]
-    if split_mode == 0:
-        candidates.append((256 + 64 + 4, 2))
+    whole = [(v, 1) for v in (16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4)]
+    candidates = {0: whole + [(256 + 64 + 4, 2)], 1: whole, 2: [(256 + 64 + 4, 2)]}[split_mode]
     for slots, split in candidates:  # see GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT
         ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
         ctx.set_tuning(_lib.GD_TUNE_SPLIT, split)

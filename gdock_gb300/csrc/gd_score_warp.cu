@@ -728,15 +728,16 @@ struct BatchPlan {
   size_t part_b = 0, cnt_b = 0, done_b = 0;  // split-mode scratch
 };
 
-constexpr size_t kSplitScratchMax = size_t(512) << 20;
+constexpr size_t kSplitScratchMax = size_t(4) << 30;  // split scratch beyond this: whole poses
 
 static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
 
-// Whole poses per work item keep the GPU evenly busy when there are many
-// poses per resident warp.  With fewer than four per warp (one GA generation
-// of a few jobs, one docking run's population, a few thousand poses of a large
-// complex) the last poses leave most warps idle, so each pose is split into
-// its ligand chunks; the energies are bit-identical either way.
+// Work items are the ligand chunks of the poses (split mode) whenever the
+// split scratch fits (4 GiB and the context's HBM budget): no warp waits on a
+// long pose at the end of a launch, which matters most with few poses per
+// warp (one GA generation of a few jobs, one docking run's population, a few
+// thousand poses of a large complex) and was measured no slower with many.
+// Whole poses per item otherwise; the energies are bit-identical either way.
 static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp,
                             int slots, bool allow_split, BatchPlan *pl) {
   const int ncx = static_cast<int>(descs.size());
@@ -762,13 +763,13 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   int per_sm = 0;
   cudaError_t e = fit(pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0, &per_sm);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
-  const long long warps = static_cast<long long>(per_sm) * ctx->sm_count * kWarps;
   const size_t part_b = static_cast<size_t>(poses) * pl->max_chunks * 96 * sizeof(double);
   const size_t cnt_b = static_cast<size_t>(poses) * pl->max_nr * sizeof(unsigned);
-  const bool fits = al256(part_b) + al256(cnt_b) <= kSplitScratchMax;
+  const size_t split_b = al256(part_b) + al256(cnt_b) + al256(static_cast<size_t>(poses) * sizeof(int));
+  const bool fits = split_b <= kSplitScratchMax && (ctx->budget == 0 || ctx->in_use + split_b <= ctx->budget);
   pl->split = 0;
   if (allow_split && fits && poses > 0 && pl->max_chunks > 1 && !serial && !clamp)
-    pl->split = ctx->tune_split == 2 || (ctx->tune_split == 0 && poses < 4 * warps);
+    pl->split = ctx->tune_split != 1;
   if (pl->split) {
     pl->part_b = part_b;
     pl->cnt_b = cnt_b;

@@ -107,10 +107,10 @@ gd_status gd_context_destroy(gd_context *ctx);
  *                      register cap of five resident CTAs per SM; valid: 4,
  *                      20, 66, 68, 322, 324; 0 = automatic (324).
  *   GD_TUNE_SPLIT:     work items of the FP32 scoring kernel: 0 = automatic
- *                      (a pose is split into its ligand chunks when a launch
- *                      has fewer than four poses per resident warp), 1 = whole
- *                      poses, 2 = always split.  Energies are bit-identical
- *                      either way. */
+ *                      (the ligand chunks of each pose when their scratch fits
+ *                      in 4 GiB and the context's HBM budget, else whole
+ *                      poses), 1 = whole poses, 2 = chunks whenever possible.
+ *                      Energies are bit-identical either way. */
 enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob);

@@ -37,7 +37,7 @@ N_REC_RES, N_LIG_RES, N_RESTRAINTS, N_POSES, SEED = 300, 150, 12, 65536, 2026
 FLOP_PER_PAIR = 37  # convention: d2 8, LJ 18, Coulomb 4, cutoff tests 5, burial 2
 # DRAM bytes per pose of the FP32 scoring kernel: 1.407 MB read + 0 B written
 # over a 4,096-pose launch of this workload (profiles/k_score_f32w_single_complex.md)
-TRAFFIC_PER_POSE = 1.12256e6 / 4096
+TRAFFIC_PER_POSE = (43.122176e6 + 8.095232e6) / 4096  # split-mode kernel, one 4,096-pose ncu capture
 METRIC = "poses/s (batched FP32 scoring, single complex)"
 
 

@@ -405,6 +405,11 @@ gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
     ctx->tune_split = value;
     return GD_OK;
   }
+  if (knob == GD_TUNE_FAULT) {
+    if (value < 0 || value > 1) return fail(ctx, GD_ERR_INVALID_ARG, "fault knob: 0 (off) or 1 (drop one stage copy)");
+    ctx->tune_fault = value;
+    return GD_OK;
+  }
   return fail(ctx, GD_ERR_INVALID_ARG, "unknown tuning knob");
 }
 
@@ -412,6 +417,7 @@ int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob) {
   if (!ctx) return -1;
   if (knob == GD_TUNE_F32_SLOTS) return ctx->tune_f32_slots;
   if (knob == GD_TUNE_SPLIT) return ctx->tune_split;
+  if (knob == GD_TUNE_FAULT) return ctx->tune_fault;
   return -1;
 }
 

@@ -115,6 +115,7 @@ struct gd_context {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int tune_f32_slots = 0;  // 0: automatic (kDefaultF32Tune)
   int tune_split = 0;      // GD_TUNE_SPLIT: 0 automatic, 1 whole poses, 2 always split
+  int tune_fault = 0;      // GD_TUNE_FAULT: 1 = drop one stage copy (failure-detection tests)
 };
 
 struct gd_complex {

@@ -64,6 +64,9 @@ struct BatchParams {
   double *part;                   // [pose][chunk][vdw, elec, ligand desolvation][32 lanes]
   unsigned *pcount;               // [pose][max_nr] receptor burial counts
   int *pdone;                     // [pose] chunks finished
+  // failure-detection test (GD_TUNE_FAULT): the warp that takes work item 0
+  // issues no copy for its first ring stage, so its bounded wait runs out
+  int drop_copy;
 };
 
 struct WarpSmem {
@@ -303,7 +306,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     const long long Qi = static_cast<long long>(ch1 - ch0) * nseg;
     const long long q0 = q;
     if (lane == 0)
-      for (long long k = 0; k < Qi && k < kWS; ++k) issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_bar);
+      for (long long k = 0; k < Qi && k < kWS; ++k)
+        if (!(bp.drop_copy && item == 0 && k == 0))
+          issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_bar);
     const float gv = p.guard_v, ge = p.guard_e, gdd = p.guard_d;
     // a row (receptor atom, ligand slot) whose atom lies farther than this
     // from the slot's bounding sphere has every FP32 d2 beyond the elec
@@ -859,6 +864,7 @@ static gd_status launch_args(gd_context *ctx, int ncx, const BatchPlan &pl, cons
   bp.warp_smem = static_cast<int>(warp_layout(pl.smem_cnt).total);
   bp.err = ctx->d_err;
   bp.split = pl.split;
+  bp.drop_copy = ctx->tune_fault == 1;
   bp.pose_start = reinterpret_cast<const long long *>(arg + L.pstart);
   bp.max_chunks = pl.max_chunks;
   bp.part = pl.split ? reinterpret_cast<double *>(arg + L.part) : nullptr;

@@ -110,8 +110,13 @@ gd_status gd_context_destroy(gd_context *ctx);
  *                      (the ligand chunks of each pose when their scratch fits
  *                      in 4 GiB and the context's HBM budget, else whole
  *                      poses), 1 = whole poses, 2 = chunks whenever possible.
- *                      Energies are bit-identical either way. */
-enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1 };
+ *                      Energies are bit-identical either way.
+ *   GD_TUNE_FAULT:     failure-detection test only: 1 = the FP32 scoring
+ *                      kernel issues no copy for one receptor stage, so that
+ *                      stage's bounded wait (2 s) runs out, the kernel drains
+ *                      its other copies (bounded) and the call reports
+ *                      GD_ERR_TIMEOUT; the context stays usable.  0 = off. */
+enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob);
 

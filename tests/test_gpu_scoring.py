@@ -226,6 +226,33 @@ def test_split_items_bit_identical():
         ctx.close()
 
 
+def test_bounded_wait_times_out_and_context_recovers(c1):
+    """Failure detection without a fault: with GD_TUNE_FAULT one receptor
+    stage copy is never issued, the bounded wait on it runs out, the kernel
+    drains its other copies and returns, and the call reports GD_ERR_TIMEOUT;
+    the same context then scores normally."""
+    import time
+    from gdock_gb300 import _lib
+    ctx = gd.Context(0)
+    try:
+        cx = gd.Complex(c1.receptor, positioned(c1), c1.restraint_pairs, ctx=ctx)
+        genes = synth.quaternion_genes(np.random.default_rng(2), 64, half_box=8.0)
+        ref = cx.score_poses(genes, gd.GD_PREC_F32)
+        ctx.set_tuning(_lib.GD_TUNE_FAULT, 1)
+        t0 = time.time()
+        with pytest.raises(gd.GdError) as ei:
+            cx.score_poses(genes, gd.GD_PREC_F32)
+        ctx.set_tuning(_lib.GD_TUNE_FAULT, 0)
+        assert ei.value.status == 4  # GD_ERR_TIMEOUT
+        assert time.time() - t0 < 30
+        again = cx.score_poses(genes, gd.GD_PREC_F32)
+        for name in FIELDS:
+            assert np.array_equal(again[name], ref[name]), name
+        cx.close()
+    finally:
+        ctx.close()
+
+
 def test_deterministic(c1):
     lig = positioned(c1)
     genes = synth.random_genes(np.random.default_rng(9), 20)

@@ -92,3 +92,30 @@ def test_admission_by_hbm_budget_and_background_thread():
         res = srv.result(jid)[0]
         assert res.queue_s >= 0 and res.latency_s >= res.queue_s
     srv.close()
+
+
+def test_worker_error_fails_jobs_and_refuses_submissions():
+    """A tick that fails (here a bounded wait that runs out, GD_TUNE_FAULT)
+    stops the server's thread: resident and queued jobs end FAILED with the
+    tick's status, and later submissions are refused with GD_ERR_STATE."""
+    ctx = gd.Context(0)
+    try:
+        J = jobs(2)
+        srv = gd.Server(ctx, max_slots=4, ga=ga_cfg())
+        ctx.set_tuning(_lib.GD_TUNE_FAULT, 1)
+        ids = [srv.submit(*J[0], seed=7), srv.submit(*J[1], seed=8)]
+        srv.start()
+        for jid in ids:
+            assert srv.wait(jid, 60.0) == _lib.GD_JOB_FAILED
+        ctx.set_tuning(_lib.GD_TUNE_FAULT, 0)
+        for jid in ids:
+            res = srv.result(jid)[0]
+            assert res.status == _lib.GD_JOB_FAILED and res.error == 4  # GD_ERR_TIMEOUT
+        with pytest.raises(gd.GdError) as ei:
+            srv.submit(*J[0], seed=9)
+        assert ei.value.status == 6  # GD_ERR_STATE
+        assert "timed out" in str(ei.value) or "wait" in str(ei.value)
+        srv.stop()
+        srv.close()
+    finally:
+        ctx.close()

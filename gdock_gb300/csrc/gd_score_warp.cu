@@ -1,28 +1,35 @@
 // Batched FP32 scoring: a persistent kernel in which every warp owns whole
-// work items (one pose of one complex) taken from a global queue, so that
-// poses of many complexes of uneven sizes share one launch and no warp ever
-// waits for another.
+// work items taken from a global queue, so that poses of many complexes of
+// uneven sizes share one launch and no warp ever waits for another.  A work
+// item is one pose, or (split mode, the default) one 128-atom ligand chunk of
+// a pose.
 //
 // Per work item a warp
 //   1. copies the complex's descriptor and the pose frame to its shared memory;
 //   2. for each chunk of 32*S ligand atoms: transforms them exactly (FP64, the
 //      reference's operation order, src/structure.rs:80-131), keeps FP32
-//      copies in registers (S slots of 32 consecutive atoms, one per lane) and
-//      a bounding sphere per slot;
-//   3. streams the receptor through its own ring of shared-memory stages, each
-//      filled by one bulk (TMA) copy of 64 atoms and guarded by a per-warp
-//      mbarrier;
+//      copies in registers (S slots of 32 atoms, one per lane; the ligand is
+//      stored in spatially compact slot order) and a bounding sphere and box
+//      per slot;
+//   3. streams the receptor through its own two-stage shared-memory ring,
+//      each stage filled by one bulk (TMA) copy of 64 atoms and guarded by a
+//      per-warp mbarrier with a bounded wait;
 //   4. row test: each lane takes one (receptor atom, slot) row of an 8 x 4
-//      round and keeps it when the atom lies within the 15 A reach of the
-//      slot's sphere (every pair of a dropped row contributes exactly
-//      nothing); kept rows go to per-slot lists in shared memory;
+//      round; a row whose atom lies beyond the 15 A reach of the slot's
+//      sphere or box is dropped (every pair of it contributes exactly
+//      nothing), one beyond the 12 A reach is a far row (Coulomb only); kept
+//      rows go to per-slot lists in shared memory;
 //   5. evaluates the kept rows four at a time (independent FP32 chains):
-//      soft-core LJ, Coulomb, burial counts, guard band;
-//   6. re-decides in FP64 any pair whose FP32 d2 lies within the guard band of
-//      a cutoff (1, 8, 12, 15 A), so all decisions equal the FP64 ones;
-//   7. reduces in FP64: per-lane Kahan partials, warp sums, desolvation from
-//      the exact burial counts, AIR in restraint order (bit-identical), and
-//      writes the six-field record (src/chromosome.rs:110-127).
+//      soft-core LJ, Coulomb, burial counts and guard-band tests for near
+//      rows, Coulomb and its band for far rows;
+//   6. re-decides in FP64, once per segment, the pairs of flagged steps whose
+//      FP32 d2 lies within the guard band of a cutoff (1, 8, 12, 15 A), so
+//      all decisions equal the FP64 ones;
+//   7. reduces in FP64: per-lane Kahan partials per chunk (split mode: the
+//      chunk that completes a pose adds the chunks' partials in order), warp
+//      sums, desolvation from the exact burial counts, AIR in restraint order
+//      (bit-identical), and writes the six-field record
+//      (src/chromosome.rs:110-127).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -46,7 +53,7 @@ constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up t
 
 struct BatchParams {
   const ScoreParams *descs;       // one per complex
-  const long long *item_start;    // prefix sums of poses, ncx + 1 entries
+  const long long *item_start;    // prefix sums of work items, ncx + 1 entries
   int ncx;
   long long total;
   unsigned long long *queue;      // work counter, zero at launch

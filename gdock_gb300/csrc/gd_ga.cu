@@ -156,7 +156,6 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   int *sel = reinterpret_cast<int *>(f2 + m);      // [n] tournament winners
   int *elite = sel + n;                            // [elitism]
   __shared__ double s_eg[64 * 6];                  // elites' genes, staged before the population is overwritten
-  __shared__ double s_best;
   __shared__ int s_evolve;
   GaJobState &st = P.state[job];
   if (st.stop) return;
@@ -189,7 +188,6 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
         st.gen = gen + 1;
         s_evolve = 1;
       }
-      s_best = best;
     }
   }
   __syncthreads();

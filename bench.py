@@ -385,7 +385,16 @@ def run_c4(args):
                       "latency_p50_s": st.latency_p50_s, "latency_p99_s": st.latency_p99_s,
                       "mean_generations": float(np.mean(gens)), "poses_scored": int(st.poses_scored)})
         srv.close()
-    # plain FP64: one job at a time, 3 generations of a sample job, scaled to its generations
+    # plain FP64 beside it: sample jobs run one at a time to completion (same
+    # GA settings, early stopping), no batching
+    t64 = []
+    for k, (r, l, p) in enumerate(pool[:2]):
+        cx64 = gd.Complex(r, l, p, ctx=ctx)
+        cfg64 = _lib.ga_default_cfg(pop_size=150, max_generations=200, early_stopping=1, seed=1000 + k)
+        t0 = time.perf_counter()
+        gd.run_ga([cx64], cfg64, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
+        t64.append(time.perf_counter() - t0)
+        cx64.close()
     dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, pool[:2], 150, 3)
     best = max(sweep, key=lambda x: x["jobs_per_s"])
     line = {"metric": "served docking jobs/s with p50/p99 latency (continuous batching)",
@@ -395,7 +404,9 @@ def run_c4(args):
             "config": {"workload": "Poisson arrivals of synthetic complexes (C3 sizes) swept over "
                                    f"{rates} jobs/s, max({per_rate}, rate x 1 s) jobs per rate, GA pop 150, early "
                                    "stopping after 10 stagnant generations, cap 200", "slots": 64},
-            "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64}
+            "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64,
+            "plain_fp64_one_job_at_a_time": {"jobs": len(t64), "seconds_per_job": float(np.mean(t64)),
+                                             "jobs_per_s": len(t64) / float(np.sum(t64))}}
     print(json.dumps(line), flush=True)
 
 
@@ -416,6 +427,12 @@ def run_c5(args):
     t0 = time.perf_counter()
     clusters = cx.cluster(res.genes[0])
     t_fcc = time.perf_counter() - t0
+    # the general path (contact keys per pose, then FCC over the key sets)
+    # must give the same clusters bit for bit
+    t0 = time.perf_counter()
+    general = gd.cluster_sets(cx.pose_contacts(res.genes[0]), ctx=ctx)
+    t_general = time.perf_counter() - t0
+    same = [(r.center_idx, r.members) for r in clusters] == [(r.center_idx, r.members) for r in general]
     pairs = len(c.receptor) * len(lig) * 4096 * (G + 1)
     line = {"metric": "poses/s (large complex GA, pop 4096) and FCC clustering time over 4096 poses",
             "value": 4096 * (G + 1) / t_ga, "unit": "poses/s", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -426,7 +443,8 @@ def run_c5(args):
                        "ligand_atoms": len(lig)},
             "pair_evals_per_s": pairs / t_ga, "ga_seconds": t_ga,
             "fcc": {"poses": 4096, "seconds": t_fcc, "fcc_pairs_per_s": 4096 * 4096 / t_fcc,
-                    "clusters": len(clusters)},
+                    "clusters": len(clusters), "same_as_general_path": same,
+                    "general_path_seconds": t_general},
             "autotune": tuned}
     print(json.dumps(line), flush=True)
 

@@ -21,6 +21,7 @@ reference itself is Rust and cannot be built here) on all host threads.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -505,27 +506,19 @@ def main():
         ctx.check(lib.gd_score_frames_device(cx.h, frames.data_ptr(), n, prec, max_disp, out.data_ptr(),
                                              stream.cuda_stream))
 
-    # --- kernel-variant sweep (a small autotune on a pose sample); the last
-    # candidate is split mode (ligand chunks as work items), which any
-    # variant value selects once GD_TUNE_SPLIT forces it ---
-    tune = {}
-    whole = [(v, 1) for v in (16 + 4, 64 + 2, 64 + 4, 256 + 64 + 2, 256 + 64 + 4)]
-    candidates = {0: whole + [(256 + 64 + 4, 2)], 1: whole, 2: [(256 + 64 + 4, 2)]}[split_mode]
-    for slots, split in candidates:  # see GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT
-        ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, slots)
-        ctx.set_tuning(_lib.GD_TUNE_SPLIT, split)
-        ns_t = min(NP, 32768)
-        launch(gd.GD_PREC_F32, ns_t)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        launch(gd.GD_PREC_F32, ns_t)
-        e1.record(stream)
-        e1.synchronize()
-        tune[(slots, split)] = ns_t / (e0.elapsed_time(e1) / 1e3)
-    best_slots, best_split = max(tune, key=tune.get)
-    ctx.set_tuning(_lib.GD_TUNE_F32_SLOTS, best_slots)
-    ctx.set_tuning(_lib.GD_TUNE_SPLIT, best_split)
+    # --- kernel-variant sweep: the library's autotuner on a pose sample
+    # (whole-pose variants and split mode; it sets the context's knobs) ---
+    ns_t = min(NP, 32768)
+    if split_mode == 0:
+        rates = (C.c_double * len(_lib.AUTOTUNE_CANDIDATES))()
+        best = C.c_int32()
+        ctx.check(lib.gd_autotune_f32(cx.h, frames.data_ptr(), ns_t, max_disp, out.data_ptr(), stream.cuda_stream,
+                                      rates, C.byref(best)))
+        tune = {k: rates[i] for i, k in enumerate(_lib.AUTOTUNE_CANDIDATES)}
+        best_slots, best_split = _lib.AUTOTUNE_CANDIDATES[best.value]
+    else:
+        best_slots, best_split = 256 + 64 + 4, split_mode
+        tune = {}
     ctx.sync()
 
     # --- device-resident throughput (value) ---

@@ -25,8 +25,10 @@ EXPORTS = (
     "gd_context_get_tuning", "gd_score_frames_device_noalloc", "gd_ga_default_cfg", "gd_ga_draw", "gd_ga_run",
     "gd_server_default_cfg", "gd_server_create", "gd_server_destroy", "gd_server_submit", "gd_server_step",
     "gd_server_start", "gd_server_stop", "gd_server_wait", "gd_server_result", "gd_server_release",
-    "gd_server_get_stats",
+    "gd_server_get_stats", "gd_autotune_f32",
 )
+# candidates of gd_autotune_f32, in its order: (GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT)
+AUTOTUNE_CANDIDATES = ((16 + 4, 1), (64 + 2, 1), (64 + 4, 1), (256 + 64 + 2, 1), (256 + 64 + 4, 1), (256 + 64 + 4, 2))
 GD_JOB_QUEUED, GD_JOB_RUNNING, GD_JOB_DONE, GD_JOB_FAILED = range(4)
 GD_TUNE_F32_SLOTS = 0
 GD_TUNE_SPLIT = 1
@@ -132,6 +134,7 @@ def load(path: Path = LIB_PATH):
         "gd_server_result": ([vp, i64, C.POINTER(GdJobResult), vp, vp, vp], C.c_int),
         "gd_server_release": ([vp, i64], C.c_int),
         "gd_server_get_stats": ([vp, C.POINTER(GdServerStats)], C.c_int),
+        "gd_autotune_f32": ([vp, vp, i32, d, vp, vp, vp, C.POINTER(i32)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)

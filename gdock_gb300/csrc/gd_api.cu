@@ -680,6 +680,51 @@ gd_status gd_score_frames_device(gd_complex *cx, const gd_pose_frame *d_frames, 
                       max_displacement);
 }
 
+gd_status gd_autotune_f32(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n, double max_displacement,
+                          gd_pose_energy *d_out, void *stream, double *rates, int32_t *best) {
+  if (!cx) return GD_ERR_INVALID_ARG;
+  gd_context *ctx = cx->ctx;
+  if (n <= 0 || !d_frames || !d_out) return fail(ctx, GD_ERR_INVALID_ARG, "bad frames/out");
+  if (!(max_displacement >= 0.0)) return fail(ctx, GD_ERR_INVALID_ARG, "bad max_displacement");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  // (GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT): whole-pose variants, then the split kernel
+  static const int kCand[GD_AUTOTUNE_CANDIDATES][2] = {{16 + 4, 1}, {64 + 2, 1}, {64 + 4, 1},
+                                                       {256 + 64 + 2, 1}, {256 + 64 + 4, 1}, {kDefaultF32Tune, 2}};
+  const int keep_tune = ctx->tune_f32_slots, keep_split = ctx->tune_split;
+  int arg = -1;
+  double top = -1.0;
+  for (int c = 0; c < GD_AUTOTUNE_CANDIDATES; ++c) {
+    ctx->tune_f32_slots = kCand[c][0];
+    ctx->tune_split = kCand[c][1];
+    gd_status s = launch_score(cx, d_frames, nullptr, n, GD_PREC_F32, d_out, st, max_displacement);
+    cudaError_t e = cudaSuccess;
+    if (s == GD_OK) e = cudaEventRecord(ctx->ev0, st);
+    if (s == GD_OK && e == cudaSuccess) s = launch_score(cx, d_frames, nullptr, n, GD_PREC_F32, d_out, st, max_displacement);
+    if (s == GD_OK && e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
+    if (s == GD_OK && e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+    float ms = 0.0f;
+    if (s == GD_OK && e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    if (s == GD_OK && e != cudaSuccess) s = cuda_fail(ctx, e, "autotune timing");
+    if (s == GD_OK) s = check_device_error(ctx);
+    if (s != GD_OK) {
+      ctx->tune_f32_slots = keep_tune;
+      ctx->tune_split = keep_split;
+      return s;
+    }
+    const double r = ms > 0.0f ? n / (ms * 1e-3) : 0.0;
+    if (rates) rates[c] = r;
+    if (r > top) {
+      top = r;
+      arg = c;
+    }
+  }
+  ctx->tune_f32_slots = kCand[arg][0];
+  ctx->tune_split = kCand[arg][1];
+  if (best) *best = arg;
+  return GD_OK;
+}
+
 gd_status gd_sync(gd_context *ctx) {
   if (!ctx) return GD_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);

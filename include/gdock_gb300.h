@@ -118,6 +118,16 @@ gd_status gd_context_destroy(gd_context *ctx);
  *                      GD_ERR_TIMEOUT; the context stays usable.  0 = off. */
 enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
+/* The FP32 scoring autotuner: times every candidate (GD_TUNE_F32_SLOTS,
+ * GD_TUNE_SPLIT) = (20,1) (66,1) (68,1) (322,1) (324,1) (324,2) on n
+ * device-resident poses of cx (two launches each, CUDA events on `stream`,
+ * NULL = the context's stream) and sets both knobs to the fastest.  rates
+ * (may be NULL) receives poses/s per candidate in that order; *best (may be
+ * NULL) the index of the chosen one.  The complex's own size and the pose
+ * count matter: tune on a sample of the real workload. */
+#define GD_AUTOTUNE_CANDIDATES 6
+gd_status gd_autotune_f32(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n, double max_displacement,
+                          gd_pose_energy *d_out, void *stream, double *rates, int32_t *best);
 int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob);
 
 /* Message of the last failing call on this context ("" if none). */

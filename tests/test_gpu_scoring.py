@@ -253,6 +253,38 @@ def test_bounded_wait_times_out_and_context_recovers(c1):
         ctx.close()
 
 
+def test_autotuner_sets_the_fastest_candidate(c1):
+    """gd_autotune_f32 times every candidate on device-resident poses, sets
+    the context's knobs to the fastest, and scoring stays within tolerance."""
+    import ctypes as C
+    import torch
+    from gdock_gb300 import _lib
+    ctx = gd.Context(0)
+    try:
+        cx = gd.Complex(c1.receptor, positioned(c1), c1.restraint_pairs, ctx=ctx)
+        genes = synth.quaternion_genes(np.random.default_rng(4), 512, half_box=8.0)
+        frames = torch.from_numpy(_lib.make_frames(genes)).to("cuda:0")
+        out = torch.zeros((len(genes), 6), dtype=torch.float64, device="cuda:0")
+        rates = (C.c_double * len(_lib.AUTOTUNE_CANDIDATES))()
+        best = C.c_int32(-1)
+        ctx.check(ctx.lib.gd_autotune_f32(cx.h, frames.data_ptr(), len(genes), float(np.abs(genes[:, 3:]).max()),
+                                          out.data_ptr(), None, rates, C.byref(best)))
+        assert 0 <= best.value < len(_lib.AUTOTUNE_CANDIDATES)
+        assert all(r > 0 for r in rates) and rates[best.value] == max(rates)
+        tune, split = _lib.AUTOTUNE_CANDIDATES[best.value]
+        assert ctx.lib.gd_context_get_tuning(ctx.h, _lib.GD_TUNE_F32_SLOTS) == tune
+        assert ctx.lib.gd_context_get_tuning(ctx.h, _lib.GD_TUNE_SPLIT) == split
+        e32 = cx.score_poses(genes, gd.GD_PREC_F32)
+        e64 = cx.score_poses(genes, gd.GD_PREC_F64)
+        for name in ("vdw", "elec"):
+            assert np.all(rel_err(e32[name], e64[name]) <= F32_TOL), name
+        for name in ("desolv", "air"):
+            assert np.array_equal(e32[name], e64[name]) or np.all(rel_err(e32[name], e64[name]) <= 1e-12), name
+        cx.close()
+    finally:
+        ctx.close()
+
+
 def test_deterministic(c1):
     lig = positioned(c1)
     genes = synth.random_genes(np.random.default_rng(9), 20)

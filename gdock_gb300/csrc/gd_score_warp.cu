@@ -299,8 +299,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     __syncwarp();
     const ScoreParams &p = *s_desc;
     if (p.skip && *p.skip) continue;  // this complex is finished (e.g. a converged GA job)
-    const int nchunks = (p.nl + kChunk - 1) / kChunk;
-    // split mode: item = (pose, chunk); otherwise item = pose, all chunks
+    // split mode: item = (pose, chunk), at least one chunk per pose (an
+    // empty ligand's single chunk holds no atom); otherwise item = pose
+    const int nchunks = SPLIT ? max(1, (p.nl + kChunk - 1) / kChunk) : (p.nl + kChunk - 1) / kChunk;
     const int pose = static_cast<int>(SPLIT ? kk / nchunks : kk);
     const int ch0 = SPLIT ? static_cast<int>(kk % nchunks) : 0;
     const int ch1 = SPLIT ? ch0 + 1 : nchunks;
@@ -793,7 +794,7 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
     pl->part_b = pl->cnt_b = pl->done_b = 0;
   }
   for (int c = 0; c < ncx; ++c) {
-    const long long per_pose = pl->split ? (descs[c].nl + chunk_split - 1) / chunk_split : 1;
+    const long long per_pose = pl->split ? std::max(1, (descs[c].nl + chunk_split - 1) / chunk_split) : 1;
     pl->start[c + 1] = pl->start[c] + static_cast<long long>(descs[c].n_poses) * per_pose;
   }
   const long long items = pl->start[ncx];

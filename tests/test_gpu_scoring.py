@@ -285,6 +285,28 @@ def test_autotuner_sets_the_fastest_candidate(c1):
         ctx.close()
 
 
+@pytest.mark.parametrize("split", [1, 2])
+def test_empty_molecules(oracle, split):
+    """An empty ligand or receptor scores zero pair terms (and the receptor's
+    or ligand's desolvation at zero burial), in both forms and both work-item
+    modes, like the oracle."""
+    from gdock_gb300 import _lib
+    c = synth.make_complex(30, 20, 0, seed=3)
+    empty = make_mol([])
+    ctx = gd.Context(0)
+    try:
+        ctx.set_tuning(_lib.GD_TUNE_SPLIT, split)
+        genes = synth.quaternion_genes(np.random.default_rng(1), 3, half_box=5.0)
+        for rec, lig in ((c.receptor, empty), (empty, c.ligand)):
+            cx = gd.Complex(rec, lig, [], ctx=ctx)
+            ref = oracle.score_poses(rec, lig, [], genes)
+            for prec, tol in ((gd.GD_PREC_F64, F64_TOL), (gd.GD_PREC_F32, F32_TOL)):
+                check(cx.score_poses(genes, prec), ref, tol)
+            cx.close()
+    finally:
+        ctx.close()
+
+
 def test_deterministic(c1):
     lig = positioned(c1)
     genes = synth.random_genes(np.random.default_rng(9), 20)

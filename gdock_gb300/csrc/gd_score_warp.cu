@@ -77,7 +77,7 @@ struct BatchParams {
 };
 
 struct WarpSmem {
-  size_t pos, meta, list, fixq, lfix, bars, desc, frame, blob, box, rc, cnt, total;
+  size_t pos, meta, list, fixq, cmask, cidx, lfix, bars, desc, frame, blob, box, rc, cnt, total;
 };
 
 __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
@@ -95,6 +95,12 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   al(16);
   L.fixq = o;
   o += sizeof(uint16_t) * kMaxS * kList;  // at most one entry per step of a segment
+  al(16);
+  L.cmask = o;  // per near row of the segment: lanes with d2 < 64 (ballot)
+  o += sizeof(unsigned) * kMaxS * kList;
+  al(16);
+  L.cidx = o;   // ... and its receptor atom (stage index)
+  o += sizeof(uint16_t) * kMaxS * kList;
   al(16);
   L.lfix = o;
   o += sizeof(int) * kMaxS * 32;
@@ -250,6 +256,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   uint16_t *s_list = reinterpret_cast<uint16_t *>(base + L.list);  // kept rows per slot, as stage indices
   uint16_t *s_fixq = reinterpret_cast<uint16_t *>(base + L.fixq);  // flagged steps: list position | slot << 8
   int *s_lfix = reinterpret_cast<int *>(base + L.lfix);            // ligand burial corrections per slot and lane
+  unsigned *s_cmask = reinterpret_cast<unsigned *>(base + L.cmask);  // near rows' burial ballots (this segment)
+  uint16_t *s_cidx = reinterpret_cast<uint16_t *>(base + L.cidx);
   uint64_t *s_bar = reinterpret_cast<uint64_t *>(base + L.bars);
   ScoreParams *s_desc = reinterpret_cast<ScoreParams *>(base + L.desc);
   gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(base + L.frame);
@@ -405,6 +413,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       const float mnear = myb.w + reach_v, mnear2 = mnear * mnear;
       float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
       int nfix = 0;  // flagged steps of the current segment
+      int ncm = 0;   // recorded near rows of the current segment
       for (int g = 0; g < nseg; ++g, ++q) {
         const int st = static_cast<int>(q % kWS);
         const bool ok = __all_sync(kFull, mbar_wait(&s_bar[st], static_cast<uint32_t>((q / kWS) & 1)));
@@ -498,18 +507,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
               if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
               ++nfix;
             }
-            // receptor burial counts of the step's rows: lane i adds row i's
-            // total (distinct atoms; the far atom never counts)
-            int my_t = 0, my_ix = kFar;
+            // receptor burial counts of the step's rows: their ballots are
+            // recorded here and added up once per segment (below)
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
-              const int tot = __reduce_add_sync(kFull, rc[i]);
+              const unsigned bm = __ballot_sync(kFull, rc[i] != 0);
               if (lane == i) {
-                my_t = tot;
-                my_ix = ix[i];
+                s_cmask[ncm + i] = bm;
+                s_cidx[ncm + i] = static_cast<uint16_t>(ix[i]);
               }
             }
-            if (my_t) s_rc[my_ix - sbase] += my_t;  // a counted row is a real atom of this stage
+            ncm += kAtoms;
           }
           ae = __fmaf_rn(aes, lq[s], ae);
         }
@@ -545,6 +553,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           }
         }
         nfix = 0;
+        // receptor burial counts of the near rows (the far atom's ballots are 0)
+        for (int t = lane; t < ncm; t += 32) {
+          const unsigned bm = s_cmask[t];
+          if (bm) atomicAdd(&s_rc[s_cidx[t] - sbase], __popc(bm));
+        }
+        ncm = 0;
         kahan_add(sv, cv, av);
         kahan_add(se, ce, ae);
         __syncwarp();

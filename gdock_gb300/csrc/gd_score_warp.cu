@@ -412,8 +412,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       const float mlim2 = (myb.w >= 0.0f) ? mlim * mlim : -1.0f;  // empty slot: no row kept
       const float mnear = myb.w + reach_v, mnear2 = mnear * mnear;
       float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
-      int nfix = 0;  // flagged steps of the current segment
-      int ncm = 0;   // recorded near rows of the current segment
+      // per segment: flagged steps (high 16 bits) and recorded near rows (low 16)
+      int seg_cnt = 0;
       for (int g = 0; g < nseg; ++g, ++q) {
         const int st = static_cast<int>(q % kWS);
         const bool ok = __all_sync(kFull, mbar_wait(&s_bar[st], static_cast<uint32_t>((q / kWS) & 1)));
@@ -478,9 +478,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             bool amb = false;
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) pair32_elec(r[i], lx[s], ly[s], lz[s], ge, aes, amb);
-            if (__any_sync(kFull, amb)) {  // at most one entry per step: nfix <= 4 * 18 per segment
-              if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
-              ++nfix;
+            if (__any_sync(kFull, amb)) {  // at most one entry per step: <= 4 * 18 per segment
+              if (lane == 0) s_fixq[seg_cnt >> 16] = static_cast<uint16_t>(k0 | (s << 8));
+              seg_cnt += 1 << 16;
             }
           }
           // near rows: every term; the first step may start in the padding
@@ -503,9 +503,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             for (int i = 0; i < kAtoms; ++i)
               pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lt[s], lser[s], gv, ge, gdd, av,
                                     aes, lcnt[s], rc[i], amb);
-            if (__any_sync(kFull, amb)) {  // at most one entry per step: nfix <= 4 * 18 per segment
-              if (lane == 0) s_fixq[nfix] = static_cast<uint16_t>(k0 | (s << 8));
-              ++nfix;
+            if (__any_sync(kFull, amb)) {  // at most one entry per step: <= 4 * 18 per segment
+              if (lane == 0) s_fixq[seg_cnt >> 16] = static_cast<uint16_t>(k0 | (s << 8));
+              seg_cnt += 1 << 16;
             }
             // receptor burial counts of the step's rows: their ballots are
             // recorded here and added up once per segment (below)
@@ -513,16 +513,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             for (int i = 0; i < kAtoms; ++i) {
               const unsigned bm = __ballot_sync(kFull, rc[i] != 0);
               if (lane == i) {
-                s_cmask[ncm + i] = bm;
-                s_cidx[ncm + i] = static_cast<uint16_t>(ix[i]);
+                s_cmask[(seg_cnt & 0xffff) + i] = bm;
+                s_cidx[(seg_cnt & 0xffff) + i] = static_cast<uint16_t>(ix[i]);
               }
             }
-            ncm += kAtoms;
+            seg_cnt += kAtoms;
           }
           ae = __fmaf_rn(aes, lq[s], ae);
         }
         __syncwarp();
         // FP64 re-decisions of the flagged steps' pairs in the guard band
+        const int nfix = seg_cnt >> 16, ncm = seg_cnt & 0xffff;
 #pragma unroll 1
         for (int t = 0; t < nfix; ++t) {
           const int e = s_fixq[t], k0 = e & 255, s = e >> 8;
@@ -552,13 +553,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             }
           }
         }
-        nfix = 0;
         // receptor burial counts of the near rows (the far atom's ballots are 0)
         for (int t = lane; t < ncm; t += 32) {
           const unsigned bm = s_cmask[t];
           if (bm) atomicAdd(&s_rc[s_cidx[t] - sbase], __popc(bm));
         }
-        ncm = 0;
+        seg_cnt = 0;
         kahan_add(sv, cv, av);
         kahan_add(se, ce, ae);
         __syncwarp();

@@ -64,9 +64,12 @@ class Clocks:
     """nvidia-smi sampling during the timed region."""
 
     def __init__(self, index=0):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        # raw samples: GD_CLOCKS_DIR when set (to keep them), else a temporary directory
+        out = Path(os.environ.get("GD_CLOCKS_DIR") or tempfile.gettempdir())
+        self.path = out / f"gd_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:

@@ -453,6 +453,101 @@ def run_c5(args):
     print(json.dumps(line), flush=True)
 
 
+EVAL_FLOP = {"transform": 28, "distance": 10, "contact": 9}  # FP64 flop convention of the DockQ kernel
+
+
+def run_dockq(args):
+    """DockQ / L-RMSD / i-RMSD / Fnat of a population against a reference
+    ligand (Population::eval_metrics, src/population.rs:63-71) on the
+    single-complex scoring workload: the reference structure is the synthetic
+    ligand's own placement moved 17 A towards the receptor (an interface of
+    9 + 15 residues and 175 native contacts, the size of gdock's 2oob test
+    complex: 10 + 13 and 222); the 65,536 SO(3)-uniform poses are the
+    population."""
+    import dataclasses
+    import torch
+    import gdock_gb300 as gd
+    from gdock_gb300 import _lib
+    NP = args.poses
+    c, lig, genes = workload(NP)
+    ctx = gd.Context(0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    reference = dataclasses.replace(c.ligand, x=c.ligand.x - 17.0)
+    ev = gd.Evaluator(cx, reference)
+    counts = ev.counts()
+    frames = torch.from_numpy(_lib.make_frames(genes)).cuda()
+    out = torch.zeros((NP, 4), dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def launch():
+        ev.eval_frames_device(frames.data_ptr(), NP, out.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    ctx.sync()
+    times = []
+    with Clocks(0) as clk:
+        time.sleep(0.5)
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    ctx.sync()
+    t_step = float(np.mean(times))
+    dev = out.cpu().numpy()
+    ev.eval_metrics(genes[:1024])  # warm
+    e2e_t = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        host = ev.eval_metrics(genes)
+        e2e_t.append(time.perf_counter() - t0)
+    same = bool(np.array_equal(np.stack([host[k] for k in host.dtype.names], axis=1), dev))
+    # the oracle on a bounded sample, timed on one host core, and checked
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    orc = oracle.Evaluator(c.receptor, reference)
+    ns = args.cpu_sample
+    t0 = time.perf_counter()
+    ref = orc.eval_metrics(lig, genes[:ns])
+    t_cpu = time.perf_counter() - t0
+    err = np.abs(dev[:ns] - ref) / np.maximum(np.abs(ref), 1e-300)
+    flop = (EVAL_FLOP["transform"] * counts["ligand_atoms_read"]
+            + EVAL_FLOP["distance"] * (counts["lrmsd_pairs"] + counts["irmsd_pairs"])
+            + EVAL_FLOP["contact"] * counts["contact_pairs_tested"])
+    peaks = measured_peaks(torch)
+    achieved = flop * NP / t_step / 1e12
+    line = {"metric": "poses/s (DockQ metrics of a population, FP64)", "value": NP / t_step, "unit": "poses/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "DockQ of 65,536 SO(3)-uniform poses of the synthetic 300-residue receptor x "
+                                   "150-residue ligand against its placement moved 17 A towards the receptor",
+                       "poses_per_step": NP, "l2": "flushed between timed steps (256 MiB write)", **counts},
+            "e2e": {"value": NP / float(np.median(e2e_t)), "unit": "poses/s",
+                    "h2d_bytes_per_step": NP * _lib.POSE_FRAME_BYTES, "d2h_bytes_per_step": NP * 32,
+                    "same_as_device_path": same},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64"], "unit": "TFLOP/s",
+                         "frac": achieved / peaks["fp64"], "traffic": None,
+                         "peak_source": "cuBLAS DGEMM measured in this run",
+                         "flop_per_pose": flop, "flop_convention": EVAL_FLOP},
+            "max_rel_error_vs_oracle": {k: float(err[:, i].max()) for i, k in
+                                        enumerate(("rmsd", "irmsd", "fnat", "dockq"))},
+            "cpu_baseline": {"value": ns / t_cpu, "unit": "poses/s", "cores": 1, "kind": "port",
+                             "sample": f"{ns} poses of the workload (numpy oracle)"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ev.close()
+    cx.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -461,9 +556,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-sample", type=int, default=2048)
     ap.add_argument("--cpu-sample", type=int, default=32)
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "dockq"],
                     help="c1: small plain FP64 GA + clustering; c2: single-complex scoring (default); "
-                         "c3: batched uneven GA; c4: served jobs; c5: large complex")
+                         "c3: batched uneven GA; c4: served jobs; c5: large complex; "
+                         "dockq: DockQ metrics of the c2 poses")
     ap.add_argument("--split", default="auto", choices=["auto", "never", "always"],
                     help="work items of the FP32 kernel (GD_TUNE_SPLIT): whole poses or ligand chunks")
     ap.add_argument("--poses", type=int, default=N_POSES,
@@ -473,7 +569,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "c2":
-        return {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
+        return {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5,
+                "dockq": run_dockq}[args.workload](args)
 
     import torch
     import torch.distributed as dist

@@ -12,6 +12,8 @@ used by the tests and the benchmark, with the reference's names:
 * ``Complex.pose_contacts`` -> clustering::calculate_contacts (src/clustering.rs:62-115)
 * ``Complex.cluster`` / ``cluster_sets`` -> clustering::cluster_structures
   (src/clustering.rs:265-293)
+* ``Evaluator`` -> evaluator::Evaluator (src/evaluator.rs:50-144);
+  ``Evaluator.eval_metrics`` -> Population::eval_metrics (src/population.rs:63-71)
 """
 from __future__ import annotations
 
@@ -22,8 +24,8 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 from . import _lib
-from ._lib import (GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms, ga_default_cfg, ga_draw,
-                   make_frames, ptr)
+from ._lib import (DOCK_METRICS_DTYPE, GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms,
+                   ga_default_cfg, ga_draw, make_frames, pack_names, ptr)
 from .pdb import Molecule, combine_molecules, position_ligand, read_pdb, read_pdb_text
 
 __all__ = [
@@ -31,6 +33,7 @@ __all__ = [
     "ClusterResult", "vdw_energy", "elec_energy", "desolv_energy", "air_energy", "satisfaction_ratio",
     "cluster_sets", "make_frames", "Molecule", "read_pdb", "read_pdb_text", "position_ligand",
     "combine_molecules", "default_context", "ga_default_cfg", "ga_draw", "run_ga", "GaResult", "Server",
+    "Evaluator", "Metrics",
 ]
 
 
@@ -152,6 +155,69 @@ class Complex:
         self.ctx.check(self.lib.gd_cluster(self.h, ptr(g), n, C.byref(cfg), C.byref(k), ptr(centers), ptr(sizes),
                                            ptr(members)))
         return _results(k.value, centers, sizes, members)
+
+
+@dataclass
+class Metrics:
+    """src/evaluator.rs:29-47"""
+    rmsd: float
+    irmsd: float
+    fnat: float
+    dockq: float
+
+    def rank(self) -> str:
+        return "High" if self.dockq >= 0.8 else "Medium" if self.dockq >= 0.5 else "Low"
+
+
+class Evaluator:
+    """DockQ, L-RMSD, i-RMSD and Fnat of poses of a complex's ligand against a
+    reference ligand structure (gd_evaluator): Evaluator::new(receptor,
+    reference) with the receptor of ``complex``."""
+
+    def __init__(self, complex: Complex, reference: Molecule):
+        self.cx, self.ctx, self.lib = complex, complex.ctx, complex.lib
+        self._ref = PackedAtoms(reference)
+        self._names = [pack_names(m.name) for m in (complex.receptor, complex.ligand, reference)]
+        h = C.c_void_p()
+        self.ctx.check(self.lib.gd_evaluator_create(complex.h, C.byref(self._ref.s), *[ptr(n) for n in self._names],
+                                                    C.byref(h)))
+        self.h = h
+
+    def eval_metrics(self, genes) -> np.ndarray:
+        """Metrics of n poses (genes n x 6) as a structured array with the
+        fields rmsd, irmsd, fnat, dockq."""
+        g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+        out = np.zeros(g.shape[0], dtype=DOCK_METRICS_DTYPE)
+        self.ctx.check(self.lib.gd_evaluate_poses(self.h, ptr(g), g.shape[0], ptr(out)))
+        return out
+
+    COUNT_NAMES = ("receptor_interface_residues", "reference_interface_residues", "native_contacts",
+                   "ligand_atoms_read", "lrmsd_pairs", "irmsd_pairs", "contact_pairs_tested")
+
+    def counts(self) -> dict:
+        c = np.zeros(len(self.COUNT_NAMES), dtype=np.int64)
+        self.ctx.check(self.lib.gd_evaluator_counts(self.h, ptr(c)))
+        return dict(zip(self.COUNT_NAMES, c.tolist()))
+
+    def eval_frames_device(self, d_frames: int, n: int, d_out: int, stream: Optional[int] = None):
+        """gd_evaluate_frames_device: device pointers of n pose frames and of
+        n metrics records; asynchronous on ``stream`` (a cudaStream_t)."""
+        self.ctx.check(self.lib.gd_evaluate_frames_device(self.h, d_frames, n, d_out, stream))
+
+    def calc_metrics(self, genes) -> Metrics:
+        m = self.eval_metrics(np.asarray(genes, dtype=np.float64).reshape(1, 6))[0]
+        return Metrics(*(float(m[k]) for k in DOCK_METRICS_DTYPE.names))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gd_evaluator_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _results(k, centers, sizes, members) -> List[ClusterResult]:

@@ -25,7 +25,8 @@ EXPORTS = (
     "gd_context_get_tuning", "gd_score_frames_device_noalloc", "gd_ga_default_cfg", "gd_ga_draw", "gd_ga_run",
     "gd_server_default_cfg", "gd_server_create", "gd_server_destroy", "gd_server_submit", "gd_server_step",
     "gd_server_start", "gd_server_stop", "gd_server_wait", "gd_server_result", "gd_server_release",
-    "gd_server_get_stats", "gd_autotune_f32",
+    "gd_server_get_stats", "gd_autotune_f32", "gd_evaluator_create", "gd_evaluator_destroy",
+    "gd_evaluate_poses", "gd_evaluate_frames_device", "gd_evaluator_counts",
 )
 # candidates of gd_autotune_f32, in its order: (GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT)
 AUTOTUNE_CANDIDATES = ((16 + 4, 1), (64 + 2, 1), (64 + 4, 1), (256 + 64 + 2, 1), (256 + 64 + 4, 1), (256 + 64 + 4, 2))
@@ -77,6 +78,19 @@ class GdServerStats(C.Structure):
 POSE_ENERGY_DTYPE = np.dtype([(k, np.float64) for k in
                               ("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")])
 POSE_FRAME_BYTES = 16 * 8
+DOCK_METRICS_DTYPE = np.dtype([(k, np.float64) for k in ("rmsd", "irmsd", "fnat", "dockq")])
+
+
+def pack_names(names) -> np.ndarray:
+    """Trimmed atom names packed little-endian into one uint32 each (byte k =
+    character k, zero-padded), as gd_evaluator_create takes them."""
+    out = np.zeros(len(names), dtype=np.uint32)
+    for i, n in enumerate(names):
+        b = n.strip().encode("ascii")
+        if len(b) > 4:
+            raise ValueError(f"atom name {n!r} is longer than 4 characters")
+        out[i] = int.from_bytes(b.ljust(4, b"\0"), "little")
+    return out
 
 _lib = None
 
@@ -135,6 +149,11 @@ def load(path: Path = LIB_PATH):
         "gd_server_release": ([vp, i64], C.c_int),
         "gd_server_get_stats": ([vp, C.POINTER(GdServerStats)], C.c_int),
         "gd_autotune_f32": ([vp, vp, i32, d, vp, vp, vp, C.POINTER(i32)], C.c_int),
+        "gd_evaluator_create": ([vp, C.POINTER(GdAtoms), vp, vp, vp, C.POINTER(vp)], C.c_int),
+        "gd_evaluator_destroy": ([vp], C.c_int),
+        "gd_evaluate_poses": ([vp, vp, i32, vp], C.c_int),
+        "gd_evaluate_frames_device": ([vp, vp, i32, vp, vp], C.c_int),
+        "gd_evaluator_counts": ([vp, vp], C.c_int),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)

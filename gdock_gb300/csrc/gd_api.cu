@@ -592,6 +592,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   cx->h_lelem.assign(lig->element, lig->element + lig->n);
   cx->h_rres.assign(rec->resseq, rec->resseq + rec->n);
   cx->h_lres.assign(lig->resseq, lig->resseq + lig->n);
+  cx->h_lig_slot = inv;
   *out = cx;
   return GD_OK;
 }

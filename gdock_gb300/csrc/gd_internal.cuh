@@ -146,6 +146,7 @@ struct gd_complex {
   std::vector<double> h_rx, h_ry, h_rz, h_lx, h_ly, h_lz;
   std::vector<uint8_t> h_rchain, h_lchain, h_relem, h_lelem;
   std::vector<int16_t> h_rres, h_lres;
+  std::vector<int> h_lig_slot;  // original ligand atom index -> slot position on the device
   void *cluster_cache = nullptr;  // gd::ClusterTopo*, built on first use
 };
 

@@ -13,6 +13,8 @@
  *   restraints::create_restraints_from_pairs src/restraints.rs:44-77 -> gd_complex_create
  *   clustering::calculate_contacts    src/clustering.rs:62-115  -> gd_pose_contacts
  *   clustering::cluster_structures    src/clustering.rs:265-293 -> gd_cluster
+ *   Evaluator::new / calc_metrics     src/evaluator.rs:50-144   -> gd_evaluator_create / gd_evaluate_poses
+ *   Population::eval_metrics          src/population.rs:63-71   -> gd_evaluate_poses
  *
  * Conventions: every call returns a gd_status; nothing throws or aborts
  * across the ABI.  The library copies all inputs; callers keep ownership of
@@ -208,6 +210,39 @@ gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cl
 gd_status gd_cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offsets, int32_t n,
                           const gd_cluster_cfg *cfg, int32_t *n_clusters, int32_t *centers,
                           int32_t *sizes, int32_t *members);
+
+/* ----------------------------------------------------------- DockQ --
+ * evaluator::Evaluator (src/evaluator.rs:50-186): quality of poses against
+ * a reference ligand structure.  Metrics as src/evaluator.rs:29-35. */
+typedef struct gd_dock_metrics { double rmsd, irmsd, fnat, dockq; } gd_dock_metrics;
+typedef struct gd_evaluator gd_evaluator;
+
+/* Evaluator::new(receptor, reference) (src/evaluator.rs:51-66) for the
+ * complex's receptor; the ligand of the complex is the moving structure.
+ * Atom names (trimmed, at most 4 characters) are packed little-endian into
+ * one uint32 per atom: byte k = character k, zero-padded.  Only the fields
+ * x, y, z, resseq and chain of `reference` are read.  The complex must
+ * outlive the evaluator. */
+gd_status gd_evaluator_create(gd_complex *cx, const gd_atoms *reference, const uint32_t *rec_names,
+                              const uint32_t *lig_names, const uint32_t *ref_names, gd_evaluator **out);
+gd_status gd_evaluator_destroy(gd_evaluator *ev);
+/* Sizes fixed at creation, into counts[GD_EVAL_COUNTS]: receptor interface
+ * residues, reference interface residues, native contacts, ligand atoms read
+ * per pose, L-RMSD pairs, i-RMSD pairs, native-identity (receptor, ligand)
+ * atom pairs tested per pose. */
+#define GD_EVAL_COUNTS 7
+gd_status gd_evaluator_counts(const gd_evaluator *ev, int64_t *counts);
+
+/* Population::eval_metrics (src/population.rs:63-71): calc_metrics of the
+ * ligand moved by each of n gene vectors (6 doubles each), FP64 on the GPU;
+ * out[n].  Contact decisions and fnat are exact; rmsd and irmsd differ from
+ * the reference's sequential sums only by summation order. */
+gd_status gd_evaluate_poses(gd_evaluator *ev, const double *genes, int32_t n, gd_dock_metrics *out);
+/* gd_evaluate_poses on device-resident frames (gd_make_frames layout) into
+ * device-resident metrics, asynchronously on `stream` (NULL = the context's
+ * stream).  Errors of the device run are reported by gd_sync. */
+gd_status gd_evaluate_frames_device(gd_evaluator *ev, const gd_pose_frame *d_frames, int32_t n,
+                                    gd_dock_metrics *d_out, void *stream);
 
 /* ----------------------------------------------------------------- GA --
  * gdock's generation loop (src/commands/run.rs:381-531: evaluate, track the

@@ -261,3 +261,101 @@ def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None):
         genes, _ = evolve(genes, f, draws, gen, cfg.elitism, cfg.tournament_size, cfg.crossover_rate,
                           cfg.mutation_rate, cfg.max_displacement)
         gen += 1
+
+
+# -- evaluator::Evaluator (src/evaluator.rs), restated on numpy ---------------
+
+def _dist(ax, ay, az, bx, by, bz):
+    """Atom::distance_to, sqrt((dx*dx + dy*dy) + dz*dz) (src/structure.rs:178-183)."""
+    dx, dy, dz = ax - bx, ay - by, az - bz
+    return np.sqrt(dx * dx + dy * dy + dz * dz)
+
+
+def _seq_sum(v) -> float:
+    """Left-to-right sum, as Iterator::sum (builtin sum() is compensated)."""
+    s = 0.0
+    for x in np.asarray(v, dtype=np.float64).tolist():
+        s += x
+    return s
+
+
+def _atoms(mol, x=None, y=None, z=None):
+    return (np.asarray(mol.x if x is None else x, np.float64), np.asarray(mol.y if y is None else y, np.float64),
+            np.asarray(mol.z if z is None else z, np.float64), np.asarray(mol.resseq).astype(np.int64),
+            list(mol.chainid), [n.strip() for n in mol.name])
+
+
+def _contacts(a, b):
+    """calculate_contacts (src/evaluator.rs:145-168): identities of the atom
+    pairs at <= 5 A, receptor-major order, duplicates kept."""
+    d = _dist(a[0][:, None], a[1][:, None], a[2][:, None], b[0][None, :], b[1][None, :], b[2][None, :])
+    ii, jj = np.nonzero(d <= 5.0)
+    return [(a[4][i], int(a[3][i]), a[5][i], b[4][j], int(b[3][j]), b[5][j]) for i, j in zip(ii.tolist(), jj.tolist())]
+
+
+def _filter(m, keep):
+    """structure::filter_by_resseq_vec (src/structure.rs:319-327)."""
+    sel = np.array([int(r) in keep for r in m[3]], dtype=bool)
+    idx = np.nonzero(sel)[0].tolist()
+    return (m[0][sel], m[1][sel], m[2][sel], m[3][sel], [m[4][i] for i in idx], [m[5][i] for i in idx])
+
+
+class Evaluator:
+    """evaluator::Evaluator::new (src/evaluator.rs:50-66): interface residues
+    (calculate_interface, :170-186), interface atoms and native contacts."""
+
+    def __init__(self, rec, ref):
+        self.rec, self.ref = _atoms(rec), _atoms(ref)
+        r, f = self.rec, self.ref
+        d = _dist(r[0][:, None], r[1][:, None], r[2][:, None], f[0][None, :], f[1][None, :], f[2][None, :])
+        hit = d <= 5.0
+        self.interface = (set(r[3][hit.any(axis=1)].tolist()), set(f[3][hit.any(axis=0)].tolist()))
+        self.receptor_interface = _filter(r, self.interface[0])
+        self.reference_interface = _filter(f, self.interface[1])
+        self.native_contacts = _contacts(self.receptor_interface, self.reference_interface)
+        self._native_set = set(self.native_contacts)
+
+    def calc_rmsd(self, lig) -> float:
+        """src/evaluator.rs:86-103 (a sum of distances, not of squares)."""
+        n = len(self.ref[0])
+        if n == 0:
+            return 0.0
+        k = min(len(lig[0]), n)
+        d = _dist(lig[0][:k], lig[1][:k], lig[2][:k], self.ref[0][:k], self.ref[1][:k], self.ref[2][:k])
+        return float(np.sqrt(_seq_sum(d) / n))
+
+    def calc_irmsd(self, lig) -> float:
+        """src/evaluator.rs:105-124"""
+        t = _filter(lig, self.interface[1])
+        ri = self.reference_interface
+        n = len(ri[0])
+        if n == 0:
+            return 0.0
+        k = min(len(t[0]), n)
+        d = _dist(t[0][:k], t[1][:k], t[2][:k], ri[0][:k], ri[1][:k], ri[2][:k])
+        return float(np.sqrt(_seq_sum(d) / n))
+
+    def calc_fnat(self, lig) -> float:
+        """src/evaluator.rs:126-143"""
+        docked = _contacts(self.receptor_interface, _filter(lig, self.interface[1]))
+        common = sum(1 for c in docked if c in self._native_set)
+        if not self.native_contacts:
+            return 0.0
+        return common / len(self.native_contacts)
+
+    def calc_metrics(self, lig_mol, x=None, y=None, z=None):
+        """src/evaluator.rs:68-84: (rmsd, irmsd, fnat, dockq) of the ligand
+        (optionally with moved coordinates x, y, z)."""
+        lig = _atoms(lig_mol, x, y, z)
+        fnat, irmsd, rmsd = self.calc_fnat(lig), self.calc_irmsd(lig), self.calc_rmsd(lig)
+        a, b = irmsd / 1.5, rmsd / 8.5
+        dockq = (fnat + 1.0 / (1.0 + a * a) + 1.0 / (1.0 + b * b)) / 3.0
+        return rmsd, irmsd, fnat, dockq
+
+    def eval_metrics(self, lig_mol, genes) -> np.ndarray:
+        """Population::eval_metrics (src/population.rs:63-71): (n, 4) array."""
+        g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
+        out = np.zeros((g.shape[0], 4))
+        for i in range(g.shape[0]):
+            out[i] = self.calc_metrics(lig_mol, *apply_genes(lig_mol, g[i]))
+        return out

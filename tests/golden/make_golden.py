@@ -1,11 +1,12 @@
 """Generate the golden fixtures of tests/golden from gdock's own test data.
 
 Reads the reference's structures (data/2oob_A.pdb, data/2oob_B.pdb,
-data/1h590A_0A.pdb, data/1h590B_0A_poses.pdb under the reference checkout),
+data/1h590A_0A.pdb, data/1h590B_0A_poses.pdb, and data/2oob_B_ref.pdb, the
+reference ligand of the DockQ evaluator, under the reference checkout),
 parses them with gdock_gb300.pdb (gdock's reader and parameter assignment),
 and stores the parsed atom arrays together with the CPU oracle's outputs:
 energies of seeded poses and of the 100 MODELs of the `score` example,
-contacts and clusters.  The GPU tests compare against these files, so they
+contacts, clusters and the evaluator's metrics.  The GPU tests compare against these files, so they
 need neither the reference checkout nor the oracle at run time.
 
 Usage: python tests/golden/make_golden.py [/path/to/reference]
@@ -66,6 +67,16 @@ def main(ref: Path):
     d["cluster_sizes"] = np.array([len(m) for _, m in cl], np.int32)
     np.savez_compressed(HERE / "2oob.npz", **d)
 
+    # evaluator::Evaluator of the crystal ligand (chain B of data/2oob.pdb)
+    ref_lig = pdb.read_pdb(data / "2oob_B_ref.pdb")[0]
+    q = {}
+    pack("ref", ref_lig, q)
+    ev = oracle.Evaluator(rec, ref_lig)
+    q["genes"] = genes
+    q["metrics"] = ev.eval_metrics(lig, genes)
+    q["interface_sizes"] = np.array([len(ev.interface[0]), len(ev.interface[1]), len(ev.native_contacts)], np.int64)
+    np.savez_compressed(HERE / "2oob_dockq.npz", **q)
+
     rec2 = pdb.read_pdb(data / "1h590A_0A.pdb")[0]
     models = pdb.read_pdb(data / "1h590B_0A_poses.pdb")
     e = {}
@@ -74,7 +85,7 @@ def main(ref: Path):
     e["models_xyz"] = np.stack([m.xyz() for m in models])
     e["energies"] = oracle.score_models(rec2, models[0], [], e["models_xyz"])
     np.savez_compressed(HERE / "1h590_score.npz", **e)
-    print("wrote", HERE / "2oob.npz", HERE / "1h590_score.npz")
+    print("wrote", HERE / "2oob.npz", HERE / "2oob_dockq.npz", HERE / "1h590_score.npz")
 
 
 if __name__ == "__main__":

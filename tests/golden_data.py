@@ -18,6 +18,7 @@ class GoldenMol:
         self.chain_code, self.element_class = g("chain").astype(np.uint8), g("element").astype(np.uint8)
         self.is_ca = g("is_ca").astype(np.uint8)
         self.name = list(g("name"))
+        self.chainid = [chr(c) for c in self.chain_code.tolist()]
 
     def __len__(self):
         return int(self.x.shape[0])

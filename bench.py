@@ -262,9 +262,10 @@ def autotune_ga(gd, _lib, ctx, cxs, pop, split_mode, generations=3):
 
 def run_c1(args):
     """The small plain-method config: receptor 50 x ligand 76 residues, 6
-    restraints, GA pop 150 x 50 generations in FP64, then FCC clustering of the
-    final population; one dock per step.  The CPU leg runs the oracle's GA on
-    the same draws (gdock's own loop, threaded per pose) on the host cores."""
+    restraints, GA pop 150 x 50 generations in FP64 with the Hall of Fame, then
+    FCC clustering of the Hall of Fame (src/commands/run.rs:666-686); one dock
+    per step.  The CPU leg runs the oracle's GA and Hall of Fame on the same
+    draws (gdock's own loop, threaded per pose) on the host cores."""
     import gdock_gb300 as gd
     from gdock_gb300 import _lib, position_ligand, synth
     ctx = gd.Context(0)
@@ -275,17 +276,17 @@ def run_c1(args):
     G, pop = 50, 150
     cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=G, early_stopping=0, seed=7)
     for _ in range(max(1, args.warmup)):
-        gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
+        gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx, hall_of_fame=True)
     times, times32 = [], []
     res = None
     for _ in range(max(1, args.steps)):
         t0 = time.perf_counter()
-        res = gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
-        clusters = cx.cluster(res.genes[0])
+        res = gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx, hall_of_fame=True)
+        clusters = cx.cluster(res.hall_of_fame[0]["genes"])
         times.append(time.perf_counter() - t0)
         t0 = time.perf_counter()
-        r32 = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
-        cx.cluster(r32.genes[0])
+        r32 = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
+        cx.cluster(r32.hall_of_fame[0]["genes"])
         times32.append(time.perf_counter() - t0)
     t, t32 = float(np.median(times)), float(np.median(times32))
     # CPU leg: the oracle's generation loop on the same draws, all host cores
@@ -293,22 +294,27 @@ def run_c1(args):
     draws = _lib.ga_draw(cfg, cfg.seed, G)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    g_cpu, e_cpu, _, _ = orc.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, nthreads=threads)
-    orc.cluster([orc.pose_contacts(c.receptor, lig, g) for g in g_cpu])
+    hof = orc.HallOfFame()
+    g_cpu, e_cpu, _, _ = orc.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, nthreads=threads, hof=hof)
+    orc.cluster([orc.pose_contacts(c.receptor, lig, np.array(g)) for g, _, _ in hof.entries])
     t_cpu = time.perf_counter() - t0
     same = bool(np.array_equal(g_cpu, res.genes[0]))
+    same_hof = bool(np.array_equal(np.array([g for g, _, _ in hof.entries]), res.hall_of_fame[0]["genes"]))
     line = {"metric": "docks/s (plain FP64 GA, pop 150 x 50 generations, then FCC clustering)",
             "value": 1.0 / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": max(1, args.warmup),
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "synthetic receptor 50 residues x ligand 76 residues, 6 restraints, GA pop 150 "
-                                   "x 50 generations (fixed), FCC clustering of the final population",
+                                   "x 50 generations (fixed) with the Hall of Fame (500 entries, top 10 per "
+                                   "generation), FCC clustering of the Hall of Fame",
                        "receptor_atoms": len(c.receptor), "ligand_atoms": len(lig)},
-            "clusters": len(clusters),
+            "clusters": len(clusters), "hall_of_fame_entries": int(len(res.hall_of_fame[0])),
+            "hall_of_fame_equals_oracle": same_hof,
             "f32_graph_docks_per_s": 1.0 / t32,
             "final_population_equals_oracle": same,
             "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "docks/s", "cores": threads, "kind": "port",
-                             "sample": "one full dock: the oracle's GA on the same draws, then its FCC clustering"}}
+                             "sample": "one full dock: the oracle's GA and Hall of Fame on the same draws, then "
+                                       "its FCC clustering"}}
     print(json.dumps(line), flush=True)
 
 
@@ -326,14 +332,14 @@ def run_c3(args):
     times = []
     for _ in range(max(1, args.steps)):
         t0 = time.perf_counter()
-        res = gd.run_ga(cxs, cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
+        res = gd.run_ga(cxs, cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
         times.append(time.perf_counter() - t0)
     t = float(np.median(times))
     evals = len(jobs) * pop * (G + 1)
     pairs = sum(len(r) * len(l) for r, l, _ in jobs) * pop * (G + 1)
-    # FCC clustering of each final population
+    # FCC clustering of each job's Hall of Fame (src/commands/run.rs:666-686)
     t0 = time.perf_counter()
-    n_clusters = [len(cx.cluster(res.genes[j])) for j, cx in enumerate(cxs)]
+    n_clusters = [len(cx.cluster(res.hall_of_fame[j]["genes"])) for j, cx in enumerate(cxs)]
     t_fcc = time.perf_counter() - t0
     # plain FP64 GA on a sample of 4 jobs x 2 generations, per pair
     dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, jobs[:4], pop, 2)
@@ -342,11 +348,13 @@ def run_c3(args):
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "64 synthetic complexes, receptor 100-800 residues, ligand 50-300 residues "
-                                   "(log-uniform), 6-20 restraints; GA pop 150 x 50 generations",
+                                   "(log-uniform), 6-20 restraints; GA pop 150 x 50 generations with the Hall "
+                                   "of Fame, then FCC clustering of each Hall of Fame",
                        "receptor_atoms": [min(len(r) for r, _, _ in jobs), max(len(r) for r, _, _ in jobs)],
                        "ligand_atoms": [min(len(l) for _, l, _ in jobs), max(len(l) for _, l, _ in jobs)]},
             "poses_per_s": evals / t, "pair_evals_per_s": pairs / t,
-            "fcc_clustering": {"seconds_for_64_populations": t_fcc, "clusters_found": int(sum(n_clusters))},
+            "fcc_clustering": {"seconds_for_64_halls_of_fame": t_fcc, "clusters_found": int(sum(n_clusters)),
+                               "hall_of_fame_entries": int(sum(len(h) for h in res.hall_of_fame))},
             "autotune": tuned,
             "plain_fp64_pair_evals_per_s": pairs64 / dt64,
             "f32_batched_over_plain_f64": (pairs / t) / (pairs64 / dt64)}

@@ -24,7 +24,7 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 from . import _lib
-from ._lib import (DOCK_METRICS_DTYPE, GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms,
+from ._lib import (DOCK_METRICS_DTYPE, HOF_ENTRY_DTYPE, GD_PREC_F32, GD_PREC_F64, Context, GdError, POSE_ENERGY_DTYPE, PackedAtoms,
                    ga_default_cfg, ga_draw, make_frames, pack_names, ptr)
 from .pdb import Molecule, combine_molecules, position_ligand, read_pdb, read_pdb_text
 
@@ -285,11 +285,13 @@ class GaResult:
     energies: np.ndarray       # (jobs, pop) structured energies of the final populations
     generations: np.ndarray    # (jobs,) generations evolved
     history: np.ndarray        # (jobs, max_generations) best fitness per generation
+    hall_of_fame: Optional[List[np.ndarray]] = None  # per job, HOF_ENTRY_DTYPE records in the reference's order
 
 
 def run_ga(complexes: Sequence[Complex], cfg=None, precision=GD_PREC_F32, use_graph: bool = True,
-           ctx: Optional[Context] = None) -> GaResult:
-    """gdock's GA loop (src/commands/run.rs:381-531) for many jobs on the GPU."""
+           ctx: Optional[Context] = None, hall_of_fame: bool = False) -> GaResult:
+    """gdock's GA loop (src/commands/run.rs:381-531) for many jobs on the GPU;
+    with ``hall_of_fame`` also each job's HallOfFame (src/commands/run.rs:77-213)."""
     ctx = ctx or complexes[0].ctx
     cfg = cfg or ga_default_cfg()
     J, n, G = len(complexes), cfg.pop_size, cfg.max_generations
@@ -298,9 +300,13 @@ def run_ga(complexes: Sequence[Complex], cfg=None, precision=GD_PREC_F32, use_gr
     energies = np.zeros((J, n), dtype=POSE_ENERGY_DTYPE)
     gens = np.zeros(J, np.int32)
     hist = np.zeros((J, max(G, 1)))
+    hof = np.zeros((J, max(cfg.hof_max_size, 1)), dtype=HOF_ENTRY_DTYPE) if hall_of_fame else None
+    hof_n = np.zeros(J, np.int32) if hall_of_fame else None
     ctx.check(ctx.lib.gd_ga_run(ctx.h, C.cast(handles, C.c_void_p), J, C.byref(cfg), _prec(precision),
-                                1 if use_graph else 0, ptr(genes), ptr(energies), ptr(gens), ptr(hist)))
-    return GaResult(genes, energies, gens, hist[:, :G])
+                                1 if use_graph else 0, ptr(genes), ptr(energies), ptr(gens), ptr(hist),
+                                ptr(hof) if hall_of_fame else None, ptr(hof_n) if hall_of_fame else None))
+    hl = [hof[j, :hof_n[j]].copy() for j in range(J)] if hall_of_fame else None
+    return GaResult(genes, energies, gens, hist[:, :G], hl)
 
 
 class Server:

@@ -57,7 +57,8 @@ class GdGaCfg(C.Structure):
                 ("crossover_rate", C.c_double), ("mutation_rate", C.c_double), ("max_displacement", C.c_double),
                 ("rot_sigma", C.c_double), ("trans_sigma", C.c_double), ("max_generations", C.c_int32),
                 ("early_stopping", C.c_int32), ("convergence_threshold", C.c_double),
-                ("convergence_window", C.c_int32), ("seed", C.c_uint64)]
+                ("convergence_window", C.c_int32), ("seed", C.c_uint64), ("hof_max_size", C.c_int32),
+                ("hof_top_k", C.c_int32)]
 
 
 class GdServerCfg(C.Structure):
@@ -78,6 +79,8 @@ class GdServerStats(C.Structure):
 POSE_ENERGY_DTYPE = np.dtype([(k, np.float64) for k in
                               ("fitness", "vdw", "elec", "desolv", "air", "restraint_penalty")])
 POSE_FRAME_BYTES = 16 * 8
+HOF_ENTRY_DTYPE = np.dtype([("genes", np.float64, (6,)), ("fitness", np.float64), ("generation", np.int32),
+                            ("pad", np.int32)])
 DOCK_METRICS_DTYPE = np.dtype([(k, np.float64) for k in ("rmsd", "irmsd", "fnat", "dockq")])
 
 
@@ -135,7 +138,7 @@ def load(path: Path = LIB_PATH):
         "gd_score_frames_device_noalloc": ([vp, vp, i32, d, vp, vp], C.c_int),
         "gd_ga_default_cfg": ([C.POINTER(GdGaCfg)], C.c_int),
         "gd_ga_draw": ([C.POINTER(GdGaCfg), C.c_uint64, i32, vp, vp, vp, vp, vp, vp], C.c_int),
-        "gd_ga_run": ([vp, vp, i32, C.POINTER(GdGaCfg), C.c_int, i32, vp, vp, vp, vp], C.c_int),
+        "gd_ga_run": ([vp, vp, i32, C.POINTER(GdGaCfg), C.c_int, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "gd_server_default_cfg": ([C.POINTER(GdServerCfg)], C.c_int),
         "gd_server_create": ([vp, C.POINTER(GdServerCfg), C.POINTER(vp)], C.c_int),
         "gd_server_destroy": ([vp], C.c_int),

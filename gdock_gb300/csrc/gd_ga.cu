@@ -137,6 +137,7 @@ struct GaStepParams {
   double *history;            // [jobs][max_gen] best fitness per generation
   const int *tour, *perm;     // [jobs][max_gen][...]
   const double *cross_u, *mut_u, *mut_z;
+  gd_hof_entry *hof, *hof_tmp;  // [jobs][hof_max_size + 1]; null = no Hall of Fame
   gd_ga_cfg cfg;
 };
 
@@ -144,8 +145,90 @@ struct GaStepParams {
 // sort does not define; it never arises for finite inputs)
 __device__ __forceinline__ double key_of(double f) { return f != f ? INFINITY : f; }
 
+// HallOfFame::genes_are_similar (src/commands/run.rs:140-160) with
+// angular_difference (:162-171): every angle within 0.2 rad (with the wrap
+// at 2 pi) and every displacement within 2 A.
+__device__ __forceinline__ bool hof_similar(const double *a, const double *b) {
+  const double pi = 3.141592653589793, two_pi = 6.283185307179586;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double d = fabs(__dsub_rn(a[i], b[i]));
+    if (d > pi) d = __dsub_rn(two_pi, d);
+    if (d > 0.2) return false;
+  }
+#pragma unroll
+  for (int i = 3; i < 6; ++i)
+    if (fabs(__dsub_rn(a[i], b[i])) > 2.0) return false;
+  return true;
+}
+
+// HallOfFame::add_from_population (src/commands/run.rs:193-213) for one job,
+// run by one warp: the population in stable ascending fitness order (order),
+// try_add (:101-127) until top_k entries went in; each add over capacity
+// prunes (:174-179): a stable sort by fitness, then truncation.  Once a
+// prune has sorted the entries, the next prune only moves the new last
+// entry behind the entries of equal or lower fitness, which is what the
+// stable sort does to a sorted list with one entry appended.
+__device__ void hof_add(const GaStepParams &P, GaJobState &st, int job, int gen, const double *G, const double *f,
+                        const int *order) {
+  const gd_ga_cfg &c = P.cfg;
+  const int lane = threadIdx.x & 31, cap = c.hof_max_size, n = c.pop_size;
+  gd_hof_entry *H = P.hof + static_cast<size_t>(job) * (cap + 1);
+  gd_hof_entry *T = P.hof_tmp + static_cast<size_t>(job) * (cap + 1);
+  int cnt = st.hof_n, sorted = st.hof_sorted, added = 0;
+  for (int r = 0; r < n && added < c.hof_top_k; ++r) {
+    const int k = order[r];
+    double g[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) g[i] = G[6 * k + i];
+    bool sim = false;
+    for (int e = lane; e < cnt && !sim; e += 32) sim = hof_similar(g, H[e].genes);
+    if (__any_sync(kFull, sim)) continue;
+    if (lane == 0) {
+      gd_hof_entry &x = H[cnt];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) x.genes[i] = g[i];
+      x.fitness = f[k];
+      x.generation = gen;
+      x.pad = 0;
+    }
+    ++cnt;
+    ++added;
+    __syncwarp();
+    if (cnt > cap) {
+      if (sorted) {
+        const double fn = key_of(H[cnt - 1].fitness);
+        int pos = 0;  // entries before the new one: fitness <= its fitness
+        for (int e = lane; e < cnt - 1; e += 32) pos += key_of(H[e].fitness) <= fn;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pos += __shfl_xor_sync(kFull, pos, o);
+        for (int e = lane; e < cnt; e += 32) T[e < pos ? e : (e == cnt - 1 ? pos : e + 1)] = H[e];
+      } else {
+        for (int e = lane; e < cnt; e += 32) {
+          const double fe = key_of(H[e].fitness);
+          int rk = 0;
+          for (int q = 0; q < cnt; ++q) {
+            const double fq = key_of(H[q].fitness);
+            rk += (fq < fe) || (fq == fe && q < e);
+          }
+          T[rk] = H[e];
+        }
+      }
+      __syncwarp();
+      cnt = cap;
+      for (int e = lane; e < cnt; e += 32) H[e] = T[e];
+      sorted = 1;
+      __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    st.hof_n = cnt;
+    st.hof_sorted = sorted;
+  }
+}
+
 // One CTA per job: the reference loop's bookkeeping for the fitness just
-// computed, then evolve.
+// computed (with the Hall of Fame), then evolve.
 __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gd_ga_cfg &c = P.cfg;
@@ -154,9 +237,10 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   double *f = reinterpret_cast<double *>(smem);   // [n] fitness of the evaluated population
   double *f2 = f + n;                              // [m] fitness carried by the offspring
   int *sel = reinterpret_cast<int *>(f2 + m);      // [n] tournament winners
-  int *elite = sel + n;                            // [elitism]
+  int *elite = sel + n;                            // [64] elites
+  int *order = elite + 64;                         // [n] stable ascending order (Hall of Fame only)
   __shared__ double s_eg[64 * 6];                  // elites' genes, staged before the population is overwritten
-  __shared__ int s_evolve;
+  __shared__ int s_evolve, s_hof, s_gen;
   GaJobState &st = P.state[job];
   if (st.stop) return;
   const gd_pose_energy *E = P.energies + static_cast<size_t>(job) * n;
@@ -164,11 +248,15 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   __syncthreads();
   if (tid == 0) {
     const int gen = st.gen;
+    s_gen = gen;
     if (gen >= c.max_generations) {
       // the evaluation just done was of the final population: stop here
       st.stop = 2;
       s_evolve = 0;
+      s_hof = 0;
     } else {
+      // Hall of Fame of every evaluation inside the loop (src/commands/run.rs:385)
+      s_hof = P.hof != nullptr && c.hof_max_size > 0 && c.hof_top_k > 0;
       // best of this generation, first minimum (src/commands/run.rs:391-398)
       int bi = 0;
       for (int k = 1; k < n; ++k)
@@ -191,18 +279,11 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
     }
   }
   __syncthreads();
-  if (!s_evolve) return;
-  const int gen = st.gen - 1;  // draws of the generation being evolved
-  const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;
-  const int *tour = P.tour + jg * c.tournament_size * n;
-  const int *perm = P.perm + jg * n;
-  const double *cu = P.cross_u + jg * 6 * (n / 2);
-  const double *mu = P.mut_u + jg * 6 * m;
-  const double *mz = P.mut_z + jg * 6 * m;
+  if (!s_evolve && !s_hof) return;
   double *G = P.genes + static_cast<size_t>(job) * n * 6;
-  double *T = P.genes_tmp + static_cast<size_t>(job) * m * 6;
   const int ne = c.elitism < n ? c.elitism : n;
-  // elites: stable ascending order, first ne (src/population.rs:76-82)
+  // stable ascending order of the evaluated population: the elites
+  // (src/population.rs:76-82) and the Hall of Fame's candidates
   for (int k = tid; k < n; k += nt) {
     const double fk = key_of(f[k]);
     int r = 0;
@@ -211,7 +292,19 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
       r += (fq < fk) || (fq == fk && q < k);
     }
     if (r < ne) elite[r] = k;
+    if (s_hof) order[r] = k;
   }
+  __syncthreads();
+  if (s_hof && tid < 32) hof_add(P, st, job, s_gen, G, f, order);
+  if (!s_evolve) return;
+  const int gen = st.gen - 1;  // draws of the generation being evolved
+  const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;
+  const int *tour = P.tour + jg * c.tournament_size * n;
+  const int *perm = P.perm + jg * n;
+  const double *cu = P.cross_u + jg * 6 * (n / 2);
+  const double *mu = P.mut_u + jg * 6 * m;
+  const double *mz = P.mut_z + jg * 6 * m;
+  double *T = P.genes_tmp + static_cast<size_t>(job) * m * 6;
   // tournament: first minimum of the draws (src/population.rs:136-156)
   for (int k = tid; k < n; k += nt) {
     int best = tour[c.tournament_size * k];
@@ -278,7 +371,8 @@ extern "C" {
 gd_status gd_ga_default_cfg(gd_ga_cfg *cfg) {
   if (!cfg) return GD_ERR_INVALID_ARG;
   // src/constants.rs:2-16 and src/chromosome.rs:64-71
-  *cfg = gd_ga_cfg{150, 5, 3, 0.6, 0.1, 50.0, 0.174, 1.0, 250, 1, 0.001, 10, 42};
+  // src/commands/run.rs:56-57 (Hall of Fame)
+  *cfg = gd_ga_cfg{150, 5, 3, 0.6, 0.1, 50.0, 0.174, 1.0, 250, 1, 0.001, 10, 42, 500, 10};
   return GD_OK;
 }
 
@@ -313,6 +407,7 @@ struct GaRun {
   gd_pose_frame *frames = nullptr;
   gd_pose_energy *energies = nullptr;
   GaJobState *state = nullptr;
+  gd_hof_entry *hof = nullptr, *hof_tmp = nullptr;
   std::vector<std::pair<void *, size_t>> allocs;
 };
 
@@ -331,7 +426,8 @@ static void ga_release(gd_context *ctx, GaRun &R) {
 
 extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs, const gd_ga_cfg *cfg,
                                gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
-                               int32_t *out_generations, double *out_history) {
+                               int32_t *out_generations, double *out_history, gd_hof_entry *out_hof,
+                               int32_t *out_hof_count) {
   using namespace gd;
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (!complexes || jobs <= 0 || !cfg || !out_genes || !out_energies)
@@ -341,6 +437,10 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
       c.elitism > c.pop_size || c.max_generations < 0 || c.pop_size > 8192)
     return fail(ctx, GD_ERR_INVALID_ARG, "GA config: even pop_size in [2, 8192], elitism <= 64");
   if (prec != GD_PREC_F32 && prec != GD_PREC_F64) return fail(ctx, GD_ERR_INVALID_ARG, "bad precision");
+  const bool hof = out_hof || out_hof_count;
+  if (hof && (!out_hof || !out_hof_count || c.hof_max_size < 0 || c.hof_max_size > (1 << 20) || c.hof_top_k < 0))
+    return fail(ctx, GD_ERR_INVALID_ARG, "Hall of Fame: out_hof and out_hof_count together, hof_max_size in [0, 2^20]");
+  const int hcap = hof ? c.hof_max_size : 0;
   for (int j = 0; j < jobs; ++j)
     if (!complexes[j] || complexes[j]->ctx != ctx) return fail(ctx, GD_ERR_INVALID_ARG, "complex of another context");
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -401,6 +501,13 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
   R.frames = static_cast<gd_pose_frame *>(p);
   if ((s = ga_alloc(ctx, R, sizeof(gd_pose_energy) * jn, &p)) != GD_OK) goto done;
   R.energies = static_cast<gd_pose_energy *>(p);
+  if (hcap > 0) {
+    const size_t hb = sizeof(gd_hof_entry) * static_cast<size_t>(jobs) * (hcap + 1);
+    if ((s = ga_alloc(ctx, R, hb, &p)) != GD_OK) goto done;
+    R.hof = static_cast<gd_hof_entry *>(p);
+    if ((s = ga_alloc(ctx, R, hb, &p)) != GD_OK) goto done;
+    R.hof_tmp = static_cast<gd_hof_entry *>(p);
+  }
   {
     // one scoring descriptor per job; poses outside [-M, M] never occur
     std::vector<ScoreParams> descs;
@@ -429,8 +536,11 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     P.cross_u = R.cross_u;
     P.mut_u = R.mut_u;
     P.mut_z = R.mut_z;
+    P.hof = R.hof;
+    P.hof_tmp = R.hof_tmp;
     P.cfg = c;
-    const size_t ga_smem = sizeof(double) * (n + m) + sizeof(int) * (n + 64);
+    P.cfg.hof_max_size = hcap;
+    const size_t ga_smem = sizeof(double) * (n + m) + sizeof(int) * (2 * n + 64);
     cudaStream_t st = ctx->stream;
     auto generation = [&]() -> gd_status {
       const int total = static_cast<int>(jn);
@@ -497,6 +607,17 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     }
     if (out_generations)
       for (int j = 0; j < jobs; ++j) out_generations[j] = h_state[j].gen;
+    if (hof) {
+      for (int j = 0; j < jobs; ++j) {
+        out_hof_count[j] = hcap > 0 ? h_state[j].hof_n : 0;
+        if (out_hof_count[j] > 0 &&
+            (e = cudaMemcpy(out_hof + static_cast<size_t>(j) * hcap, R.hof + static_cast<size_t>(j) * (hcap + 1),
+                            sizeof(gd_hof_entry) * out_hof_count[j], cudaMemcpyDeviceToHost)) != cudaSuccess) {
+          s = cuda_fail(ctx, e, "Hall of Fame results");
+          goto done;
+        }
+      }
+    }
   }
 done:
   ga_release(ctx, R);
@@ -811,7 +932,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
   P.mut_u = R.mut_u;
   P.mut_z = R.mut_z;
   P.cfg = c;
-  const size_t ga_smem = sizeof(double) * 2 * n + sizeof(int) * (n + 64);
+  const size_t ga_smem = sizeof(double) * 2 * n + sizeof(int) * (2 * n + 64);
   if (ga_smem > 48 * 1024)
     cudaFuncSetAttribute(k_ga_step, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ga_smem));
   k_ga_step<<<J, 256, ga_smem, st>>>(P);

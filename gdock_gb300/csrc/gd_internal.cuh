@@ -34,8 +34,9 @@ enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };
 // Per-job state of the device GA (the reference loop's counters,
 // src/commands/run.rs:371-425).  stop: 0 running, 1 converged, 2 done.
 struct GaJobState {
-  int gen, stop, stagnant, pad;
+  int gen, stop, stagnant, hof_n;  // hof_n: Hall of Fame entries held
   double last_best;
+  int hof_sorted, pad;             // 1 once a prune has sorted the Hall of Fame
 };
 
 // Per-pair parameters of one type pair, FP32 form, for the soft-core LJ

@@ -264,7 +264,17 @@ typedef struct gd_ga_cfg {
   double convergence_threshold; /* CONVERGENCE_THRESHOLD (0.001) */
   int32_t convergence_window;   /* CONVERGENCE_WINDOW (10) */
   uint64_t seed;                /* job j uses seed + j */
+  int32_t hof_max_size;         /* HALL_OF_FAME_MAX_SIZE (500); 0 = no Hall of Fame */
+  int32_t hof_top_k;            /* HALL_OF_FAME_TOP_K (10) */
 } gd_ga_cfg;
+
+/* One Hall of Fame entry (src/commands/run.rs:64-73). */
+typedef struct gd_hof_entry {
+  double genes[6];
+  double fitness;
+  int32_t generation;
+  int32_t pad;
+} gd_hof_entry;
 
 /* The reference's constants (src/constants.rs:2-16, src/chromosome.rs:64-71). */
 gd_status gd_ga_default_cfg(gd_ga_cfg *cfg);
@@ -277,10 +287,16 @@ gd_status gd_ga_draw(const gd_ga_cfg *cfg, uint64_t seed, int32_t generations, d
  * use_graph (FP32 form) one generation is a captured CUDA graph replayed.
  * Outputs: final populations (jobs x pop x 6), their energies
  * (jobs x pop), generations evolved per job, best fitness per generation
- * (jobs x max_generations, may be NULL). */
+ * (jobs x max_generations, may be NULL), and each job's Hall of Fame
+ * (HallOfFame::add_from_population after every evaluation inside the
+ * generation loop, src/commands/run.rs:99-213,385; kept on the device):
+ * out_hof receives jobs x hof_max_size entries in the reference's order,
+ * out_hof_count the entries per job.  Both NULL (or hof_max_size 0) = no
+ * Hall of Fame. */
 gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs, const gd_ga_cfg *cfg,
                     gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
-                    int32_t *out_generations, double *out_history);
+                    int32_t *out_generations, double *out_history, gd_hof_entry *out_hof,
+                    int32_t *out_hof_count);
 
 /* ------------------------------------------------------------- serving --
  * A request loop for docking jobs (gdock's `run` GA per job): jobs are

@@ -7,6 +7,7 @@ imports it.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 from pathlib import Path
@@ -234,9 +235,54 @@ def evolve(genes, fitness, draws, g, elitism=5, tournament=3, crossover_rate=0.6
     return go, fo
 
 
-def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None):
+class HallOfFame:
+    """HallOfFame (src/commands/run.rs:75-215) restated: entries are
+    (genes tuple, fitness, generation) in the reference's order."""
+
+    def __init__(self, max_size=500, top_k=10, rot=0.2, trans=2.0):
+        self.entries, self.max_size, self.top_k, self.rot, self.trans = [], max_size, top_k, rot, trans
+
+    @staticmethod
+    def angular_difference(a, b):  # src/commands/run.rs:162-171
+        d = abs(a - b)
+        return 2.0 * math.pi - d if d > math.pi else d
+
+    def genes_are_similar(self, a, b):  # src/commands/run.rs:140-160
+        for i in range(3):
+            if self.angular_difference(a[i], b[i]) > self.rot:
+                return False
+        for i in range(3, 6):
+            if abs(a[i] - b[i]) > self.trans:
+                return False
+        return True
+
+    def try_add(self, genes, fitness, generation):  # src/commands/run.rs:101-127
+        if len(genes) != 6:
+            return False
+        g = tuple(float(x) for x in genes)
+        if any(self.genes_are_similar(g, e[0]) for e in self.entries):
+            return False
+        self.entries.append((g, float(fitness), int(generation)))
+        if len(self.entries) > self.max_size:  # prune, :174-179 (a stable sort)
+            self.entries.sort(key=lambda e: e[1])
+            del self.entries[self.max_size:]
+        return True
+
+    def add_from_population(self, genes, fitness, generation):  # src/commands/run.rs:193-213
+        order = sorted(range(len(fitness)), key=lambda k: fitness[k])  # stable
+        added = 0
+        for k in order:
+            if added >= self.top_k:
+                break
+            if self.try_add(genes[k], fitness[k], generation):
+                added += 1
+
+
+def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, hof=None):
     """gdock's generation loop (src/commands/run.rs:381-531) on the CPU with
-    explicit draws: returns final genes, final energies, generations, history."""
+    explicit draws: returns final genes, final energies, generations, history;
+    ``hof`` (a HallOfFame) is fed after every evaluation inside the loop
+    (src/commands/run.rs:385)."""
     genes = draws["init"].copy()
     last_best, stagnant, history = None, 0, []
     gen = 0
@@ -245,6 +291,8 @@ def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None):
         if gen >= cfg.max_generations:
             return genes, e, gen, np.array(history)
         f = e[:, 0]
+        if hof is not None:
+            hof.add_from_population(genes, f, gen)
         best = f[int(np.argmin(f))]
         bi = 0
         for k in range(1, len(f)):

@@ -67,3 +67,53 @@ def test_batched_jobs_same_alone_and_in_the_mix():
         np.testing.assert_array_equal(alone.genes[0], mix.genes[j])
         assert alone.energies[0].tobytes() == mix.energies[j].tobytes()
         np.testing.assert_array_equal(alone.history[0], mix.history[j])
+
+
+def hof_list(recs):
+    return [(tuple(r["genes"].tolist()), float(r["fitness"]), int(r["generation"])) for r in recs]
+
+
+@pytest.mark.parametrize("early,cap,top_k", [(False, 500, 10), (True, 500, 10), (False, 7, 3), (False, 40, 10)])
+def test_ga_hall_of_fame_matches_oracle(oracle, early, cap, top_k):
+    # plain FP64: the device Hall of Fame equals the oracle's HallOfFame fed
+    # with the same populations, entry for entry and in order (small caps
+    # exercise the prune, src/commands/run.rs:174-179)
+    c, lig = setup_job(30, 36, 4, seed=79)
+    cfg = _lib.ga_default_cfg(pop_size=24, max_generations=14 if not early else 40, seed=6,
+                              early_stopping=1 if early else 0, convergence_window=3, convergence_threshold=0.01,
+                              hof_max_size=cap, hof_top_k=top_k)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs)
+    res = gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, hall_of_fame=True)
+    draws = _lib.ga_draw(cfg, cfg.seed, cfg.max_generations)
+    hof = oracle.HallOfFame(max_size=cap, top_k=top_k)
+    genes, _, gens, _ = oracle.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, hof=hof)
+    np.testing.assert_array_equal(res.genes[0], genes)
+    got = hof_list(res.hall_of_fame[0])
+    assert len(got) == len(hof.entries) <= cap
+    assert [(g, gen) for g, _, gen in got] == [(g, gen) for g, _, gen in hof.entries]
+    np.testing.assert_allclose([x[1] for x in got], [x[1] for x in hof.entries], rtol=1e-12)
+
+
+def test_ga_hall_of_fame_fp32_graph_invariants(oracle):
+    # FP32 graph form, several jobs: every job's entries are pairwise
+    # dissimilar, at most hof_max_size, each at most top_k per generation,
+    # and the mix equals each job alone
+    jobs = [setup_job(25, 20, 3, 111), setup_job(60, 45, 6, 112)]
+    ctx = gd.Context(0)
+    cxs = [gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx) for c, lig in jobs]
+    cfg = _lib.ga_default_cfg(pop_size=32, max_generations=12, seed=21, early_stopping=0, hof_max_size=30,
+                              hof_top_k=4)
+    mix = gd.run_ga(cxs, cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
+    sim = oracle.HallOfFame().genes_are_similar
+    for j, cx in enumerate(cxs):
+        h = hof_list(mix.hall_of_fame[j])
+        assert 0 < len(h) <= 30
+        for a in range(len(h)):
+            for b in range(a + 1, len(h)):
+                assert not sim(h[a][0], h[b][0])
+        per_gen = np.bincount([x[2] for x in h])
+        assert per_gen.max() <= 4
+        c1 = _lib.ga_default_cfg(pop_size=32, max_generations=12, seed=21 + j, early_stopping=0, hof_max_size=30,
+                                 hof_top_k=4)
+        alone = gd.run_ga([cx], c1, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
+        assert alone.hall_of_fame[0].tobytes() == mix.hall_of_fame[j].tobytes()

@@ -162,68 +162,177 @@ __device__ __forceinline__ bool hof_similar(const double *a, const double *b) {
   return true;
 }
 
+constexpr int kHofChunk = 32;    // candidates pre-checked per round (one per lane)
+constexpr int kHofNewMax = 32;   // entries a round may add before the pre-check is redone
+constexpr int kHofF32Max = 512;  // entries mirrored in FP32 for the pre-filter
+
+// FP32 pre-filter of hof_similar: true only where the exact FP64 test says
+// "not similar": some angle differs by more than 0.2 and less than
+// 2 pi - 0.2 (so also by more than 0.2 across the wrap), or some
+// displacement by more than 2, each by a margin (1e-4 + 1e-6 (|a| + |b|))
+// far above the FP32 rounding of both values and of their difference.
+__device__ __forceinline__ bool hof_far32(const float *a, const float *b) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float d = fabsf(a[i] - b[i]), mg = 1e-4f + 1e-6f * (fabsf(a[i]) + fabsf(b[i]));
+    if (d > 0.2f + mg && d < 6.0831853f - mg) return true;
+  }
+#pragma unroll
+  for (int i = 3; i < 6; ++i) {
+    const float d = fabsf(a[i] - b[i]), mg = 1e-4f + 1e-6f * (fabsf(a[i]) + fabsf(b[i]));
+    if (d > 2.0f + mg) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool genes_equal(const double *a, const double *b) {
+  return a[0] == b[0] && a[1] == b[1] && a[2] == b[2] && a[3] == b[3] && a[4] == b[4] && a[5] == b[5];
+}
+
 // HallOfFame::add_from_population (src/commands/run.rs:193-213) for one job,
-// run by one warp: the population in stable ascending fitness order (order),
-// try_add (:101-127) until top_k entries went in; each add over capacity
-// prunes (:174-179): a stable sort by fitness, then truncation.  Once a
-// prune has sorted the entries, the next prune only moves the new last
-// entry behind the entries of equal or lower fitness, which is what the
-// stable sort does to a sorted list with one entry appended.
-__device__ void hof_add(const GaStepParams &P, GaJobState &st, int job, int gen, const double *G, const double *f,
-                        const int *order) {
+// by the whole CTA: the population in stable ascending fitness order (order)
+// goes through try_add (:101-127) until top_k entries went in; each add over
+// capacity prunes (:174-179): a stable sort by fitness, then truncation.
+// Rounds of kHofChunk candidates: all threads first count, per candidate, the
+// similar entries held at the start of the round (the O(candidates x entries)
+// part: lane = candidate, warp = a slice of the entries, an FP32 pre-filter
+// before the exact FP64 test); one warp then walks the round in order.  A candidate goes in when no
+// entry of the round's start is left similar to it and it is not similar to
+// an entry added in this round.  The entry a prune drops is either one added
+// in this round (taken off that list) or one of the round's start (the later
+// candidates similar to it lose one count).  Once a prune has sorted the
+// entries, the next prune only moves the new last entry behind the entries of
+// equal or lower fitness, which is what the stable sort does to a sorted list
+// with one entry appended.
+__device__ void hof_update(const GaStepParams &P, GaJobState &st, int job, int gen, const double *G,
+                           const double *f, const int *order, int *s_csim, double *s_new, int *s_ctl, int *s_part,
+                           float *s_hf) {
   const gd_ga_cfg &c = P.cfg;
-  const int lane = threadIdx.x & 31, cap = c.hof_max_size, n = c.pop_size;
+  const int tid = threadIdx.x, lane = tid & 31, cap = c.hof_max_size, n = c.pop_size;
   gd_hof_entry *H = P.hof + static_cast<size_t>(job) * (cap + 1);
   gd_hof_entry *T = P.hof_tmp + static_cast<size_t>(job) * (cap + 1);
-  int cnt = st.hof_n, sorted = st.hof_sorted, added = 0;
-  for (int r = 0; r < n && added < c.hof_top_k; ++r) {
-    const int k = order[r];
-    double g[6];
+  if (tid == 0) {
+    s_ctl[0] = 0;  // first candidate of the round (rank)
+    s_ctl[1] = 0;  // entries added in this generation
+    s_ctl[2] = st.hof_n;
+    s_ctl[3] = st.hof_sorted;
+  }
+  __syncthreads();
+  for (;;) {
+    const int base = s_ctl[0], cnt0 = s_ctl[2];
+    if (base >= n || s_ctl[1] >= c.hof_top_k) break;
+    const int end = min(base + kHofChunk, n);
+    const int nw = blockDim.x >> 5, w = tid >> 5;
+    const bool f32 = cnt0 <= kHofF32Max;
+    if (f32)
+      for (int i = tid; i < 6 * cnt0; i += blockDim.x) s_hf[i] = __double2float_rn(H[i / 6].genes[i % 6]);
+    __syncthreads();
+    {
+      int cs = 0;
+      if (base + lane < end) {
+        const double *gp = G + 6 * order[base + lane];
+        double g[6];
+        float g32[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) g[i] = G[6 * k + i];
-    bool sim = false;
-    for (int e = lane; e < cnt && !sim; e += 32) sim = hof_similar(g, H[e].genes);
-    if (__any_sync(kFull, sim)) continue;
-    if (lane == 0) {
-      gd_hof_entry &x = H[cnt];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) x.genes[i] = g[i];
-      x.fitness = f[k];
-      x.generation = gen;
-      x.pad = 0;
-    }
-    ++cnt;
-    ++added;
-    __syncwarp();
-    if (cnt > cap) {
-      if (sorted) {
-        const double fn = key_of(H[cnt - 1].fitness);
-        int pos = 0;  // entries before the new one: fitness <= its fitness
-        for (int e = lane; e < cnt - 1; e += 32) pos += key_of(H[e].fitness) <= fn;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) pos += __shfl_xor_sync(kFull, pos, o);
-        for (int e = lane; e < cnt; e += 32) T[e < pos ? e : (e == cnt - 1 ? pos : e + 1)] = H[e];
-      } else {
-        for (int e = lane; e < cnt; e += 32) {
-          const double fe = key_of(H[e].fitness);
-          int rk = 0;
-          for (int q = 0; q < cnt; ++q) {
-            const double fq = key_of(H[q].fitness);
-            rk += (fq < fe) || (fq == fe && q < e);
-          }
-          T[rk] = H[e];
+        for (int i = 0; i < 6; ++i) {
+          g[i] = gp[i];
+          g32[i] = __double2float_rn(g[i]);
         }
+        for (int e = w; e < cnt0; e += nw)
+          if (!(f32 && hof_far32(g32, s_hf + 6 * e))) cs += hof_similar(g, H[e].genes);
+      }
+      s_part[tid] = cs;
+    }
+    __syncthreads();
+    if (tid < 32) {
+      {
+        int cs = 0;
+        for (int q = 0; q < nw; ++q) cs += s_part[32 * q + lane];
+        s_csim[lane] = cs;
       }
       __syncwarp();
-      cnt = cap;
-      for (int e = lane; e < cnt; e += 32) H[e] = T[e];
-      sorted = 1;
-      __syncwarp();
+      int cnt = cnt0, sorted = s_ctl[3], added = s_ctl[1], n_new = 0, next = end;
+      for (int r = base; r < end; ++r) {
+        if (s_csim[r - base] > 0) continue;
+        const double *gp = G + 6 * order[r];
+        double g[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) g[i] = gp[i];
+        const bool sim = lane < n_new && hof_similar(g, s_new + 6 * lane);
+        if (__any_sync(kFull, sim)) continue;
+        if (lane == 0) {
+          gd_hof_entry &x = H[cnt];
+#pragma unroll
+          for (int i = 0; i < 6; ++i) {
+            x.genes[i] = g[i];
+            s_new[6 * n_new + i] = g[i];
+          }
+          x.fitness = f[order[r]];
+          x.generation = gen;
+          x.pad = 0;
+        }
+        ++cnt;
+        ++n_new;
+        ++added;
+        __syncwarp();
+        if (cnt > cap) {
+          if (sorted) {
+            const double fn = key_of(H[cnt - 1].fitness);
+            int pos = 0;  // entries before the new one: fitness <= its fitness
+            for (int e = lane; e < cnt - 1; e += 32) pos += key_of(H[e].fitness) <= fn;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) pos += __shfl_xor_sync(kFull, pos, o);
+            for (int e = lane; e < cnt; e += 32) T[e < pos ? e : (e == cnt - 1 ? pos : e + 1)] = H[e];
+          } else {
+            for (int e = lane; e < cnt; e += 32) {
+              const double fe = key_of(H[e].fitness);
+              int rk = 0;
+              for (int q = 0; q < cnt; ++q) {
+                const double fq = key_of(H[q].fitness);
+                rk += (fq < fe) || (fq == fe && q < e);
+              }
+              T[rk] = H[e];
+            }
+          }
+          __syncwarp();
+          // the entry the prune drops: T[cap]
+          double x[6];
+#pragma unroll
+          for (int i = 0; i < 6; ++i) x[i] = T[cap].genes[i];
+          const unsigned mine = __ballot_sync(kFull, lane < n_new && genes_equal(x, s_new + 6 * lane));
+          if (mine) {
+            const int w = __ffs(mine) - 1;
+            if (lane == 0 && w != n_new - 1)
+              for (int i = 0; i < 6; ++i) s_new[6 * w + i] = s_new[6 * (n_new - 1) + i];
+            --n_new;
+          } else {
+            for (int q = r + 1 + lane; q < end; q += 32) {
+              const double *gq = G + 6 * order[q];
+              if (s_csim[q - base] > 0 && hof_similar(gq, x)) --s_csim[q - base];
+            }
+          }
+          cnt = cap;
+          for (int e = lane; e < cnt; e += 32) H[e] = T[e];
+          sorted = 1;
+          __syncwarp();
+        }
+        if (added >= c.hof_top_k || n_new == kHofNewMax) {
+          next = r + 1;
+          break;
+        }
+      }
+      if (lane == 0) {
+        s_ctl[0] = next;
+        s_ctl[1] = added;
+        s_ctl[2] = cnt;
+        s_ctl[3] = sorted;
+      }
     }
+    __syncthreads();
   }
-  if (lane == 0) {
-    st.hof_n = cnt;
-    st.hof_sorted = sorted;
+  if (tid == 0) {
+    st.hof_n = s_ctl[2];
+    st.hof_sorted = s_ctl[3];
   }
 }
 
@@ -241,6 +350,9 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   int *order = elite + 64;                         // [n] stable ascending order (Hall of Fame only)
   __shared__ double s_eg[64 * 6];                  // elites' genes, staged before the population is overwritten
   __shared__ int s_evolve, s_hof, s_gen;
+  __shared__ int s_csim[kHofChunk], s_hctl[4], s_hpart[256];  // Hall of Fame rounds
+  __shared__ double s_hnew[kHofNewMax * 6];
+  __shared__ float s_hf[kHofF32Max * 6];
   GaJobState &st = P.state[job];
   if (st.stop) return;
   const gd_pose_energy *E = P.energies + static_cast<size_t>(job) * n;
@@ -295,7 +407,7 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
     if (s_hof) order[r] = k;
   }
   __syncthreads();
-  if (s_hof && tid < 32) hof_add(P, st, job, s_gen, G, f, order);
+  if (s_hof) hof_update(P, st, job, s_gen, G, f, order, s_csim, s_hnew, s_hctl, s_hpart, s_hf);
   if (!s_evolve) return;
   const int gen = st.gen - 1;  // draws of the generation being evolved
   const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;

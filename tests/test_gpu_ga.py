@@ -73,13 +73,15 @@ def hof_list(recs):
     return [(tuple(r["genes"].tolist()), float(r["fitness"]), int(r["generation"])) for r in recs]
 
 
-@pytest.mark.parametrize("early,cap,top_k", [(False, 500, 10), (True, 500, 10), (False, 7, 3), (False, 40, 10)])
-def test_ga_hall_of_fame_matches_oracle(oracle, early, cap, top_k):
+@pytest.mark.parametrize("early,cap,top_k,pop", [(False, 500, 10, 24), (True, 500, 10, 24), (False, 7, 3, 24),
+                                                 (False, 40, 10, 24), (False, 90, 60, 300), (False, 500, 300, 300)])
+def test_ga_hall_of_fame_matches_oracle(oracle, early, cap, top_k, pop):
     # plain FP64: the device Hall of Fame equals the oracle's HallOfFame fed
     # with the same populations, entry for entry and in order (small caps
-    # exercise the prune, src/commands/run.rs:174-179)
+    # exercise the prune, src/commands/run.rs:174-179; populations over 256
+    # and top_k over 32 exercise several pre-check rounds per generation)
     c, lig = setup_job(30, 36, 4, seed=79)
-    cfg = _lib.ga_default_cfg(pop_size=24, max_generations=14 if not early else 40, seed=6,
+    cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=14 if not early else 40, seed=6,
                               early_stopping=1 if early else 0, convergence_window=3, convergence_threshold=0.01,
                               hof_max_size=cap, hof_top_k=top_k)
     cx = gd.Complex(c.receptor, lig, c.restraint_pairs)

@@ -286,12 +286,17 @@ class GaResult:
     generations: np.ndarray    # (jobs,) generations evolved
     history: np.ndarray        # (jobs, max_generations) best fitness per generation
     hall_of_fame: Optional[List[np.ndarray]] = None  # per job, HOF_ENTRY_DTYPE records in the reference's order
+    best_metrics: Optional[np.ndarray] = None  # (jobs, generations) DOCK_METRICS_DTYPE of each generation's best pose
+    mean_dockq: Optional[np.ndarray] = None    # (jobs, generations) mean DockQ of each generation
 
 
 def run_ga(complexes: Sequence[Complex], cfg=None, precision=GD_PREC_F32, use_graph: bool = True,
-           ctx: Optional[Context] = None, hall_of_fame: bool = False) -> GaResult:
+           ctx: Optional[Context] = None, hall_of_fame: bool = False,
+           evaluators: Optional[Sequence[Optional["Evaluator"]]] = None) -> GaResult:
     """gdock's GA loop (src/commands/run.rs:381-531) for many jobs on the GPU;
-    with ``hall_of_fame`` also each job's HallOfFame (src/commands/run.rs:77-213)."""
+    with ``hall_of_fame`` also each job's HallOfFame (src/commands/run.rs:77-213);
+    with ``evaluators`` (one per job, None allowed) the DockQ metrics of every
+    generation (src/commands/run.rs:388,449-451; NaN where not reached)."""
     ctx = ctx or complexes[0].ctx
     cfg = cfg or ga_default_cfg()
     J, n, G = len(complexes), cfg.pop_size, cfg.max_generations
@@ -302,11 +307,19 @@ def run_ga(complexes: Sequence[Complex], cfg=None, precision=GD_PREC_F32, use_gr
     hist = np.zeros((J, max(G, 1)))
     hof = np.zeros((J, max(cfg.hof_max_size, 1)), dtype=HOF_ENTRY_DTYPE) if hall_of_fame else None
     hof_n = np.zeros(J, np.int32) if hall_of_fame else None
+    best = mean = met = None
+    if evaluators is not None:
+        evh = (C.c_void_p * J)(*[e.h.value if e is not None else None for e in evaluators])
+        best = np.full((J, max(G, 1)), np.nan, dtype=DOCK_METRICS_DTYPE)
+        mean = np.full((J, max(G, 1)), np.nan)
+        met = _lib.GdGaMetrics(C.cast(evh, C.c_void_p), ptr(best), ptr(mean))
     ctx.check(ctx.lib.gd_ga_run(ctx.h, C.cast(handles, C.c_void_p), J, C.byref(cfg), _prec(precision),
                                 1 if use_graph else 0, ptr(genes), ptr(energies), ptr(gens), ptr(hist),
-                                ptr(hof) if hall_of_fame else None, ptr(hof_n) if hall_of_fame else None))
+                                ptr(hof) if hall_of_fame else None, ptr(hof_n) if hall_of_fame else None,
+                                C.byref(met) if met is not None else None))
     hl = [hof[j, :hof_n[j]].copy() for j in range(J)] if hall_of_fame else None
-    return GaResult(genes, energies, gens, hist[:, :G], hl)
+    return GaResult(genes, energies, gens, hist[:, :G], hl, best[:, :G] if best is not None else None,
+                    mean[:, :G] if mean is not None else None)
 
 
 class Server:

@@ -43,6 +43,10 @@ class GdAtoms(C.Structure):
                 ("chain", C.c_void_p), ("element", C.c_void_p), ("is_ca", C.c_void_p)]
 
 
+class GdGaMetrics(C.Structure):
+    _fields_ = [("evaluators", C.c_void_p), ("best", C.c_void_p), ("mean_dockq", C.c_void_p)]
+
+
 class GdWeights(C.Structure):
     _fields_ = [("vdw", C.c_double), ("elec", C.c_double), ("desolv", C.c_double), ("air", C.c_double)]
 
@@ -138,7 +142,8 @@ def load(path: Path = LIB_PATH):
         "gd_score_frames_device_noalloc": ([vp, vp, i32, d, vp, vp], C.c_int),
         "gd_ga_default_cfg": ([C.POINTER(GdGaCfg)], C.c_int),
         "gd_ga_draw": ([C.POINTER(GdGaCfg), C.c_uint64, i32, vp, vp, vp, vp, vp, vp], C.c_int),
-        "gd_ga_run": ([vp, vp, i32, C.POINTER(GdGaCfg), C.c_int, i32, vp, vp, vp, vp, vp, vp], C.c_int),
+        "gd_ga_run": ([vp, vp, i32, C.POINTER(GdGaCfg), C.c_int, i32, vp, vp, vp, vp, vp, vp, C.POINTER(GdGaMetrics)],
+                      C.c_int),
         "gd_server_default_cfg": ([C.POINTER(GdServerCfg)], C.c_int),
         "gd_server_create": ([vp, C.POINTER(GdServerCfg), C.POINTER(vp)], C.c_int),
         "gd_server_destroy": ([vp], C.c_int),

@@ -55,6 +55,7 @@ struct EvalParams {
   const D4 *u_ref, *u_iref, *p_rec;
   int n_u, n_ref, n_iref, n_native;
   double thr5;
+  const int *skip;  // nonzero: no work (a finished GA job); may be null
   gd_dock_metrics *out;
 };
 
@@ -65,7 +66,7 @@ constexpr int kEvalWarps = 4;
 __global__ void __launch_bounds__(kEvalWarps * 32) k_dockq(const EvalParams e) {
   const int lane = threadIdx.x & 31;
   const int pose = blockIdx.x * kEvalWarps + (threadIdx.x >> 5);
-  if (pose >= e.p.n_poses) return;
+  if (pose >= e.p.n_poses || (e.skip && *e.skip)) return;
   gd_pose_frame f;
   {
     const double *src = reinterpret_cast<const double *>(e.p.frames + pose);
@@ -111,6 +112,31 @@ double host_dist(double ax, double ay, double az, double bx, double by, double b
 }
 
 }  // namespace
+
+gd_complex *evaluator_complex(const gd_evaluator *ev) { return ev->cx; }
+
+gd_status launch_dockq(gd_evaluator *ev, const gd_pose_frame *d_frames, int n, gd_dock_metrics *d_out,
+                       const int *skip, cudaStream_t stream) {
+  if (n == 0) return GD_OK;
+  EvalParams ep{};
+  ep.p = make_params(ev->cx, d_frames, nullptr, n, nullptr, 0.0);
+  ep.u_slot = ev->u_slot;
+  ep.u_pbeg = ev->u_pbeg;
+  ep.u_ref = ev->u_ref;
+  ep.u_iref = ev->u_iref;
+  ep.p_rec = ev->p_rec;
+  ep.n_u = ev->n_u;
+  ep.n_ref = ev->n_ref;
+  ep.n_iref = ev->n_iref;
+  ep.n_native = ev->n_native;
+  ep.thr5 = ev->thr5;
+  ep.skip = skip;
+  ep.out = d_out;
+  k_dockq<<<(n + kEvalWarps - 1) / kEvalWarps, kEvalWarps * 32, 0, stream>>>(ep);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GD_OK : cuda_fail(ev->ctx, e, "evaluator launch");
+}
+
 }  // namespace gd
 
 using namespace gd;
@@ -262,25 +288,8 @@ gd_status gd_evaluate_frames_device(gd_evaluator *ev, const gd_pose_frame *d_fra
   if (!ev) return GD_ERR_INVALID_ARG;
   gd_context *ctx = ev->ctx;
   if (n < 0 || (n > 0 && (!d_frames || !d_out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad frames/out");
-  if (n == 0) return GD_OK;
   cudaSetDevice(ctx->device);
-  EvalParams ep{};
-  ep.p = make_params(ev->cx, d_frames, nullptr, n, nullptr, 0.0);
-  ep.u_slot = ev->u_slot;
-  ep.u_pbeg = ev->u_pbeg;
-  ep.u_ref = ev->u_ref;
-  ep.u_iref = ev->u_iref;
-  ep.p_rec = ev->p_rec;
-  ep.n_u = ev->n_u;
-  ep.n_ref = ev->n_ref;
-  ep.n_iref = ev->n_iref;
-  ep.n_native = ev->n_native;
-  ep.thr5 = ev->thr5;
-  ep.out = d_out;
-  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-  k_dockq<<<(n + kEvalWarps - 1) / kEvalWarps, kEvalWarps * 32, 0, st>>>(ep);
-  const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? GD_OK : cuda_fail(ctx, e, "evaluator launch");
+  return launch_dockq(ev, d_frames, n, d_out, nullptr, stream ? static_cast<cudaStream_t>(stream) : ctx->stream);
 }
 
 gd_status gd_evaluate_poses(gd_evaluator *ev, const double *genes, int32_t n, gd_dock_metrics *out) {

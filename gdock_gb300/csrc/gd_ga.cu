@@ -138,6 +138,10 @@ struct GaStepParams {
   const int *tour, *perm;     // [jobs][max_gen][...]
   const double *cross_u, *mut_u, *mut_z;
   gd_hof_entry *hof, *hof_tmp;  // [jobs][hof_max_size + 1]; null = no Hall of Fame
+  const gd_dock_metrics *metrics;  // [jobs][n] DockQ of the evaluated population; null = none
+  const int *eval_on;              // [jobs] 1 = the job has an evaluator
+  gd_dock_metrics *best_metrics;   // [jobs][max_gen]
+  double *mean_dockq;              // [jobs][max_gen]
   gd_ga_cfg cfg;
 };
 
@@ -375,6 +379,16 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
         if (f[bi] > f[k]) bi = k;
       const double best = f[bi];
       P.history[static_cast<size_t>(job) * c.max_generations + gen] = best;
+      if (P.metrics && P.eval_on[job]) {
+        // the generation's metrics: the best pose's and the mean DockQ as a
+        // left-to-right sum (src/commands/run.rs:388,449-451)
+        const gd_dock_metrics *M = P.metrics + static_cast<size_t>(job) * n;
+        const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;
+        P.best_metrics[jg] = M[bi];
+        double sum = 0.0;
+        for (int k = 0; k < n; ++k) sum += M[k].dockq;
+        P.mean_dockq[jg] = sum / static_cast<double>(n);
+      }
       if (gen > 0) {  // convergence window (src/commands/run.rs:400-409)
         const double imp = (st.last_best - best) / fabs(st.last_best);
         if (imp < c.convergence_threshold) st.stagnant += 1;
@@ -520,6 +534,9 @@ struct GaRun {
   gd_pose_energy *energies = nullptr;
   GaJobState *state = nullptr;
   gd_hof_entry *hof = nullptr, *hof_tmp = nullptr;
+  gd_dock_metrics *metrics = nullptr, *best_metrics = nullptr;
+  double *mean_dockq = nullptr;
+  int *eval_on = nullptr;
   std::vector<std::pair<void *, size_t>> allocs;
 };
 
@@ -539,7 +556,7 @@ static void ga_release(gd_context *ctx, GaRun &R) {
 extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs, const gd_ga_cfg *cfg,
                                gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
                                int32_t *out_generations, double *out_history, gd_hof_entry *out_hof,
-                               int32_t *out_hof_count) {
+                               int32_t *out_hof_count, const gd_ga_metrics *metrics) {
   using namespace gd;
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (!complexes || jobs <= 0 || !cfg || !out_genes || !out_energies)
@@ -553,6 +570,13 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
   if (hof && (!out_hof || !out_hof_count || c.hof_max_size < 0 || c.hof_max_size > (1 << 20) || c.hof_top_k < 0))
     return fail(ctx, GD_ERR_INVALID_ARG, "Hall of Fame: out_hof and out_hof_count together, hof_max_size in [0, 2^20]");
   const int hcap = hof ? c.hof_max_size : 0;
+  const bool with_metrics = metrics && metrics->evaluators;
+  if (with_metrics && (!metrics->best || !metrics->mean_dockq))
+    return fail(ctx, GD_ERR_INVALID_ARG, "GA metrics: best and mean_dockq are required with evaluators");
+  if (with_metrics)
+    for (int j = 0; j < jobs; ++j)
+      if (metrics->evaluators[j] && evaluator_complex(metrics->evaluators[j]) != complexes[j])
+        return fail(ctx, GD_ERR_INVALID_ARG, "GA metrics: an evaluator of another complex");
   for (int j = 0; j < jobs; ++j)
     if (!complexes[j] || complexes[j]->ctx != ctx) return fail(ctx, GD_ERR_INVALID_ARG, "complex of another context");
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -620,6 +644,29 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     if ((s = ga_alloc(ctx, R, hb, &p)) != GD_OK) goto done;
     R.hof_tmp = static_cast<gd_hof_entry *>(p);
   }
+  if (with_metrics) {
+    std::vector<int> on(jobs);
+    for (int j = 0; j < jobs; ++j) on[j] = metrics->evaluators[j] != nullptr;
+    if ((s = up(on.data(), sizeof(int) * jobs, &p)) != GD_OK) goto done;
+    R.eval_on = static_cast<int *>(p);
+    if ((s = ga_alloc(ctx, R, sizeof(gd_dock_metrics) * jn, &p)) != GD_OK) goto done;
+    R.metrics = static_cast<gd_dock_metrics *>(p);
+    const size_t jgb = static_cast<size_t>(jobs) * std::max(G, 1);
+    if ((s = ga_alloc(ctx, R, sizeof(gd_dock_metrics) * jgb, &p)) != GD_OK) goto done;
+    R.best_metrics = static_cast<gd_dock_metrics *>(p);
+    if ((s = ga_alloc(ctx, R, sizeof(double) * jgb, &p)) != GD_OK) goto done;
+    R.mean_dockq = static_cast<double *>(p);
+    // entries of generations not reached keep the caller's values
+    if (G > 0) {
+      e = cudaMemcpy(R.best_metrics, metrics->best, sizeof(gd_dock_metrics) * jobs * G, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(R.mean_dockq, metrics->mean_dockq, sizeof(double) * jobs * G, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        s = cuda_fail(ctx, e, "GA metrics upload");
+        goto done;
+      }
+    }
+  }
   {
     // one scoring descriptor per job; poses outside [-M, M] never occur
     std::vector<ScoreParams> descs;
@@ -650,6 +697,10 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     P.mut_z = R.mut_z;
     P.hof = R.hof;
     P.hof_tmp = R.hof_tmp;
+    P.metrics = R.metrics;
+    P.eval_on = R.eval_on;
+    P.best_metrics = R.best_metrics;
+    P.mean_dockq = R.mean_dockq;
     P.cfg = c;
     P.cfg.hof_max_size = hcap;
     const size_t ga_smem = sizeof(double) * (n + m) + sizeof(int) * (2 * n + 64);
@@ -671,6 +722,13 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
           if (ss != GD_OK) return ss;
         }
       }
+      if (with_metrics)
+        for (int j = 0; j < jobs; ++j)
+          if (metrics->evaluators[j]) {
+            gd_status ss = launch_dockq(metrics->evaluators[j], descs[j].frames, n,
+                                        R.metrics + static_cast<size_t>(j) * n, &R.state[j].stop, st);
+            if (ss != GD_OK) return ss;
+          }
       k_ga_step<<<jobs, 256, ga_smem, st>>>(P);
       ee = cudaGetLastError();
       return ee == cudaSuccess ? GD_OK : cuda_fail(ctx, ee, "GA step kernel");
@@ -719,6 +777,15 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     }
     if (out_generations)
       for (int j = 0; j < jobs; ++j) out_generations[j] = h_state[j].gen;
+    if (with_metrics && G > 0) {
+      e = cudaMemcpy(metrics->best, R.best_metrics, sizeof(gd_dock_metrics) * jobs * G, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(metrics->mean_dockq, R.mean_dockq, sizeof(double) * jobs * G, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        s = cuda_fail(ctx, e, "GA metrics results");
+        goto done;
+      }
+    }
     if (hof) {
       for (int j = 0; j < jobs; ++j) {
         out_hof_count[j] = hcap > 0 ? h_state[j].hof_n : 0;

@@ -177,5 +177,10 @@ struct BatchLaunch;
 gd_status batch_prepare(gd_context *ctx, const std::vector<ScoreParams> &descs, bool serial, bool clamp, int slots,
                         BatchLaunch **out);
 gd_status batch_launch(gd_context *ctx, BatchLaunch *b, cudaStream_t stream);
+// DockQ metrics of n device-resident frames of the evaluator's complex
+// (gd_eval.cu); skip (may be null) is read on the device: nonzero = no work.
+gd_status launch_dockq(gd_evaluator *ev, const gd_pose_frame *d_frames, int n, gd_dock_metrics *d_out,
+                       const int *skip, cudaStream_t stream);
+gd_complex *evaluator_complex(const gd_evaluator *ev);
 void batch_free(gd_context *ctx, BatchLaunch *b);
 }  // namespace gd

@@ -283,6 +283,19 @@ gd_status gd_ga_default_cfg(gd_ga_cfg *cfg);
  * uniforms and the mutation perturbations (any pointer may be NULL). */
 gd_status gd_ga_draw(const gd_ga_cfg *cfg, uint64_t seed, int32_t generations, double *init_genes, int32_t *tour,
                      int32_t *perm, double *cross_u, double *mut_u, double *mut_z);
+/* DockQ metrics of every generation (src/commands/run.rs:387-388,449-450):
+ * for each job with an evaluator (created on that job's complex), the
+ * metrics of the generation's first best-fitness pose and the mean DockQ of
+ * the population, computed on the device after each evaluation inside the
+ * generation loop.  best and mean_dockq are jobs x max_generations; entries
+ * of generations a job did not reach, or of jobs without an evaluator, are
+ * left as they were. */
+typedef struct gd_ga_metrics {
+  gd_evaluator *const *evaluators; /* [jobs], NULL entries allowed */
+  gd_dock_metrics *best;           /* [jobs][max_generations] */
+  double *mean_dockq;              /* [jobs][max_generations] */
+} gd_ga_metrics;
+
 /* Run the GA of `jobs` complexes to completion on the device; with
  * use_graph (FP32 form) one generation is a captured CUDA graph replayed.
  * Outputs: final populations (jobs x pop x 6), their energies
@@ -292,11 +305,11 @@ gd_status gd_ga_draw(const gd_ga_cfg *cfg, uint64_t seed, int32_t generations, d
  * generation loop, src/commands/run.rs:99-213,385; kept on the device):
  * out_hof receives jobs x hof_max_size entries in the reference's order,
  * out_hof_count the entries per job.  Both NULL (or hof_max_size 0) = no
- * Hall of Fame. */
+ * Hall of Fame.  metrics may be NULL (no per-generation DockQ). */
 gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, int32_t jobs, const gd_ga_cfg *cfg,
                     gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
                     int32_t *out_generations, double *out_history, gd_hof_entry *out_hof,
-                    int32_t *out_hof_count);
+                    int32_t *out_hof_count, const gd_ga_metrics *metrics);
 
 /* ------------------------------------------------------------- serving --
  * A request loop for docking jobs (gdock's `run` GA per job): jobs are

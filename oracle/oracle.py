@@ -278,11 +278,15 @@ class HallOfFame:
                 added += 1
 
 
-def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, hof=None):
+def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, hof=None, evaluator=None,
+           metrics_out=None):
     """gdock's generation loop (src/commands/run.rs:381-531) on the CPU with
     explicit draws: returns final genes, final energies, generations, history;
     ``hof`` (a HallOfFame) is fed after every evaluation inside the loop
-    (src/commands/run.rs:385)."""
+    (src/commands/run.rs:385); with ``evaluator`` (an Evaluator) the list
+    ``metrics_out`` receives, per generation, the metrics (rmsd, irmsd, fnat,
+    dockq) of the first best-fitness pose and the mean DockQ
+    (src/commands/run.rs:388,449-451)."""
     genes = draws["init"].copy()
     last_best, stagnant, history = None, 0, []
     gen = 0
@@ -293,6 +297,13 @@ def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, 
         f = e[:, 0]
         if hof is not None:
             hof.add_from_population(genes, f, gen)
+        if evaluator is not None:
+            m = evaluator.eval_metrics(lig, genes)
+            bi = 0
+            for k in range(1, len(f)):
+                if f[bi] > f[k]:
+                    bi = k
+            metrics_out.append((tuple(m[bi]), _seq_sum(m[:, 3]) / len(f)))
         best = f[int(np.argmin(f))]
         bi = 0
         for k in range(1, len(f)):

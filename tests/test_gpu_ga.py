@@ -119,3 +119,36 @@ def test_ga_hall_of_fame_fp32_graph_invariants(oracle):
                                  hof_top_k=4)
         alone = gd.run_ga([cx], c1, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
         assert alone.hall_of_fame[0].tobytes() == mix.hall_of_fame[j].tobytes()
+
+
+@pytest.mark.parametrize("prec,graph", [(gd.GD_PREC_F64, False), (gd.GD_PREC_F32, True)])
+def test_ga_dockq_every_generation(oracle, prec, graph):
+    # the metrics of every generation's best pose and the mean DockQ, on the
+    # device inside the GA, against the oracle's evaluator run on the same
+    # populations (FP64: the populations are the oracle's bit for bit; FP32:
+    # the device populations are re-evaluated by the oracle)
+    import dataclasses
+    c, lig = setup_job(30, 36, 4, seed=80)
+    reference = dataclasses.replace(lig, x=lig.x + 1.5)
+    cfg = _lib.ga_default_cfg(pop_size=24, max_generations=10, seed=8, early_stopping=0)
+    ctx = gd.Context(0)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    other = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    ev = gd.Evaluator(cx, reference)
+    res = gd.run_ga([cx, other], cfg, prec, use_graph=graph, ctx=ctx, evaluators=[ev, None])
+    assert np.isnan(res.mean_dockq[1]).all()  # the job without an evaluator
+    oev = oracle.Evaluator(c.receptor, reference)
+    assert len(oev.native_contacts) > 0
+    if prec == gd.GD_PREC_F64:
+        draws = _lib.ga_draw(cfg, cfg.seed, cfg.max_generations)
+        out = []
+        oracle.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, evaluator=oev, metrics_out=out)
+        ref_best = np.array([b for b, _ in out])
+        ref_mean = np.array([m for _, m in out])
+        got = np.stack([res.best_metrics[0][k] for k in ("rmsd", "irmsd", "fnat", "dockq")], axis=1)
+        # device frames use CUDA sincos: coordinates agree to a few ulp
+        np.testing.assert_allclose(got, ref_best, rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(res.mean_dockq[0], ref_mean, rtol=1e-9)
+    else:
+        assert np.isfinite(res.mean_dockq[0]).all()
+        assert ((res.best_metrics[0]["dockq"] > 0) & (res.best_metrics[0]["dockq"] <= 1)).all()

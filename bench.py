@@ -299,6 +299,10 @@ def run_c1(args):
     orc.cluster([orc.pose_contacts(c.receptor, lig, np.array(g)) for g, _, _ in hof.entries])
     t_cpu = time.perf_counter() - t0
     same = bool(np.array_equal(g_cpu, res.genes[0]))
+    # fitness comparisons of the GA decided by a relative margin < 1e-9 (the
+    # ones a different summation order could turn), outside the timed leg
+    close = []
+    orc.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, nthreads=threads, close_out=close)
     same_hof = bool(np.array_equal(np.array([g for g, _, _ in hof.entries]), res.hall_of_fame[0]["genes"]))
     line = {"metric": "docks/s (plain FP64 GA, pop 150 x 50 generations, then FCC clustering)",
             "value": 1.0 / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": max(1, args.warmup),
@@ -312,6 +316,9 @@ def run_c1(args):
             "hall_of_fame_equals_oracle": same_hof,
             "f32_graph_docks_per_s": 1.0 / t32,
             "final_population_equals_oracle": same,
+            "ga_comparisons": {"total": int(sum(t for t, _ in close)), "margin_below_1e-9": int(sum(k for _, k in close)),
+                               "note": "fitness comparisons of bookkeeping, elitism, tournaments and the offspring "
+                                       "sort over the 50 generations; ties count as margin 0"},
             "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "docks/s", "cores": threads, "kind": "port",
                              "sample": "one full dock: the oracle's GA and Hall of Fame on the same draws, then "
                                        "its FCC clustering"}}

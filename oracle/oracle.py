@@ -235,6 +235,49 @@ def evolve(genes, fitness, draws, g, elitism=5, tournament=3, crossover_rate=0.6
     return go, fo
 
 
+def ga_close_comparisons(f, tour, perm, tournament=3, tol=1e-9):
+    """The fitness comparisons one generation's bookkeeping and evolve decide
+    (first best of the generation, src/commands/run.rs:391-398; elitism's
+    stable sort, src/population.rs:76-82; tournaments, :136-156; the stable
+    sort of the offspring by carried fitness, :110-118), counted as
+    (total, close): close = decided by a relative margin below tol (ties
+    included).  Sorts count their adjacent pairs in sorted order.  A close
+    comparison is one that a difference of summation order in the energies
+    could turn."""
+    f = np.asarray(f, dtype=np.float64)
+    n = len(f)
+    total = close = 0
+
+    def cmp(a, b):
+        nonlocal total, close
+        total += 1
+        if abs(a - b) <= tol * max(abs(a), abs(b)):
+            close += 1
+
+    bi = 0
+    for k in range(1, n):
+        cmp(f[bi], f[k])
+        if f[bi] > f[k]:
+            bi = k
+    srt = np.sort(f, kind="stable")
+    for k in range(n - 1):
+        cmp(srt[k], srt[k + 1])
+    sel = []
+    for k in range(n):
+        best = int(tour[tournament * k])
+        for t in range(1, tournament):
+            q = int(tour[tournament * k + t])
+            cmp(f[best], f[q])
+            if f[best] > f[q]:
+                best = q
+        sel.append(best)
+    m = 2 * (n // 2)
+    carried = np.sort(np.array([f[sel[int(perm[i])]] for i in range(m)]), kind="stable")
+    for k in range(m - 1):
+        cmp(carried[k], carried[k + 1])
+    return total, close
+
+
 class HallOfFame:
     """HallOfFame (src/commands/run.rs:75-215) restated: entries are
     (genes tuple, fitness, generation) in the reference's order."""
@@ -279,14 +322,16 @@ class HallOfFame:
 
 
 def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, hof=None, evaluator=None,
-           metrics_out=None):
+           metrics_out=None, close_out=None):
     """gdock's generation loop (src/commands/run.rs:381-531) on the CPU with
     explicit draws: returns final genes, final energies, generations, history;
     ``hof`` (a HallOfFame) is fed after every evaluation inside the loop
     (src/commands/run.rs:385); with ``evaluator`` (an Evaluator) the list
     ``metrics_out`` receives, per generation, the metrics (rmsd, irmsd, fnat,
     dockq) of the first best-fitness pose and the mean DockQ
-    (src/commands/run.rs:388,449-451)."""
+    (src/commands/run.rs:388,449-451); ``close_out`` (a list) receives the
+    (total, close) fitness comparisons of every evolved generation
+    (ga_close_comparisons)."""
     genes = draws["init"].copy()
     last_best, stagnant, history = None, 0, []
     gen = 0
@@ -317,6 +362,8 @@ def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, 
         last_best = best
         if cfg.early_stopping and stagnant >= cfg.convergence_window:
             return genes, e, gen, np.array(history)
+        if close_out is not None:
+            close_out.append(ga_close_comparisons(f, draws["tour"][gen], draws["perm"][gen], cfg.tournament_size))
         genes, _ = evolve(genes, f, draws, gen, cfg.elitism, cfg.tournament_size, cfg.crossover_rate,
                           cfg.mutation_rate, cfg.max_displacement)
         gen += 1

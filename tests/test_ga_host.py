@@ -74,3 +74,17 @@ def test_crossover_complementary_and_bounds(oracle):
         genes, fit = oracle.evolve(genes, fit, d2, g, mutation_rate=1.0)
         assert ((genes[:, :3] >= 0) & (genes[:, :3] <= 2 * math.pi)).all()
         assert ((genes[:, 3:] >= -50) & (genes[:, 3:] <= 50)).all()
+
+
+def test_ga_close_comparisons_counts(oracle):
+    # n = 4, tournament 2: best-of-generation 3 + elitism 3 + tournaments 4 +
+    # offspring 3 comparisons; the two equal values and the 1e-12 pair are close
+    f = [-10.0, -10.0, -5.0, -5.0 * (1 + 1e-12)]
+    tour = [0, 1, 2, 3, 0, 2, 1, 3]
+    perm = [0, 1, 2, 3]
+    total, close = oracle.ga_close_comparisons(f, tour, perm, tournament=2)
+    assert total == 3 + 3 + 4 + 3
+    # bookkeeping: (0,1) tie; elitism adjacent: (-10,-10) tie, (-5(1+1e-12), -5) close;
+    # tournaments: (0,1) tie, (2,3) close; offspring: winners 0, 3, 0, 1 -> carried
+    # -10, -5.000..., -10, -10: two ties
+    assert close == 1 + 2 + 2 + 2

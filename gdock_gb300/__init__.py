@@ -377,6 +377,14 @@ class Server:
         self.ctx.check(self.lib.gd_server_result(self.h, job, C.byref(res), ptr(genes), ptr(energies), ptr(hist)))
         return res, genes, energies, hist[: self.cfg.ga.max_generations]
 
+    def hall_of_fame(self, job: int) -> np.ndarray:
+        """The finished job's Hall of Fame (HOF_ENTRY_DTYPE records)."""
+        cap = max(self.cfg.ga.hof_max_size, 1)
+        out = np.zeros(cap, dtype=HOF_ENTRY_DTYPE)
+        k = C.c_int32(0)
+        self.ctx.check(self.lib.gd_server_hall_of_fame(self.h, job, ptr(out), cap, C.byref(k)))
+        return out[:k.value].copy()
+
     def release(self, job: int):
         self.ctx.check(self.lib.gd_server_release(self.h, job))
 

@@ -26,7 +26,7 @@ EXPORTS = (
     "gd_server_default_cfg", "gd_server_create", "gd_server_destroy", "gd_server_submit", "gd_server_step",
     "gd_server_start", "gd_server_stop", "gd_server_wait", "gd_server_result", "gd_server_release",
     "gd_server_get_stats", "gd_autotune_f32", "gd_evaluator_create", "gd_evaluator_destroy",
-    "gd_evaluate_poses", "gd_evaluate_frames_device", "gd_evaluator_counts",
+    "gd_evaluate_poses", "gd_evaluate_frames_device", "gd_evaluator_counts", "gd_server_hall_of_fame",
 )
 # candidates of gd_autotune_f32, in its order: (GD_TUNE_F32_SLOTS, GD_TUNE_SPLIT)
 AUTOTUNE_CANDIDATES = ((16 + 4, 1), (64 + 2, 1), (64 + 4, 1), (256 + 64 + 2, 1), (256 + 64 + 4, 1), (256 + 64 + 4, 2))
@@ -162,6 +162,7 @@ def load(path: Path = LIB_PATH):
         "gd_evaluate_poses": ([vp, vp, i32, vp], C.c_int),
         "gd_evaluate_frames_device": ([vp, vp, i32, vp, vp], C.c_int),
         "gd_evaluator_counts": ([vp, vp], C.c_int),
+        "gd_server_hall_of_fame": ([vp, i64, vp, i32, C.POINTER(i32)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         f = getattr(lib, name)

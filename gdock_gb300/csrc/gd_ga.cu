@@ -858,6 +858,7 @@ struct Job {
   int generations = 0;
   std::vector<double> genes, history;
   std::vector<gd_pose_energy> energies;
+  std::vector<gd_hof_entry> hof;  // the job's Hall of Fame, in the reference's order
   int error = GD_OK;
   // host draws (made on the submitting thread, uploaded at admission)
   std::vector<double> d_init, d_cu, d_mu, d_mz;
@@ -934,6 +935,13 @@ gd_status server_alloc(gd_server *S) {
   R.state = static_cast<GaJobState *>(p);
   if ((s = A(sizeof(int) * jn, &p)) != GD_OK) return s;
   R.job_of = static_cast<int *>(p);
+  if (c.hof_max_size > 0 && c.hof_top_k > 0) {  // each slot's Hall of Fame
+    const size_t hb = sizeof(gd_hof_entry) * static_cast<size_t>(J) * (c.hof_max_size + 1);
+    if ((s = A(hb, &p)) != GD_OK) return s;
+    R.hof = static_cast<gd_hof_entry *>(p);
+    if ((s = A(hb, &p)) != GD_OK) return s;
+    R.hof_tmp = static_cast<gd_hof_entry *>(p);
+  }
   std::vector<int> job_of(jn);
   for (size_t k = 0; k < jn; ++k) job_of[k] = static_cast<int>(k / n);
   std::vector<GaJobState> st(J, GaJobState{0, kStopFree, 0, 0, 0.0});
@@ -1110,6 +1118,8 @@ gd_status server_tick(gd_server *S, int *active_out) {
   P.cross_u = R.cross_u;
   P.mut_u = R.mut_u;
   P.mut_z = R.mut_z;
+  P.hof = R.hof;
+  P.hof_tmp = R.hof_tmp;
   P.cfg = c;
   const size_t ga_smem = sizeof(double) * 2 * n + sizeof(int) * (2 * n + 64);
   if (ga_smem > 48 * 1024)
@@ -1142,6 +1152,10 @@ gd_status server_tick(gd_server *S, int *active_out) {
     if (e == cudaSuccess && c.max_generations > 0)
       e = cudaMemcpy(job->history.data(), R.history + static_cast<size_t>(j) * c.max_generations,
                      sizeof(double) * c.max_generations, cudaMemcpyDeviceToHost);
+    job->hof.resize(R.hof ? states[j].hof_n : 0);
+    if (e == cudaSuccess && !job->hof.empty())
+      e = cudaMemcpy(job->hof.data(), R.hof + static_cast<size_t>(j) * (c.hof_max_size + 1),
+                     sizeof(gd_hof_entry) * job->hof.size(), cudaMemcpyDeviceToHost);
     GaJobState freed{0, kStopFree, 0, 0, 0.0};
     if (e == cudaSuccess) e = cudaMemcpy(R.state + j, &freed, sizeof(freed), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "server retire");
@@ -1331,6 +1345,19 @@ gd_status gd_server_result(gd_server *S, int64_t job_id, gd_job_result *res, dou
     if (energies) std::memcpy(energies, job->energies.data(), sizeof(gd_pose_energy) * job->energies.size());
     if (history) std::memcpy(history, job->history.data(), sizeof(double) * job->history.size());
   }
+  return GD_OK;
+}
+
+gd_status gd_server_hall_of_fame(gd_server *S, int64_t job_id, gd_hof_entry *entries, int32_t cap, int32_t *count) {
+  if (!S || !count || cap < 0 || (cap > 0 && !entries)) return GD_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return gd::fail(S->ctx, GD_ERR_INVALID_ARG, "unknown job");
+  gd::Job *job = it->second;
+  if (job->status != GD_JOB_DONE) return gd::fail(S->ctx, GD_ERR_STATE, "the job has not finished");
+  *count = static_cast<int32_t>(job->hof.size());
+  if (job->hof.size() > static_cast<size_t>(cap)) return GD_ERR_CAPACITY;
+  if (!job->hof.empty()) std::memcpy(entries, job->hof.data(), sizeof(gd_hof_entry) * job->hof.size());
   return GD_OK;
 }
 

@@ -357,6 +357,12 @@ gd_status gd_server_wait(gd_server *s, int64_t job_id, double timeout_s, int32_t
  * best fitness per generation (max_generations); pointers may be NULL. */
 gd_status gd_server_result(gd_server *s, int64_t job_id, gd_job_result *res, double *genes,
                            gd_pose_energy *energies, double *history);
+/* The Hall of Fame of a finished job (the server keeps one per job when the
+ * GA config's hof_max_size and hof_top_k are positive; the defaults are
+ * 500 and 10): *count receives the entries; up to cap of them go to
+ * entries, GD_ERR_CAPACITY when cap is too small, GD_ERR_STATE before the
+ * job is done. */
+gd_status gd_server_hall_of_fame(gd_server *s, int64_t job_id, gd_hof_entry *entries, int32_t cap, int32_t *count);
 gd_status gd_server_release(gd_server *s, int64_t job_id);
 gd_status gd_server_get_stats(gd_server *s, gd_server_stats *out);
 

@@ -240,18 +240,21 @@ def ga_close_comparisons(f, tour, perm, tournament=3, tol=1e-9):
     (first best of the generation, src/commands/run.rs:391-398; elitism's
     stable sort, src/population.rs:76-82; tournaments, :136-156; the stable
     sort of the offspring by carried fitness, :110-118), counted as
-    (total, close): close = decided by a relative margin below tol (ties
-    included).  Sorts count their adjacent pairs in sorted order.  A close
-    comparison is one that a difference of summation order in the energies
-    could turn."""
+    (total, ties, close): ties = equal values (identical poses give identical
+    energies in any implementation, so ties are resolved by index alike);
+    close = unequal values decided by a relative margin below tol, the
+    comparisons a difference of summation order in the energies could turn.
+    Sorts count their adjacent pairs in sorted order."""
     f = np.asarray(f, dtype=np.float64)
     n = len(f)
-    total = close = 0
+    total = ties = close = 0
 
     def cmp(a, b):
-        nonlocal total, close
+        nonlocal total, ties, close
         total += 1
-        if abs(a - b) <= tol * max(abs(a), abs(b)):
+        if a == b:
+            ties += 1
+        elif abs(a - b) <= tol * max(abs(a), abs(b)):
             close += 1
 
     bi = 0
@@ -275,7 +278,7 @@ def ga_close_comparisons(f, tour, perm, tournament=3, tol=1e-9):
     carried = np.sort(np.array([f[sel[int(perm[i])]] for i in range(m)]), kind="stable")
     for k in range(m - 1):
         cmp(carried[k], carried[k + 1])
-    return total, close
+    return total, ties, close
 
 
 class HallOfFame:
@@ -330,7 +333,7 @@ def run_ga(rec, lig, pairs, cfg, draws, weights=DEFAULT_WEIGHTS, nthreads=None, 
     ``metrics_out`` receives, per generation, the metrics (rmsd, irmsd, fnat,
     dockq) of the first best-fitness pose and the mean DockQ
     (src/commands/run.rs:388,449-451); ``close_out`` (a list) receives the
-    (total, close) fitness comparisons of every evolved generation
+    (total, ties, close) fitness comparisons of every evolved generation
     (ga_close_comparisons)."""
     genes = draws["init"].copy()
     last_best, stagnant, history = None, 0, []

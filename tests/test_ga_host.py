@@ -82,9 +82,9 @@ def test_ga_close_comparisons_counts(oracle):
     f = [-10.0, -10.0, -5.0, -5.0 * (1 + 1e-12)]
     tour = [0, 1, 2, 3, 0, 2, 1, 3]
     perm = [0, 1, 2, 3]
-    total, close = oracle.ga_close_comparisons(f, tour, perm, tournament=2)
+    total, ties, close = oracle.ga_close_comparisons(f, tour, perm, tournament=2)
     assert total == 3 + 3 + 4 + 3
     # bookkeeping: (0,1) tie; elitism adjacent: (-10,-10) tie, (-5(1+1e-12), -5) close;
     # tournaments: (0,1) tie, (2,3) close; offspring: winners 0, 3, 0, 1 -> carried
     # -10, -5.000..., -10, -10: two ties
-    assert close == 1 + 2 + 2 + 2
+    assert ties == 1 + 1 + 1 + 2 and close == 0 + 1 + 1 + 0

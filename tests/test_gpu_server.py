@@ -69,11 +69,19 @@ def test_server_matches_batched_ga_run():
     cfg = ga_cfg()
     cfg.seed = 77
     cx = gd.Complex(rec, lig, pairs, ctx=ctx)
-    ref = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=False, ctx=ctx)
+    ref = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=False, ctx=ctx, hall_of_fame=True)
     res, genes, e, hist = run_alone(ctx, (rec, lig, pairs), 77)
     assert res.generations == ref.generations[0]
     np.testing.assert_array_equal(genes, ref.genes[0])
     assert e.tobytes() == ref.energies[0].tobytes()
+    # the served job's Hall of Fame equals the batched run's
+    srv = gd.Server(ctx, max_slots=2, ga=cfg)
+    jid = srv.submit(rec, lig, pairs, seed=77)
+    while srv.step():
+        pass
+    h = srv.hall_of_fame(jid)
+    assert len(h) > 0 and h.tobytes() == ref.hall_of_fame[0].tobytes()
+    srv.close()
 
 
 def test_admission_by_hbm_budget_and_background_thread():

@@ -340,87 +340,135 @@ __device__ void hof_update(const GaStepParams &P, GaJobState &st, int job, int g
   }
 }
 
+// Sort keys of fitness values: unsigned order = the order of the values,
+// -0 with +0, NaN after every number (an order the reference's partial_cmp
+// sorts do not define; NaN never arises for finite inputs).
+__device__ __forceinline__ unsigned long long asc_key(double f) {
+  if (f != f) f = INFINITY;
+  if (f == 0.0) f = 0.0;
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(f));
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Block-wide bitonic sort of (key, idx) pairs, ascending by key then index,
+// over P (a power of two) entries; every thread of the block calls it.
+__device__ void bitonic_sort(unsigned long long *key, int *idx, int P) {
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+        const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i | j;
+        const unsigned long long a = key[i], b = key[l];
+        const int ia = idx[i], ib = idx[l];
+        const bool a_after_b = a > b || (a == b && ia > ib);
+        if (a_after_b == ((i & k) == 0)) {
+          key[i] = b;
+          key[l] = a;
+          idx[i] = ib;
+          idx[l] = ia;
+        }
+      }
+      __syncthreads();
+    }
+}
+
+__host__ __device__ inline int pow2_at_least(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+// dynamic shared memory of k_ga_step for a population of n
+inline size_t ga_step_smem(int n) {
+  const size_t p2 = static_cast<size_t>(pow2_at_least(n));
+  return sizeof(double) * n + sizeof(unsigned long long) * p2 + sizeof(int) * (n + p2);
+}
+
 // One CTA per job: the reference loop's bookkeeping for the fitness just
-// computed (with the Hall of Fame), then evolve.
+// computed (with the Hall of Fame), then evolve.  The stable orders of the
+// population (elitism, Hall of Fame, best of the generation) and of the
+// offspring are bitonic sorts of integer keys: FP64 comparisons run at a
+// small fraction of the integer rate on this part, and the O(n^2) rank
+// counts they replace took 29 ms per generation at 4,096 poses.
 __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gd_ga_cfg &c = P.cfg;
   const int job = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
-  const int n = c.pop_size, m = 2 * (n / 2);
-  double *f = reinterpret_cast<double *>(smem);   // [n] fitness of the evaluated population
-  double *f2 = f + n;                              // [m] fitness carried by the offspring
-  int *sel = reinterpret_cast<int *>(f2 + m);      // [n] tournament winners
-  int *elite = sel + n;                            // [64] elites
-  int *order = elite + 64;                         // [n] stable ascending order (Hall of Fame only)
+  const int n = c.pop_size, m = 2 * (n / 2), P2 = pow2_at_least(n);
+  double *f = reinterpret_cast<double *>(smem);                            // [n] fitness of the population
+  unsigned long long *kb = reinterpret_cast<unsigned long long *>(f + n);  // [P2] sort keys
+  int *sel = reinterpret_cast<int *>(kb + P2);                             // [n] tournament winners
+  int *order = sel + n;                                                    // [P2] sort indices
   __shared__ double s_eg[64 * 6];                  // elites' genes, staged before the population is overwritten
-  __shared__ int s_evolve, s_hof, s_gen;
+  __shared__ int s_evolve, s_hof, s_gen, s_final, s_nan;
   __shared__ int s_csim[kHofChunk], s_hctl[4], s_hpart[256];  // Hall of Fame rounds
   __shared__ double s_hnew[kHofNewMax * 6];
   __shared__ float s_hf[kHofF32Max * 6];
   GaJobState &st = P.state[job];
   if (st.stop) return;
   const gd_pose_energy *E = P.energies + static_cast<size_t>(job) * n;
+  if (tid == 0) {
+    s_final = st.gen >= c.max_generations;
+    s_nan = 0;
+  }
   for (int k = tid; k < n; k += nt) f[k] = E[k].fitness;
   __syncthreads();
+  if (s_final) {
+    // the evaluation just done was of the final population: stop here
+    if (tid == 0) st.stop = 2;
+    return;
+  }
+  // stable ascending order of the population (src/population.rs:76-82 for
+  // the elites, src/commands/run.rs:195-201 for the Hall of Fame)
+  for (int k = tid; k < P2; k += nt) {
+    if (k < n && f[k] != f[k]) s_nan = 1;
+    kb[k] = k < n ? asc_key(f[k]) : ~0ull;
+    order[k] = k;
+  }
+  __syncthreads();
+  bitonic_sort(kb, order, P2);
   if (tid == 0) {
     const int gen = st.gen;
     s_gen = gen;
-    if (gen >= c.max_generations) {
-      // the evaluation just done was of the final population: stop here
-      st.stop = 2;
-      s_evolve = 0;
-      s_hof = 0;
-    } else {
-      // Hall of Fame of every evaluation inside the loop (src/commands/run.rs:385)
-      s_hof = P.hof != nullptr && c.hof_max_size > 0 && c.hof_top_k > 0;
-      // best of this generation, first minimum (src/commands/run.rs:391-398)
-      int bi = 0;
+    // Hall of Fame of every evaluation inside the loop (src/commands/run.rs:385)
+    s_hof = P.hof != nullptr && c.hof_max_size > 0 && c.hof_top_k > 0;
+    // best of this generation, first minimum (src/commands/run.rs:391-398):
+    // the head of the stable order unless a NaN makes the comparisons differ
+    int bi = order[0];
+    if (s_nan) {
+      bi = 0;
       for (int k = 1; k < n; ++k)
         if (f[bi] > f[k]) bi = k;
-      const double best = f[bi];
-      P.history[static_cast<size_t>(job) * c.max_generations + gen] = best;
-      if (P.metrics && P.eval_on[job]) {
-        // the generation's metrics: the best pose's and the mean DockQ as a
-        // left-to-right sum (src/commands/run.rs:388,449-451)
-        const gd_dock_metrics *M = P.metrics + static_cast<size_t>(job) * n;
-        const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;
-        P.best_metrics[jg] = M[bi];
-        double sum = 0.0;
-        for (int k = 0; k < n; ++k) sum += M[k].dockq;
-        P.mean_dockq[jg] = sum / static_cast<double>(n);
-      }
-      if (gen > 0) {  // convergence window (src/commands/run.rs:400-409)
-        const double imp = (st.last_best - best) / fabs(st.last_best);
-        if (imp < c.convergence_threshold) st.stagnant += 1;
-        else st.stagnant = 0;
-      }
-      st.last_best = best;
-      if (c.early_stopping && st.stagnant >= c.convergence_window) {
-        st.stop = 1;  // converged: this population is the final one
-        s_evolve = 0;
-      } else {
-        st.gen = gen + 1;
-        s_evolve = 1;
-      }
+    }
+    const double best = f[bi];
+    P.history[static_cast<size_t>(job) * c.max_generations + gen] = best;
+    if (P.metrics && P.eval_on[job]) {
+      // the generation's metrics: the best pose's and the mean DockQ as a
+      // left-to-right sum (src/commands/run.rs:388,449-451)
+      const gd_dock_metrics *M = P.metrics + static_cast<size_t>(job) * n;
+      const size_t jg = static_cast<size_t>(job) * c.max_generations + gen;
+      P.best_metrics[jg] = M[bi];
+      double sum = 0.0;
+      for (int k = 0; k < n; ++k) sum += M[k].dockq;
+      P.mean_dockq[jg] = sum / static_cast<double>(n);
+    }
+    if (gen > 0) {  // convergence window (src/commands/run.rs:400-409)
+      const double imp = (st.last_best - best) / fabs(st.last_best);
+      if (imp < c.convergence_threshold) st.stagnant += 1;
+      else st.stagnant = 0;
+    }
+    st.last_best = best;
+    if (c.early_stopping && st.stagnant >= c.convergence_window) {
+      st.stop = 1;  // converged: this population is the final one
+      s_evolve = 0;
+    } else {
+      st.gen = gen + 1;
+      s_evolve = 1;
     }
   }
   __syncthreads();
   if (!s_evolve && !s_hof) return;
   double *G = P.genes + static_cast<size_t>(job) * n * 6;
   const int ne = c.elitism < n ? c.elitism : n;
-  // stable ascending order of the evaluated population: the elites
-  // (src/population.rs:76-82) and the Hall of Fame's candidates
-  for (int k = tid; k < n; k += nt) {
-    const double fk = key_of(f[k]);
-    int r = 0;
-    for (int q = 0; q < n; ++q) {
-      const double fq = key_of(f[q]);
-      r += (fq < fk) || (fq == fk && q < k);
-    }
-    if (r < ne) elite[r] = k;
-    if (s_hof) order[r] = k;
-  }
-  __syncthreads();
   if (s_hof) hof_update(P, st, job, s_gen, G, f, order, s_csim, s_hnew, s_hctl, s_hpart, s_hf);
   if (!s_evolve) return;
   const int gen = st.gen - 1;  // draws of the generation being evolved
@@ -440,10 +488,12 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
     }
     sel[k] = best;
   }
+  // elites: the first ne of the stable order
+  for (int i = tid; i < ne * 6; i += nt) s_eg[i] = G[6 * order[i / 6] + i % 6];
   __syncthreads();
-  for (int i = tid; i < ne * 6; i += nt) s_eg[i] = G[6 * elite[i / 6] + i % 6];
   // shuffle + crossover + mutation (src/population.rs:88-107, src/ga.rs:7-39,
-  // src/chromosome.rs:56-77)
+  // src/chromosome.rs:56-77); the offspring's carried fitness goes straight
+  // into descending sort keys
   const double two_pi = 6.283185307179586;
   for (int p = tid; p < n / 2; p += nt) {
     const int a = sel[perm[2 * p]], b = sel[perm[2 * p + 1]];
@@ -467,22 +517,18 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
         T[6 * k + g] = o[h];
       }
     }
-    f2[2 * p] = f[a];
-    f2[2 * p + 1] = f[b];
+    kb[2 * p] = ~asc_key(f[a]);
+    kb[2 * p + 1] = ~asc_key(f[b]);
   }
+  for (int k = m + tid; k < P2; k += nt) kb[k] = ~0ull;
+  for (int k = tid; k < P2; k += nt) order[k] = k;
   __syncthreads();
   // stable descending order by the carried fitness; elites over the first
   // slots (src/population.rs:110-118)
-  for (int k = tid; k < m; k += nt) {
-    const double fk = key_of(f2[k]);
-    int r = 0;
-    for (int q = 0; q < m; ++q) {
-      const double fq = key_of(f2[q]);
-      r += (fq > fk) || (fq == fk && q < k);
-    }
-    if (r >= ne) {
-      for (int g = 0; g < 6; ++g) G[6 * r + g] = T[6 * k + g];
-    }
+  bitonic_sort(kb, order, P2);
+  for (int r = ne + tid; r < m; r += nt) {
+    const int k = order[r];
+    for (int g = 0; g < 6; ++g) G[6 * r + g] = T[6 * k + g];
   }
   for (int i = tid; i < ne * 6; i += nt) G[i] = s_eg[i];
 }
@@ -703,7 +749,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     P.mean_dockq = R.mean_dockq;
     P.cfg = c;
     P.cfg.hof_max_size = hcap;
-    const size_t ga_smem = sizeof(double) * (n + m) + sizeof(int) * (2 * n + 64);
+    const size_t ga_smem = ga_step_smem(n);
     cudaStream_t st = ctx->stream;
     auto generation = [&]() -> gd_status {
       const int total = static_cast<int>(jn);
@@ -1121,7 +1167,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
   P.hof = R.hof;
   P.hof_tmp = R.hof_tmp;
   P.cfg = c;
-  const size_t ga_smem = sizeof(double) * 2 * n + sizeof(int) * (2 * n + 64);
+  const size_t ga_smem = ga_step_smem(n);
   if (ga_smem > 48 * 1024)
     cudaFuncSetAttribute(k_ga_step, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ga_smem));
   k_ga_step<<<J, 256, ga_smem, st>>>(P);

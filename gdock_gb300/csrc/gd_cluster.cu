@@ -121,6 +121,7 @@ struct ContactParams {
 constexpr int kContactWarps = 8;
 constexpr int kLigBlock = 8;    // ligand residues per contact-bitmap work item
 constexpr int kCandMax = 1024;  // receptor residue candidates kept per block
+constexpr int kBlockAtoms = 128;  // ligand atoms of a block transformed in one pass (else residue by residue)
 
 __global__ void __launch_bounds__(kContactWarps * 32) k_contacts_rl(const ContactParams p) {
   __shared__ double s_xyz[kContactWarps][3][kMaxGroupAtoms];
@@ -310,8 +311,10 @@ struct BitsParams {
 // re-deciding in FP64 the atom pairs whose FP32 d2 is within the guard band
 // of the cutoff.
 __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsParams p) {
-  __shared__ double s_xyz[kContactWarps][3][kMaxGroupAtoms];
-  __shared__ float4 s_f[kContactWarps][kMaxGroupAtoms];
+  // FP32 images of the exact ligand coordinates: the whole block's atoms when
+  // they fit (one lane per atom, all residues at once), else one residue's
+  __shared__ float4 s_f[kContactWarps][kBlockAtoms];
+  __shared__ float4 s_ls[kContactWarps][kLigBlock + 1];  // residue spheres, then the block's (FP32 centre, radius)
   __shared__ uint16_t s_cand[kContactWarps][kCandMax];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nb = (p.GL + kLigBlock - 1) / kLigBlock;
@@ -319,21 +322,41 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
   for (long long it = static_cast<long long>(blockIdx.x) * kContactWarps + wib; it < items;
        it += static_cast<long long>(gridDim.x) * kContactWarps) {
     const int pose = static_cast<int>(it / nb), blk = static_cast<int>(it % nb);
-    const gd_pose_frame f = p.frames[pose];
+    // the frame is read where it is used (not held in registers across the item)
+    const gd_pose_frame &f = p.frames[pose];
+    const int lg0 = blk * kLigBlock, lg_end = min(p.GL, lg0 + kLigBlock);
+    // the FP64 transforms of the item in lane-parallel rounds (FP64 issues at
+    // a small fraction of the FP32 rate on this part): the residue spheres'
+    // and the block sphere's centres in one round, the block's atoms in
+    // rounds of 32
+    if (lane <= kLigBlock) {
+      const bool on = lane == kLigBlock || lg0 + lane < lg_end;
+      const D4 sp = lane == kLigBlock ? p.lb_sph[blk] : (on ? p.lg_sph[lg0 + lane] : D4{0.0, 0.0, 0.0, 0.0});
+      double X, Y, Z;
+      xform(f, p.cx, p.cy, p.cz, sp.x, sp.y, sp.z, X, Y, Z);
+      s_ls[wib][lane] = make_float4(static_cast<float>(X - p.ox), static_cast<float>(Y - p.oy),
+                                    static_cast<float>(Z - p.oz), static_cast<float>(sp.w));
+    }
+    const int A0 = p.lg_off[lg0], A1 = p.lg_off[lg_end];
+    const bool batched = A1 - A0 <= kBlockAtoms;
+    if (batched)
+      for (int a = lane; a < A1 - A0; a += 32) {
+        double X, Y, Z;
+        xform(f, p.cx, p.cy, p.cz, p.lx[A0 + a], p.ly[A0 + a], p.lz[A0 + a], X, Y, Z);
+        s_f[wib][a] = make_float4(static_cast<float>(X - p.ox), static_cast<float>(Y - p.oy),
+                                  static_cast<float>(Z - p.oz), 0.0f);
+      }
+    __syncwarp();
     int ncand = 0;
     {
-      const D4 bs = p.lb_sph[blk];
-      double BX, BY, BZ;
-      xform(f, p.cx, p.cy, p.cz, bs.x, bs.y, bs.z, BX, BY, BZ);
-      const float bcx = static_cast<float>(BX - p.ox), bcy = static_cast<float>(BY - p.oy),
-                  bcz = static_cast<float>(BZ - p.oz), brad = static_cast<float>(bs.w);
+      const float4 bs = s_ls[wib][kLigBlock];
       for (int r0 = 0; r0 < p.GR; r0 += 32) {
         const int rg = r0 + lane;
         bool near = false;
         if (rg < p.GR) {
           const float4 rs = p.rg_sph[rg];
-          const float dx = rs.x - bcx, dy = rs.y - bcy, dz = rs.z - bcz;
-          const float lim = rs.w + brad + p.reach;
+          const float dx = rs.x - bs.x, dy = rs.y - bs.y, dz = rs.z - bs.z;
+          const float lim = rs.w + bs.w + p.reach;
           near = dx * dx + dy * dy + dz * dz <= lim * lim;
         }
         const unsigned m = __ballot_sync(0xffffffffu, near);
@@ -345,27 +368,28 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
     }
     const bool every = ncand > kCandMax;  // list overflowed: scan every receptor residue
     const int nscan = every ? p.GR : ncand;
-    const int lg_end = min(p.GL, (blk + 1) * kLigBlock);
-    for (int lg = blk * kLigBlock; lg < lg_end; ++lg) {
+    for (int lg = lg0; lg < lg_end; ++lg) {
     const int a0 = p.lg_off[lg], na = min(p.lg_off[lg + 1] - a0, kMaxGroupAtoms);
-    for (int a = lane; a < na; a += 32) {
-      double X, Y, Z;
-      xform(f, p.cx, p.cy, p.cz, p.lx[a0 + a], p.ly[a0 + a], p.lz[a0 + a], X, Y, Z);
-      s_xyz[wib][0][a] = X;
-      s_xyz[wib][1][a] = Y;
-      s_xyz[wib][2][a] = Z;
-      s_f[wib][a] = make_float4(static_cast<float>(X - p.ox), static_cast<float>(Y - p.oy),
-                                static_cast<float>(Z - p.oz), 0.0f);
+    const float4 *laf = s_f[wib] + (batched ? a0 - A0 : 0);
+    if (!batched) {
+      for (int a = lane; a < na; a += 32) {
+        double X, Y, Z;
+        xform(f, p.cx, p.cy, p.cz, p.lx[a0 + a], p.ly[a0 + a], p.lz[a0 + a], X, Y, Z);
+        s_f[wib][a] = make_float4(static_cast<float>(X - p.ox), static_cast<float>(Y - p.oy),
+                                  static_cast<float>(Z - p.oz), 0.0f);
+      }
+      __syncwarp();
     }
-    __syncwarp();
-    const D4 ls = p.lg_sph[lg];
-    double CX, CY, CZ;
-    xform(f, p.cx, p.cy, p.cz, ls.x, ls.y, ls.z, CX, CY, CZ);
-    const float lcx = static_cast<float>(CX - p.ox), lcy = static_cast<float>(CY - p.oy),
-                lcz = static_cast<float>(CZ - p.oz);
-    const float lrad = static_cast<float>(ls.w);
+    const float4 ls = s_ls[wib][lg - lg0];
     const uint8_t lchain = p.lg_chain[lg];
     uint32_t *row = p.bits + static_cast<size_t>(pose) * p.words;
+    // exact re-decision of a pair in the guard band: the ligand atom moved in
+    // FP64 again (rare), the reference's distance order
+    auto exact_le = [&](int b, int a) {
+      double X, Y, Z;
+      xform(f, p.cx, p.cy, p.cz, p.lx[a0 + a], p.ly[a0 + a], p.lz[a0 + a], X, Y, Z);
+      return d2_exact(p.rx[b], p.ry[b], p.rz[b], X, Y, Z) <= p.t_le;
+    };
     // lanes split a residue pair's atom pairs: lane = (receptor atom step,
     // ligand atom a); na <= 32 gives per = 32 / na receptor atoms per round
     const int per = na <= 32 ? 32 / na : 1;
@@ -380,8 +404,8 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
         rg = every ? k : s_cand[wib][k];
         if (p.rg_chain[rg] != lchain) {
           const float4 rs = p.rg_sph[rg];
-          const float dx = rs.x - lcx, dy = rs.y - lcy, dz = rs.z - lcz;
-          const float lim = rs.w + lrad + p.reach;
+          const float dx = rs.x - ls.x, dy = rs.y - ls.y, dz = rs.z - ls.z;
+          const float lim = rs.w + ls.w + p.reach;
           near = dx * dx + dy * dy + dz * dz <= lim * lim;
         }
       }
@@ -400,12 +424,10 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
             bool hit = false;
             if (lane_on && b < b1) {
               const float4 rb = p.r32[b];
-              const float4 la = s_f[wib][my_a];
+              const float4 la = laf[my_a];
               const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
               const float d2 = ex * ex + ey * ey + ez * ez;
-              if (d2 <= p.t32 + p.guard)
-                hit = d2 < p.t32 - p.guard || d2_exact(p.rx[b], p.ry[b], p.rz[b], s_xyz[wib][0][my_a],
-                                                      s_xyz[wib][1][my_a], s_xyz[wib][2][my_a]) <= p.t_le;
+              if (d2 <= p.t32 + p.guard) hit = d2 < p.t32 - p.guard || exact_le(b, my_a);
             }
             found = __any_sync(0xffffffffu, hit);
           }
@@ -415,13 +437,10 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
             const float4 rb = p.r32[b];
             bool hit = false;
             for (int a = lane; a < na; a += 32) {
-              const float4 la = s_f[wib][a];
+              const float4 la = laf[a];
               const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
               const float d2 = ex * ex + ey * ey + ez * ez;
-              if (d2 <= p.t32 + p.guard)
-                hit = hit || d2 < p.t32 - p.guard ||
-                      d2_exact(p.rx[b], p.ry[b], p.rz[b], s_xyz[wib][0][a], s_xyz[wib][1][a], s_xyz[wib][2][a]) <=
-                          p.t_le;
+              if (d2 <= p.t32 + p.guard) hit = hit || d2 < p.t32 - p.guard || exact_le(b, a);
             }
             found = __any_sync(0xffffffffu, hit);
           }

@@ -425,6 +425,7 @@ uint64_t gd_context_bytes_in_use(const gd_context *ctx) { return ctx ? ctx->in_u
 
 gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms *lig, const int32_t *restraint_pairs,
                             int32_t n_pairs, const gd_weights *w, gd_complex **out) {
+  gd::NvtxRange nvtx_range("gd_complex_create");
   if (!ctx || !out) return GD_ERR_INVALID_ARG;
   *out = nullptr;
   if (!atoms_ok(rec) || !atoms_ok(lig)) return fail(ctx, GD_ERR_INVALID_ARG, "receptor/ligand arrays incomplete");
@@ -641,6 +642,7 @@ static double max_abs_disp(const double *genes, int n) {
 }
 
 gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_precision prec, gd_pose_energy *out) {
+  gd::NvtxRange nvtx_range("gd_score_poses");
   if (!cx) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   if (n < 0 || (n > 0 && (!genes || !out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad genes/out");
@@ -671,6 +673,7 @@ gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_prec
 
 gd_status gd_score_frames_device(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n, gd_precision prec,
                                  double max_displacement, gd_pose_energy *d_out, void *stream) {
+  gd::NvtxRange nvtx_range("gd_score_frames_device");
   if (!cx) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   if (n < 0 || (n > 0 && (!d_frames || !d_out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad frames/out");
@@ -683,6 +686,7 @@ gd_status gd_score_frames_device(gd_complex *cx, const gd_pose_frame *d_frames, 
 
 gd_status gd_autotune_f32(gd_complex *cx, const gd_pose_frame *d_frames, int32_t n, double max_displacement,
                           gd_pose_energy *d_out, void *stream, double *rates, int32_t *best) {
+  gd::NvtxRange nvtx_range("gd_autotune_f32");
   if (!cx) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   if (n <= 0 || !d_frames || !d_out) return fail(ctx, GD_ERR_INVALID_ARG, "bad frames/out");
@@ -736,6 +740,7 @@ gd_status gd_sync(gd_context *ctx) {
 
 gd_status gd_score_models(gd_complex *cx, const double *lig_xyz, int32_t n_models, gd_precision prec,
                           gd_pose_energy *out) {
+  gd::NvtxRange nvtx_range("gd_score_models");
   if (!cx) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   if (n_models < 0 || (n_models > 0 && (!lig_xyz || !out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad models/out");

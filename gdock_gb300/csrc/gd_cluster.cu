@@ -1126,6 +1126,7 @@ extern "C" {
 
 gd_status gd_pose_contacts(gd_complex *cx, const double *genes, int32_t n, int64_t *keys, int64_t cap,
                            int64_t *offsets) {
+  gd::NvtxRange nvtx_range("gd_pose_contacts");
   if (!cx) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   if (n < 0 || (n > 0 && (!genes || !offsets)) || cap < 0 || (cap > 0 && !keys))
@@ -1142,6 +1143,7 @@ gd_status gd_pose_contacts(gd_complex *cx, const double *genes, int32_t n, int64
 
 gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cluster_cfg *cfg, int32_t *n_clusters,
                      int32_t *centers, int32_t *sizes, int32_t *members) {
+  gd::NvtxRange nvtx_range("gd_cluster");
   if (!cx) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   if (n < 0 || (n > 0 && (!genes || !centers || !sizes || !members)) || !n_clusters)
@@ -1162,6 +1164,7 @@ gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cl
 gd_status gd_cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offsets, int32_t n,
                           const gd_cluster_cfg *cfg, int32_t *n_clusters, int32_t *centers, int32_t *sizes,
                           int32_t *members) {
+  gd::NvtxRange nvtx_range("gd_cluster_sets");
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (n < 0 || (n > 0 && (!offsets || !centers || !sizes || !members)) || !n_clusters)
     return fail(ctx, GD_ERR_INVALID_ARG, "bad cluster arguments");

@@ -145,6 +145,7 @@ extern "C" {
 
 gd_status gd_evaluator_create(gd_complex *cx, const gd_atoms *reference, const uint32_t *rec_names,
                               const uint32_t *lig_names, const uint32_t *ref_names, gd_evaluator **out) {
+  gd::NvtxRange nvtx_range("gd_evaluator_create");
   if (!cx || !reference || !out) return GD_ERR_INVALID_ARG;
   gd_context *ctx = cx->ctx;
   *out = nullptr;
@@ -293,6 +294,7 @@ gd_status gd_evaluate_frames_device(gd_evaluator *ev, const gd_pose_frame *d_fra
 }
 
 gd_status gd_evaluate_poses(gd_evaluator *ev, const double *genes, int32_t n, gd_dock_metrics *out) {
+  gd::NvtxRange nvtx_range("gd_evaluate_poses");
   if (!ev) return GD_ERR_INVALID_ARG;
   gd_context *ctx = ev->ctx;
   if (n < 0 || (n > 0 && (!genes || !out))) return fail(ctx, GD_ERR_INVALID_ARG, "bad genes/out");

@@ -603,6 +603,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
                                gd_precision prec, int32_t use_graph, double *out_genes, gd_pose_energy *out_energies,
                                int32_t *out_generations, double *out_history, gd_hof_entry *out_hof,
                                int32_t *out_hof_count, const gd_ga_metrics *metrics) {
+  gd::NvtxRange nvtx_range("gd_ga_run");
   using namespace gd;
   if (!ctx) return GD_ERR_INVALID_ARG;
   if (!complexes || jobs <= 0 || !cfg || !out_genes || !out_energies)
@@ -1054,6 +1055,7 @@ gd_status server_load_slot(gd_server *S, int j, Job *job) {
 
 // One tick: admit, run one generation of every resident job, retire.
 gd_status server_tick(gd_server *S, int *active_out) {
+  gd::NvtxRange nvtx_range("server_tick");
   gd_context *ctx = S->ctx;
   const gd_ga_cfg &c = S->cfg.ga;
   GaRun &R = S->arena;

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "gdock_gb300.h"
+#include <nvtx3/nvToolsExt.h>
 
 namespace gd {
 
@@ -156,6 +157,14 @@ namespace gd {
 // environment (off by default).
 bool trace_on();
 void trace(const char *phase, double seconds);
+// NVTX range over a scope, named after the ABI call or phase (seen by ncu and
+// nsys; without a tool attached a push/pop is a null-pointer check).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 gd_status fail(gd_context *ctx, gd_status s, const std::string &msg);
 gd_status cuda_fail(gd_context *ctx, cudaError_t e, const char *what);
 gd_status dev_alloc(gd_context *ctx, uint64_t bytes, void **p);

@@ -7,11 +7,15 @@ CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libgdock_gb300.so"
+LIB_DEBUG_PATH = Path(__file__).resolve().parent / "_build" / "libgdock_gb300_debug.so"
+# GD_LIBRARY=debug selects the debug variant (kernel index checks compiled in)
+DEBUG_LIBRARY = os.environ.get("GD_LIBRARY", "") == "debug"
 
 GD_OK, GD_ERR_INVALID_ARG, GD_ERR_OOM, GD_ERR_CUDA, GD_ERR_TIMEOUT, GD_ERR_CAPACITY, GD_ERR_STATE = range(7)
 GD_PREC_F64, GD_PREC_F32 = 0, 1
@@ -108,14 +112,15 @@ class GdError(RuntimeError):
         self.status = status
 
 
-def load(path: Path = LIB_PATH):
-    """Load the library (building it first if the build is missing or stale)."""
+def load(path: Path = None):
+    """Load the library (building it first if the build is missing or stale);
+    the debug variant when GD_LIBRARY=debug."""
     global _lib
     if _lib is not None:
         return _lib
     from . import build as _build
-    _build.build()
-    lib = C.CDLL(str(path))
+    _build.build(debug=DEBUG_LIBRARY)
+    lib = C.CDLL(str(path or (LIB_DEBUG_PATH if DEBUG_LIBRARY else LIB_PATH)))
     vp, i32, i64, d = C.c_void_p, C.c_int32, C.c_int64, C.c_double
     sigs = {
         "gd_abi_version": ([], i32),

@@ -108,6 +108,9 @@ gd_status check_device_error(gd_context *ctx) {
   cudaMemset(ctx->d_err, 0, sizeof(int));
   if (h == kDevTimeout) return fail(ctx, GD_ERR_TIMEOUT, "a device-side wait exceeded its spin limit");
   if (h == kDevCapacity) return fail(ctx, GD_ERR_CAPACITY, "a device-side buffer was too small");
+  if (h > kDevBoundsBase)
+    return fail(ctx, GD_ERR_CUDA, "device index check failed at site " + std::to_string(h - kDevBoundsBase) +
+                                      " (debug library)");
   return fail(ctx, GD_ERR_CUDA, "device error code " + std::to_string(h));
 }
 

@@ -300,6 +300,7 @@ struct BitsParams {
   float reach;
   uint32_t *bits;    // [n][words], bit rg*GL + lg
   long long words;
+  int *err;          // the context's error word (index checks of the debug library)
 };
 
 // One warp per (pose, block of kLigBlock consecutive ligand residues).  The
@@ -424,7 +425,7 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
             bool hit = false;
             if (lane_on && b < b1) {
               const float4 rb = p.r32[b];
-              const float4 la = laf[my_a];
+              const float4 la = laf[GD_DCHECK(p.err, laf + my_a < s_f[wib] + kBlockAtoms, 30) ? my_a : 0];
               const float ex = rb.x - la.x, ey = rb.y - la.y, ez = rb.z - la.z;
               const float d2 = ex * ex + ey * ey + ez * ez;
               if (d2 <= p.t32 + p.guard) hit = d2 < p.t32 - p.guard || exact_le(b, my_a);
@@ -447,7 +448,7 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
         }
         if (found && lane == 0) {
           const long long idx = static_cast<long long>(r) * p.GL + lg;
-          atomicOr(&row[idx >> 5], 1u << (idx & 31));
+          if (GD_DCHECK(p.err, (idx >> 5) < p.words, 31)) atomicOr(&row[idx >> 5], 1u << (idx & 31));
         }
       }
     }
@@ -1058,6 +1059,7 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   p.reach = static_cast<float>(cfg.contact_distance) + 0.05f;
   p.bits = d_bits;
   p.words = words;
+  p.err = ctx->d_err;
   if (pairs > 0 && n > 0) {
     const long long items = static_cast<long long>(n) * ((t->GL + kLigBlock - 1) / kLigBlock);
     const int grid = static_cast<int>(std::min<long long>((items + kContactWarps - 1) / kContactWarps,
@@ -1153,6 +1155,7 @@ gd_status gd_cluster(gd_complex *cx, const double *genes, int32_t n, const gd_cl
   if (n == 0) return GD_OK;  // cluster_structures on no structures
   cudaSetDevice(ctx->device);
   gd_status s = cluster_device(cx, genes, n, c, n_clusters, centers, sizes, members);
+  if (s == GD_OK) s = check_device_error(ctx);
   if (s != GD_ERR_STATE) return s;
   // multi-chain molecules or shared residues: contact keys on the host path
   std::vector<int64_t> k, o;

@@ -78,7 +78,9 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_dockq(const EvalParams e) {
   int common = 0;
   for (int u = lane; u < e.n_u; u += 32) {
     double X, Y, Z;
-    ligand_atom(e.p, f, pose, e.u_slot[u], X, Y, Z);
+    int slot = e.u_slot[u];
+    if (!GD_DCHECK(e.p.err, slot >= 0 && slot < e.p.nl, 40)) slot = 0;
+    ligand_atom(e.p, f, pose, slot, X, Y, Z);
     const D4 r = e.u_ref[u], q = e.u_iref[u];
     // ligand atom first, as atom1.distance_to(atom2) (src/evaluator.rs:96-100)
     if (r.w != 0.0) sl += sqrt(exact_d2(X, Y, Z, r.x, r.y, r.z));
@@ -315,7 +317,7 @@ gd_status gd_evaluate_poses(gd_evaluator *ev, const double *genes, int32_t n, gd
   e = cudaMemcpyAsync(out, d_out, ob, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "evaluator");
-  return GD_OK;
+  return check_device_error(ctx);
 }
 
 }  // extern "C"

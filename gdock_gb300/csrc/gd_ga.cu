@@ -142,6 +142,7 @@ struct GaStepParams {
   const int *eval_on;              // [jobs] 1 = the job has an evaluator
   gd_dock_metrics *best_metrics;   // [jobs][max_gen]
   double *mean_dockq;              // [jobs][max_gen]
+  int *err;                        // the context's error word (index checks of the debug library)
   gd_ga_cfg cfg;
 };
 
@@ -264,7 +265,7 @@ __device__ void hof_update(const GaStepParams &P, GaJobState &st, int job, int g
         for (int i = 0; i < 6; ++i) g[i] = gp[i];
         const bool sim = lane < n_new && hof_similar(g, s_new + 6 * lane);
         if (__any_sync(kFull, sim)) continue;
-        if (lane == 0) {
+        if (lane == 0 && GD_DCHECK(P.err, cnt <= cap, 50)) {
           gd_hof_entry &x = H[cnt];
 #pragma unroll
           for (int i = 0; i < 6; ++i) {
@@ -286,7 +287,10 @@ __device__ void hof_update(const GaStepParams &P, GaJobState &st, int job, int g
             for (int e = lane; e < cnt - 1; e += 32) pos += key_of(H[e].fitness) <= fn;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) pos += __shfl_xor_sync(kFull, pos, o);
-            for (int e = lane; e < cnt; e += 32) T[e < pos ? e : (e == cnt - 1 ? pos : e + 1)] = H[e];
+            for (int e = lane; e < cnt; e += 32) {
+              const int d = e < pos ? e : (e == cnt - 1 ? pos : e + 1);
+              if (GD_DCHECK(P.err, d >= 0 && d <= cap, 51)) T[d] = H[e];
+            }
           } else {
             for (int e = lane; e < cnt; e += 32) {
               const double fe = key_of(H[e].fitness);
@@ -528,6 +532,7 @@ __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   bitonic_sort(kb, order, P2);
   for (int r = ne + tid; r < m; r += nt) {
     const int k = order[r];
+    if (!GD_DCHECK(P.err, k >= 0 && k < m, 52)) continue;
     for (int g = 0; g < 6; ++g) G[6 * r + g] = T[6 * k + g];
   }
   for (int i = tid; i < ne * 6; i += nt) G[i] = s_eg[i];
@@ -748,6 +753,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     P.eval_on = R.eval_on;
     P.best_metrics = R.best_metrics;
     P.mean_dockq = R.mean_dockq;
+    P.err = ctx->d_err;
     P.cfg = c;
     P.cfg.hof_max_size = hcap;
     const size_t ga_smem = ga_step_smem(n);
@@ -1168,6 +1174,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
   P.mut_z = R.mut_z;
   P.hof = R.hof;
   P.hof_tmp = R.hof_tmp;
+  P.err = ctx->d_err;
   P.cfg = c;
   const size_t ga_smem = ga_step_smem(n);
   if (ga_smem > 48 * 1024)

@@ -30,7 +30,17 @@ constexpr int kMaxTypes = 64;
 constexpr int kDefaultF32Tune = 256 + 64 + 4;
 
 // device error codes written to the context's error word
-enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2 };
+enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2, kDevBoundsBase = 1000 };
+// Index checks of the library's debug variant (built with -DGD_DEBUG_CHECKS:
+// libgdock_gb300_debug.so).  A failed check records kDevBoundsBase + site in
+// the context's error word (the first failure stays) and the caller skips or
+// clamps the access; the call then reports the site.  In the release library
+// every check is the constant true.
+#ifdef GD_DEBUG_CHECKS
+#define GD_DCHECK(errp, cond, site) ((cond) || (atomicCAS((errp), 0, kDevBoundsBase + (site)), false))
+#else
+#define GD_DCHECK(errp, cond, site) true
+#endif
 
 // Per-job state of the device GA (the reference loop's counters,
 // src/commands/run.rs:371-425).  stop: 0 running, 1 converged, 2 done.

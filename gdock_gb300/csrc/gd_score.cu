@@ -138,6 +138,7 @@ __global__ void __launch_bounds__(NT) k_score_f64(const ScoreParams p) {
           ligand_atom(p, f, pose, j, lx[s], ly[s], lz[s]);
           lq[s] = p.lig_q[j];
           lt[s] = p.lig_type[j];
+          if (!GD_DCHECK(p.err, lt[s] >= 0 && lt[s] < p.nt, 22)) lt[s] = 0;
           lser[s] = SERIAL ? p.lig_serial[j] : 0;
         } else {
           lx[s] = ly[s] = lz[s] = 1.0e30;
@@ -154,7 +155,8 @@ __global__ void __launch_bounds__(NT) k_score_f64(const ScoreParams p) {
         if (ok) {
           for (int a = 0; a < cnt; ++a) {
             const D4 r = s_pos[st * kTile + a];
-            const int2 m = s_meta[st * kTile + a];
+            int2 m = s_meta[st * kTile + a];
+            if (!GD_DCHECK(p.err, m.x >= 0 && m.x + p.nt <= p.nt * p.nt, 20)) m.x = 0;
             int rc = 0;
 #pragma unroll
             for (int s = 0; s < S; ++s) {
@@ -182,7 +184,8 @@ __global__ void __launch_bounds__(NT) k_score_f64(const ScoreParams p) {
               rc += pd;
             }
             const int tot = __reduce_add_sync(kFull, rc);
-            if (lane == 0 && tot) atomicAdd(&s_rcnt[base + a], static_cast<uint32_t>(tot));
+            if (lane == 0 && tot && GD_DCHECK(p.err, base + a < p.nr, 21))
+              atomicAdd(&s_rcnt[base + a], static_cast<uint32_t>(tot));
           }
         }
         if (__syncthreads_or(!ok)) {

@@ -354,6 +354,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           lz[s] = static_cast<float>(Z - p.oz);
           lq[s] = static_cast<float>(p.lig_q[j]);
           lt[s] = p.lig_type[j];
+          if (!GD_DCHECK(bp.err, lt[s] >= 0 && lt[s] < p.nt, 6)) lt[s] = 0;
           lser[s] = SERIAL ? p.lig_serial[j] : 0;
         } else {
           // far from every receptor atom, including the padding at +1e9
@@ -447,12 +448,14 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           const uint16_t idx = static_cast<uint16_t>(sbase + b0 + my_a);
           // at most na <= kSeg rows per slot: far rows fill [0, nf), near rows
           // (kList - nn, kList - 1], with room for both paddings in between
-          if (keep && !nearr) my_list[nf_mine + __popc(Mf & my_group & lt_mask)] = idx;
-          if (keep && nearr) my_list[kList - 1 - nn_mine - __popc(Mn & my_group & lt_mask)] = idx;
+          const int pf = nf_mine + __popc(Mf & my_group & lt_mask), pn = kList - 1 - nn_mine - __popc(Mn & my_group & lt_mask);
+          if (keep && !nearr && GD_DCHECK(bp.err, pf >= 0 && pf < kList, 1)) my_list[pf] = idx;
+          if (keep && nearr && GD_DCHECK(bp.err, pn >= 0 && pn < kList, 2)) my_list[pn] = idx;
           nf_mine += __popc(Mf & my_group);
           nn_mine += __popc(Mn & my_group);
         }
-        if (my_s < S && my_a < kAtoms) {
+        if (my_s < S && my_a < kAtoms &&
+            GD_DCHECK(bp.err, nf_mine + my_a < kList && kList - 1 - nn_mine - my_a >= 0, 3)) {
           my_list[nf_mine + my_a] = static_cast<uint16_t>(kFar);
           my_list[kList - 1 - nn_mine - my_a] = static_cast<uint16_t>(kFar);
         }
@@ -473,13 +476,15 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
               ix[i] = lst[k0 + i];
+              if (!GD_DCHECK(bp.err, ix[i] <= kFar, 4)) ix[i] = kFar;
               r[i] = s_pos[ix[i]];
             }
             bool amb = false;
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) pair32_elec(r[i], lx[s], ly[s], lz[s], ge, aes, amb);
             if (__any_sync(kFull, amb)) {  // at most one entry per step: <= 4 * 18 per segment
-              if (lane == 0) s_fixq[seg_cnt >> 16] = static_cast<uint16_t>(k0 | (s << 8));
+              if (lane == 0 && GD_DCHECK(bp.err, (seg_cnt >> 16) < kMaxS * kList, 7))
+                s_fixq[seg_cnt >> 16] = static_cast<uint16_t>(k0 | (s << 8));
               seg_cnt += 1 << 16;
             }
           }
@@ -492,9 +497,11 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
               ix[i] = lst[k0 + i];
+              if (!GD_DCHECK(bp.err, ix[i] <= kFar, 4)) ix[i] = kFar;
               r[i] = s_pos[ix[i]];
               const int2 mt = s_meta[ix[i]];
               rt[i] = mt.x;
+              if (!GD_DCHECK(bp.err, rt[i] >= 0 && rt[i] + lt[s] < p.nt * p.nt, 5)) rt[i] = 0;
               rs[i] = mt.y;
               rc[i] = 0;
             }
@@ -504,7 +511,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
               pair32<SERIAL, CLAMP>(r[i], rt[i], rs[i], tab, lx[s], ly[s], lz[s], lt[s], lser[s], gv, ge, gdd, av,
                                     aes, lcnt[s], rc[i], amb);
             if (__any_sync(kFull, amb)) {  // at most one entry per step: <= 4 * 18 per segment
-              if (lane == 0) s_fixq[seg_cnt >> 16] = static_cast<uint16_t>(k0 | (s << 8));
+              if (lane == 0 && GD_DCHECK(bp.err, (seg_cnt >> 16) < kMaxS * kList, 7))
+                s_fixq[seg_cnt >> 16] = static_cast<uint16_t>(k0 | (s << 8));
               seg_cnt += 1 << 16;
             }
             // receptor burial counts of the step's rows: their ballots are
@@ -512,7 +520,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 #pragma unroll
             for (int i = 0; i < kAtoms; ++i) {
               const unsigned bm = __ballot_sync(kFull, rc[i] != 0);
-              if (lane == i) {
+              if (lane == i && GD_DCHECK(bp.err, (seg_cnt & 0xffff) + i < kMaxS * kList, 8)) {
                 s_cmask[(seg_cnt & 0xffff) + i] = bm;
                 s_cidx[(seg_cnt & 0xffff) + i] = static_cast<uint16_t>(ix[i]);
               }
@@ -539,7 +547,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 #pragma unroll 1
           for (int i = 0; i < kAtoms; ++i) {
             const int ixi = s_list[s * kList + k0 + i];
-            if (ixi == kFar) continue;
+            if (ixi == kFar || !GD_DCHECK(bp.err, ixi < kFar, 4)) continue;
             const float4 ri = s_pos[ixi];
             if (!near_band(d2f(ri, fx, fy, fz), gv, ge, gdd)) continue;
             const int2 mt = s_meta[ixi];
@@ -566,7 +574,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         for (int i = lane; i < na; i += 32) {
           const int c = s_rc[i];
           if (c) {
-            if (SPLIT) atomicAdd(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + gbase + i], static_cast<unsigned>(c));
+            if (SPLIT) {
+              if (GD_DCHECK(bp.err, gbase + i < bp.max_nr, 10))
+                atomicAdd(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + gbase + i], static_cast<unsigned>(c));
+            }
             else bump_count(cnt, gbase + i, c);
             s_rc[i] = 0;
           }
@@ -591,6 +602,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       const double vch = static_cast<double>(sv) - static_cast<double>(cv);
       const double ech = static_cast<double>(se) - static_cast<double>(ce);
       if (SPLIT) {
+        if (!GD_DCHECK(bp.err, ch < bp.max_chunks, 9)) break;
         double *pt = bp.part + (static_cast<size_t>(gp) * bp.max_chunks + ch) * 96;
         pt[lane] = vch;
         pt[32 + lane] = ech;

@@ -52,3 +52,14 @@ def test_context_without_gpu_fails_loudly():
         pass
     with pytest.raises(_lib.GdError):
         _lib.Context(0)
+
+
+def test_debug_library_builds_and_exports_all_symbols():
+    # the debug variant: the same sources with the kernels' index checks
+    # compiled in (-DGD_DEBUG_CHECKS)
+    path = build.build(debug=True)
+    assert path.name == "libgdock_gb300_debug.so"
+    lib = ctypes.CDLL(str(path))
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert lib.gd_abi_version() == 1

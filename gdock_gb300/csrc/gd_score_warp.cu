@@ -136,6 +136,11 @@ __device__ __forceinline__ void issue_seg(long long q, int seg, const ScoreParam
 }
 
 // acc += v when |t| < lim (one predicated add)
+// acc += v when t < 0
+__device__ __forceinline__ void add_if_lt0(float &acc, float t, float v) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, 0f00000000;\n\t@p add.f32 %0, %0, %2;\n\t}" : "+f"(acc)
+      : "f"(t), "f"(v));
+}
 __device__ __forceinline__ void add_if_abs_lt(float &acc, float t, float lim, float v) {
   asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, %2;\n\t@p add.f32 %0, %0, %3;\n\t}" : "+f"(acc)
       : "f"(fabsf(t)), "f"(lim), "f"(v));
@@ -153,36 +158,40 @@ __device__ __forceinline__ float d2f(const float4 &r, float lx, float ly, float 
 }
 
 // soft-core LJ in FP32 (src/fitness.rs:57-70): eps*(q^2 - 2q) with
-// q = R6/(r^6 + R6/2), evaluated as 4 eps x (x - 1), x = q/2 = 1/(r^6 2/R6 + 1)
+// q = R6/(r^6 + R6/2), evaluated as 4 eps x (x - 1) = 4 eps (x^2 - x),
+// x = q/2 = 1/(r^6 2/R6 + 1); at d2 = 0 it is exactly 0
 template <bool CLAMP>
 __device__ __forceinline__ float vdw_term(float d2, float2 tp) {
   const float r6 = d2 * d2 * d2;
   const float x = rcp_approx(__fmaf_rn(r6, tp.x, 1.0f));
-  float v = (x * (x - 1.0f)) * tp.y;
+  float v = __fmaf_rn(x, x, -x) * tp.y;
   if (CLAMP) v = v < -50.0f ? -50.0f : (v > 500.0f ? 500.0f : v);
   return v;
 }
 
 // One pair's FP32 terms.  The Coulomb sum accumulates q_r / d2 (scaled by
-// the lane's ligand charge once per segment).
+// the lane's ligand charge once per segment).  The vdW decision is d2 < 144
+// alone: the reference's 0 < r excludes only coincident atoms, whose FP32
+// d2 is then exactly 0 too (the FP32 coordinates are roundings of the same
+// doubles) and whose FP32 term is exactly 0, so the sums are unchanged; the
+// guard band of the vdW cutoff is the one at 144.
 template <bool SERIAL, bool CLAMP>
 __device__ __forceinline__ void pair32(const float4 &r, int rtrow, int rser, const float2 *tab, float lx, float ly,
                                        float lz, int lt, int lser, float gv, float ge, float gdd, float &av,
                                        float &ae, int &lc, int &rc, bool &amb) {
   const float d2 = d2f(r, lx, ly, lz);
   const float v = vdw_term<CLAMP>(d2, __ldg(&tab[rtrow + lt]));
-  const float tv = __fsub_rn(d2, 72.0f);  // 0 < d2 < 144  <=>  |tv| < 72
+  const float tv = __fsub_rn(d2, 144.0f);  // d2 < 144  <=>  tv < 0
   if (SERIAL) {
-    av += (fabsf(tv) < 72.0f && rser != lser) ? v : 0.0f;
+    av += (tv < 0.0f && rser != lser) ? v : 0.0f;
   } else {
-    add_if_abs_lt(av, tv, 72.0f, v);
+    add_if_lt0(av, tv, v);
   }
   const float e = r.w * rcp_approx(d2);
   const float te = __fsub_rn(d2, 113.0f);  // 1 < d2 < 225  <=>  |te| < 112
   add_if_abs_lt(ae, te, 112.0f, e);
   count_if_lt64(lc, rc, d2);
-  amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < gv) |
-        (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
+  amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(tv) < gv) | (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
 }
 
 // One pair of a far row (no pair within the vdW cutoff): Coulomb only, the
@@ -197,9 +206,8 @@ __device__ __forceinline__ void pair32_elec(const float4 &r, float lx, float ly,
 }
 
 __device__ __forceinline__ bool near_band(float d2, float gv, float ge, float gdd) {
-  const float tv = __fsub_rn(d2, 72.0f), te = __fsub_rn(d2, 113.0f);
-  return (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(__fsub_rn(fabsf(tv), 72.0f)) < gv) |
-         (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
+  const float tv = __fsub_rn(d2, 144.0f), te = __fsub_rn(d2, 113.0f);
+  return (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(tv) < gv) | (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
 }
 
 // Corrections of one pair's FP32 contributions after its FP64 re-decision.
@@ -216,9 +224,8 @@ __device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, double X, doubl
                                         int rtrow, int rser, float lx, float ly, float lz, float lq, int lt, int lser) {
   FixOut o{0.0f, 0.0f, 0};
   const float d2 = d2f(r, lx, ly, lz);
-  const float tv = __fsub_rn(d2, 72.0f);
   const float te = __fsub_rn(d2, 113.0f);
-  bool pv32 = fabsf(tv) < 72.0f;
+  bool pv32 = __fsub_rn(d2, 144.0f) < 0.0f;
   if (SERIAL) pv32 = pv32 && (rser != lser);
   const bool pe32 = fabsf(te) < 112.0f;
   const bool pd32 = d2 < 64.0f;

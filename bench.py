@@ -352,6 +352,21 @@ def run_c3(args):
     t_fcc = time.perf_counter() - t0
     # plain FP64 GA on a sample of 4 jobs x 2 generations, per pair
     dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, jobs[:4], pop, 2)
+    # CPU leg: the oracle scoring one generation (pop poses) of 4 of the jobs
+    # on all host threads, extrapolated to the 64 jobs x (G + 1) evaluations
+    # (the GA's own steps are a negligible part of a CPU dock)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    from gdock_gb300 import synth
+    g0 = synth.random_genes(np.random.default_rng(3), pop)
+    t0 = time.perf_counter()
+    for r, l, p in jobs[:4]:
+        oracle.score_poses(r, l, p, g0, nthreads=threads)
+    t_gen = (time.perf_counter() - t0) / 4
+    pair_frac = sum(len(r) * len(l) for r, l, _ in jobs) / (16 * sum(len(r) * len(l) for r, l, _ in jobs[:4]))
+    cpu_docks = 1.0 / (t_gen * (G + 1) * pair_frac)
     line = {"metric": "docks/s (batched uneven GA, 64 complexes, pop 150, 50 generations, CUDA graphs)",
             "value": len(jobs) / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": 1,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -366,7 +381,10 @@ def run_c3(args):
                                "hall_of_fame_entries": int(sum(len(h) for h in res.hall_of_fame))},
             "autotune": tuned,
             "plain_fp64_pair_evals_per_s": pairs64 / dt64,
-            "f32_batched_over_plain_f64": (pairs / t) / (pairs64 / dt64)}
+            "f32_batched_over_plain_f64": (pairs / t) / (pairs64 / dt64),
+            "cpu_baseline": {"value": cpu_docks, "unit": "docks/s", "cores": threads, "kind": "port",
+                             "sample": "the oracle scoring one generation (150 poses) of 4 of the 64 complexes, "
+                                       "extrapolated by pair count to 64 docks x 51 evaluations"}}
     print(json.dumps(line), flush=True)
 
 
@@ -455,6 +473,14 @@ def run_c5(args):
     t_general = time.perf_counter() - t0
     same = [(r.center_idx, r.members) for r in clusters] == [(r.center_idx, r.members) for r in general]
     pairs = len(c.receptor) * len(lig) * 4096 * (G + 1)
+    # CPU leg: the oracle on 4 poses of the final population, all host threads
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.score_poses(c.receptor, lig, c.restraint_pairs, res.genes[0][:4], nthreads=threads)
+    cpu_pps = 4 / (time.perf_counter() - t0)
     line = {"metric": "poses/s (large complex GA, pop 4096) and FCC clustering time over 4096 poses",
             "value": 4096 * (G + 1) / t_ga, "unit": "poses/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": t_ga * 1e3 / (G + 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -466,7 +492,9 @@ def run_c5(args):
             "fcc": {"poses": 4096, "seconds": t_fcc, "fcc_pairs_per_s": 4096 * 4096 / t_fcc,
                     "clusters": len(clusters), "same_as_general_path": same,
                     "general_path_seconds": t_general},
-            "autotune": tuned}
+            "autotune": tuned,
+            "cpu_baseline": {"value": cpu_pps, "unit": "poses/s", "cores": threads, "kind": "port",
+                             "sample": "the oracle scoring 4 poses of the final population"}}
     print(json.dumps(line), flush=True)
 
 

@@ -435,6 +435,22 @@ def run_c4(args):
         t64.append(time.perf_counter() - t0)
         cx64.close()
     dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, pool[:2], 150, 3)
+    # CPU leg: the oracle scoring one generation (150 poses) of 4 of the pool's
+    # complexes on all host threads, times the served jobs' mean generations
+    # (+1 evaluation), one job after another
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    from gdock_gb300 import synth
+    g0 = synth.random_genes(np.random.default_rng(4), 150)
+    t0 = time.perf_counter()
+    for r, l, p in pool[:4]:
+        oracle.score_poses(r, l, p, g0, nthreads=threads)
+    t_gen = (time.perf_counter() - t0) / 4
+    pair_frac = sum(len(r) * len(l) for r, l, _ in pool) / (len(pool) / 4 * sum(len(r) * len(l) for r, l, _ in pool[:4]))
+    mean_gens = float(np.mean([x["mean_generations"] for x in sweep]))
+    cpu_jobs = 1.0 / (t_gen * pair_frac * (mean_gens + 1))
     best = max(sweep, key=lambda x: x["jobs_per_s"])
     line = {"metric": "served docking jobs/s with p50/p99 latency (continuous batching)",
             "value": best["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
@@ -445,7 +461,10 @@ def run_c4(args):
                                    "stopping after 10 stagnant generations, cap 200", "slots": 64},
             "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64,
             "plain_fp64_one_job_at_a_time": {"jobs": len(t64), "seconds_per_job": float(np.mean(t64)),
-                                             "jobs_per_s": len(t64) / float(np.sum(t64))}}
+                                             "jobs_per_s": len(t64) / float(np.sum(t64))},
+            "cpu_baseline": {"value": cpu_jobs, "unit": "jobs/s", "cores": threads, "kind": "port",
+                             "sample": "the oracle scoring one generation (150 poses) of 4 of the 48 complexes, "
+                                       "extrapolated by pair count and the served jobs' mean generations"}}
     print(json.dumps(line), flush=True)
 
 

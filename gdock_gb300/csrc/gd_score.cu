@@ -1,29 +1,20 @@
-// Population fitness kernels: pose transform + all-pairs receptor x ligand
-// soft-core LJ, Coulomb (epsilon = r), desolvation burial counts and the AIR
-// restraint term, one pose per CTA iteration of a persistent grid.
+// The plain FP64 scoring kernel (the correctness form) and the per-call
+// scoring set-up shared with the FP32 form (gd_score_warp.cu): the
+// parameter block of a complex and the dispatch by precision.
 //
 // Reference arithmetic (gdock): transform src/structure.rs:80-131 and
 // src/chromosome.rs:79-83; energies src/fitness.rs:57-302; per-pose
 // combination src/chromosome.rs:110-127.
 //
-// Layout.  Receptor atoms are streamed through shared memory in tiles of
-// kTile atoms by bulk (TMA) copies into a kStages-deep ring guarded by
-// mbarriers; the receptor stream is the same for every pose, so the ring runs
+// k_score_f64: one pose per CTA iteration of a persistent grid.  Receptor
+// atoms are streamed through shared memory in tiles of kTile atoms by bulk
+// (TMA) copies into a kStages-deep ring guarded by mbarriers with bounded
+// waits; the receptor stream is the same for every pose, so the ring runs
 // continuously across the poses a CTA owns.  Each thread holds S ligand atoms
-// of the current pose ("slots", atoms tid, tid+NT, ... of the chunk) in
-// registers after transforming them in FP64 with the reference's operation
-// order, so coordinates are bit-identical to gdock's.  Ligands longer than
-// NT*S atoms are processed in chunks, each streaming the whole receptor.
-//
-// FP32 form: per-pair terms in FP32, partial sums per receptor tile folded
-// into per-thread Kahan accumulators, FP64 per-pose reduction.  Every cutoff
-// decision is made on d2 against the FP32 image of the cutoff; pairs whose
-// FP32 d2 lies within a guard band of a discontinuous cutoff (1, 8, 12,
-// 15 A) are re-decided in FP64 from the exact coordinates and the FP32
-// contribution corrected, so that all decisions equal the FP64 ones.
-//
-// FP64 form: the plain method, FP64 throughout, decisions against exact
-// thresholds on d2.
+// of the current pose (atoms tid, tid+NT, ... of the chunk) in registers
+// after transforming them in FP64 with the reference's operation order, so
+// coordinates are bit-identical to gdock's.  Every pair is evaluated in FP64
+// (no culling), with decisions against exact thresholds on d2.
 #include <algorithm>
 #include <cmath>
 

@@ -14,9 +14,10 @@
 //
 // Per generation, for all jobs: pose frames from genes (device sin/cos),
 // batched scoring (the persistent FP32 kernel, or the plain FP64 kernel per
-// job), then one CTA per job runs the convergence bookkeeping of the
-// reference loop and, unless the job stopped, evolve.  One generation is
-// captured as a CUDA graph and replayed.
+// job), optionally the DockQ metrics of every pose (gd_eval.cu), then one CTA
+// per job runs the convergence bookkeeping of the reference loop, the Hall
+// of Fame (src/commands/run.rs:75-215,385) and, unless the job stopped,
+// evolve.  One generation is captured as a CUDA graph and replayed.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

@@ -518,6 +518,9 @@ def run_c5(args):
 
 
 EVAL_FLOP = {"transform": 28, "distance": 10, "contact": 9}  # FP64 flop convention of the DockQ kernel
+# DRAM bytes per pose of k_dockq: 1.223 MB read + 0 written over one
+# 8,192-pose ncu capture of this workload (profiles/k_dockq_single_complex.md)
+DOCKQ_TRAFFIC_PER_POSE = 1.223424e6 / 8192
 
 
 def run_dockq(args):
@@ -598,7 +601,9 @@ def run_dockq(args):
                     "same_as_device_path": same},
             "gpu_launches": args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64"], "unit": "TFLOP/s",
-                         "frac": achieved / peaks["fp64"], "traffic": None,
+                         "frac": achieved / peaks["fp64"], "traffic": DOCKQ_TRAFFIC_PER_POSE * NP,
+                         "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
+                                           "(8,192 poses), scaled per pose",
                          "peak_source": "cuBLAS DGEMM measured in this run",
                          "flop_per_pose": flop, "flop_convention": EVAL_FLOP},
             "max_rel_error_vs_oracle": {k: float(err[:, i].max()) for i, k in

@@ -655,7 +655,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
   for (int j = 0; j < jobs; ++j)
     for (int k = 0; k < n; ++k) h_job[static_cast<size_t>(j) * n + k] = j;
   std::vector<GaJobState> h_state(jobs);
-  for (auto &s : h_state) s = GaJobState{0, 0, 0, 0, 1.7976931348623157e308};
+  for (auto &s : h_state) s = GaJobState{0, 0, 0, 0, 1.7976931348623157e308, 0, 0};
 
   auto up = [&](const void *src, size_t bytes, void **dst) -> gd_status {
     gd_status s = ga_alloc(ctx, R, std::max<size_t>(bytes, 16), dst);
@@ -998,7 +998,7 @@ gd_status server_alloc(gd_server *S) {
   }
   std::vector<int> job_of(jn);
   for (size_t k = 0; k < jn; ++k) job_of[k] = static_cast<int>(k / n);
-  std::vector<GaJobState> st(J, GaJobState{0, kStopFree, 0, 0, 0.0});
+  std::vector<GaJobState> st(J, GaJobState{0, kStopFree, 0, 0, 0.0, 0, 0});
   cudaError_t e = cudaMemcpy(R.job_of, job_of.data(), sizeof(int) * jn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(R.state, st.data(), sizeof(GaJobState) * J, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "server arena");
@@ -1047,7 +1047,7 @@ gd_status server_load_slot(gd_server *S, int j, Job *job) {
       e = cudaMemcpyAsync(R.mut_z + j * Gs * gM, job->d_mz.data(), sizeof(double) * gM * Gs, cudaMemcpyHostToDevice,
                           st);
   }
-  GaJobState s0{0, 0, 0, 0, 1.7976931348623157e308};
+  GaJobState s0{0, 0, 0, 0, 1.7976931348623157e308, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpyAsync(R.state + j, &s0, sizeof(s0), cudaMemcpyHostToDevice, st);
   // pageable sources: staged before the calls return, so the host draws can go
   if (e != cudaSuccess) return cuda_fail(S->ctx, e, "server slot upload");
@@ -1212,7 +1212,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
     if (e == cudaSuccess && !job->hof.empty())
       e = cudaMemcpy(job->hof.data(), R.hof + static_cast<size_t>(j) * (c.hof_max_size + 1),
                      sizeof(gd_hof_entry) * job->hof.size(), cudaMemcpyDeviceToHost);
-    GaJobState freed{0, kStopFree, 0, 0, 0.0};
+    GaJobState freed{0, kStopFree, 0, 0, 0.0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpy(R.state + j, &freed, sizeof(freed), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "server retire");
     const uint64_t before = ctx->in_use;

@@ -38,6 +38,7 @@ GD_JOB_QUEUED, GD_JOB_RUNNING, GD_JOB_DONE, GD_JOB_FAILED = range(4)
 GD_TUNE_F32_SLOTS = 0
 GD_TUNE_SPLIT = 1
 GD_TUNE_FAULT = 2
+GD_TUNE_FCC = 3
 
 
 class GdAtoms(C.Structure):

@@ -413,6 +413,12 @@ gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
     ctx->tune_fault = value;
     return GD_OK;
   }
+  if (knob == GD_TUNE_FCC) {
+    if (value < 0 || value > 2)
+      return fail(ctx, GD_ERR_INVALID_ARG, "FCC tuning: 0 (automatic), 1 (bitsets), 2 (contact postings)");
+    ctx->tune_fcc = value;
+    return GD_OK;
+  }
   return fail(ctx, GD_ERR_INVALID_ARG, "unknown tuning knob");
 }
 
@@ -421,6 +427,7 @@ int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob) {
   if (knob == GD_TUNE_F32_SLOTS) return ctx->tune_f32_slots;
   if (knob == GD_TUNE_SPLIT) return ctx->tune_split;
   if (knob == GD_TUNE_FAULT) return ctx->tune_fault;
+  if (knob == GD_TUNE_FCC) return ctx->tune_fcc;
   return -1;
 }
 

@@ -516,6 +516,104 @@ __global__ void k_compact(const uint32_t *bits, const uint32_t *ubits, const int
   }
 }
 
+// ---- FCC pair counts from per-contact pose lists ("postings") ----
+// For poses whose contacts are spread (few poses per contact), the common
+// count of a pose pair is the number of contacts whose list holds both: the
+// work is the sum over contacts of k (k - 1) / 2 for k poses per contact,
+// against n^2 / 2 pose pairs x W words for the bitsets.  Counts are exact
+// integers either way, so the clusters are identical.
+
+// Per contact (compacted index): how many poses make it; per pose: its size.
+__global__ void k_post_count(const uint32_t *bits, const uint32_t *ubits, const int *base, int n, long long words,
+                             int *kc, int *sizes) {
+  for (long long it = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; it < static_cast<long long>(n) * words;
+       it += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int p = static_cast<int>(it / words);
+    const long long w = it % words;
+    const uint32_t u = ubits[w];
+    if (!u) continue;
+    uint32_t v = bits[static_cast<size_t>(p) * words + w] & u;
+    if (!v) continue;
+    atomicAdd(&sizes[p], __popc(v));
+    while (v) {
+      const int b = __ffs(v) - 1;
+      v &= v - 1;
+      atomicAdd(&kc[base[w] + __popc(u & ((1u << b) - 1u))], 1);
+    }
+  }
+}
+
+// Sum over contacts of k (k - 1) / 2: the pair increments of the posting path.
+__global__ void k_post_work(const int *kc, int U, unsigned long long *sum) {
+  unsigned long long acc = 0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < U; c += gridDim.x * blockDim.x) {
+    const unsigned long long k = static_cast<unsigned long long>(kc[c]);
+    acc += k * (k - (k > 0 ? 1 : 0)) / 2;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(sum, acc);
+}
+
+// The poses of each contact, at offs[c] onwards (order within a list is
+// free: the counts do not depend on it).
+__global__ void k_post_fill(const uint32_t *bits, const uint32_t *ubits, const int *base, int n, long long words,
+                            const int *offs, int *cursor, int *post) {
+  for (long long it = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; it < static_cast<long long>(n) * words;
+       it += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int p = static_cast<int>(it / words);
+    const long long w = it % words;
+    const uint32_t u = ubits[w];
+    if (!u) continue;
+    uint32_t v = bits[static_cast<size_t>(p) * words + w] & u;
+    while (v) {
+      const int b = __ffs(v) - 1;
+      v &= v - 1;
+      const int c = base[w] + __popc(u & ((1u << b) - 1u));
+      post[offs[c] + atomicAdd(&cursor[c], 1)] = p;
+    }
+  }
+}
+
+// One warp per contact: +1 on the common count of every pose pair in its list.
+__global__ void k_post_pairs(const int *offs, const int *kc, const int *post, int U, int n, uint32_t *common) {
+  const int lane = threadIdx.x & 31;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < U; c += (gridDim.x * blockDim.x) >> 5) {
+    const int k = kc[c], o = offs[c];
+    for (int a = 0; a + 1 < k; ++a) {
+      const int i = post[o + a];
+      for (int b = a + 1 + lane; b < k; b += 32) {
+        const int j = post[o + b];
+        const int lo = min(i, j), hi = max(i, j);
+        atomicAdd(&common[static_cast<size_t>(lo) * n + hi], 1u);
+      }
+    }
+  }
+}
+
+// calculate_fcc and create_elements (src/clustering.rs:122-132,171) from the
+// common counts of the pairs i <= j (the diagonal: the pose's own size), as
+// k_fcc decides them.
+__global__ void k_post_decide(const uint32_t *common, const int *sizes, int n, double c, double cs, uint32_t *adj,
+                              int adj_words) {
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const int si = sizes[i];
+    for (int j = i + threadIdx.x; j < n; j += blockDim.x) {
+      const int sj = sizes[j];
+      bool edge = false, back = false;
+      if (si > 0 && sj > 0) {
+        const double cm = static_cast<double>(i == j ? si : static_cast<int>(common[static_cast<size_t>(i) * n + j]));
+        const double fcc = cm / static_cast<double>(si);
+        const double fcc_v = cm / static_cast<double>(sj);
+        edge = fcc >= c && fcc_v >= cs;
+        back = fcc_v >= c && fcc >= cs;
+      }
+      if (edge) atomicOr(&adj[static_cast<size_t>(i) * adj_words + (j >> 5)], 1u << (j & 31));
+      if (back && j != i) atomicOr(&adj[static_cast<size_t>(j) * adj_words + (i >> 5)], 1u << (i & 31));
+    }
+  }
+}
+
 // host mirror of the device transform (same operation order, no fused ops)
 void xform_host(const gd_pose_frame &f, double cx, double cy, double cz, double xo, double yo, double zo, double &X,
                 double &Y, double &Z) {
@@ -1080,18 +1178,90 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   trace("cluster (device): contacts + union", std::chrono::duration<double>(t_union - pt_all.t0).count());
   const int W = std::max(1, (U + 63) / 64);
   const int aw = (n + 31) / 32;
-  const size_t compact_b = sizeof(unsigned long long) * static_cast<size_t>(W) * n, sz_b = sizeof(int) * n,
-               adj_b = sizeof(uint32_t) * static_cast<size_t>(n) * aw;
+  const size_t adj_b = sizeof(uint32_t) * static_cast<size_t>(n) * aw, sz_b = sizeof(int) * n;
+  const long long tot = static_cast<long long>(n) * words;
+  const int g3 = static_cast<int>(std::min<long long>((tot + 255) / 256, static_cast<long long>(ctx->sm_count) * 32));
+  // pair counts: contact postings or bitsets (GD_TUNE_FCC; automatic: the
+  // estimated cheaper one, postings only up to 16,384 poses, and considered
+  // only when the bitsets would take more than ~2e10 word pairs, some 5 ms:
+  // counting the postings costs a pass and a synchronisation)
+  bool postings = ctx->tune_fcc == 2 && n <= 16384;
+  const double bits_work = 0.5 * static_cast<double>(n) * (n + 1) * W;
+  void *pre = nullptr;  // posting counts: kc[U], sizes[n], the work sum
+  const size_t kc_b = sizeof(int) * static_cast<size_t>(std::max(U, 1));
+  if (ctx->tune_fcc != 1 && n <= 16384 && (ctx->tune_fcc == 2 || bits_work > 2e10)) {
+    s = dev_alloc(ctx, al(kc_b) + al(sz_b) + al(8), &pre);
+    if (s != GD_OK) return s;
+    int *d_kc = static_cast<int *>(pre);
+    int *d_psz = reinterpret_cast<int *>(static_cast<char *>(pre) + al(kc_b));
+    unsigned long long *d_work = reinterpret_cast<unsigned long long *>(static_cast<char *>(pre) + al(kc_b) + al(sz_b));
+    unsigned long long work = 0;
+    e = cudaMemsetAsync(pre, 0, al(kc_b) + al(sz_b) + al(8), st);
+    if (e == cudaSuccess) {
+      k_post_count<<<std::max(g3, 1), 256, 0, st>>>(d_bits, d_u, d_base, n, words, d_kc, d_psz);
+      k_post_work<<<std::max(1, std::min((U + 255) / 256, ctx->sm_count * 8)), 256, 0, st>>>(d_kc, U, d_work);
+      e = cudaMemcpyAsync(&work, d_work, 8, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
+      return cuda_fail(ctx, e, "FCC posting counts");
+    }
+    // an atomic increment costs about as much as 80 word pairs of popcount
+    if (ctx->tune_fcc == 0) postings = 80.0 * static_cast<double>(work) < bits_work;
+  }
+  if (!postings && pre) {
+    dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
+    pre = nullptr;
+  }
+  const size_t compact_b = postings ? 0 : sizeof(unsigned long long) * static_cast<size_t>(W) * n;
+  // postings: offsets and cursors per contact, the lists (one entry per
+  // (pose, contact)), the n x n common counts
+  const size_t off_b = sizeof(int) * (static_cast<size_t>(U) + 1), cur_b = kc_b;
+  size_t memberships = 0;
+  if (postings) {
+    // the lists hold sum(kc) = sum of the pose sizes entries
+    std::vector<int> hsz(n);
+    e = cudaMemcpy(hsz.data(), static_cast<char *>(pre) + al(kc_b), sz_b, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
+      return cuda_fail(ctx, e, "FCC posting sizes");
+    }
+    for (int v : hsz) memberships += static_cast<size_t>(v);
+  }
+  const size_t list_b = sizeof(int) * std::max<size_t>(memberships, 1),
+               common_b = postings ? sizeof(uint32_t) * static_cast<size_t>(n) * n : 0;
+  const size_t extra_b = postings ? al(off_b) + al(cur_b) + al(list_b) + al(common_b) + al(sz_b) + al(adj_b)
+                                  : al(compact_b) + al(sz_b) + al(adj_b);
   void *extra = nullptr;
-  s = dev_alloc(ctx, al(compact_b) + al(sz_b) + al(adj_b), &extra);
-  if (s != GD_OK) return s;
-  unsigned long long *d_compact = static_cast<unsigned long long *>(extra);
-  int *d_sizes = reinterpret_cast<int *>(static_cast<char *>(extra) + al(compact_b));
-  uint32_t *d_adj = reinterpret_cast<uint32_t *>(static_cast<char *>(extra) + al(compact_b) + al(sz_b));
-  e = cudaMemsetAsync(extra, 0, al(compact_b) + al(sz_b) + al(adj_b), st);
-  if (e == cudaSuccess) {
-    const long long tot = static_cast<long long>(n) * words;
-    const int g3 = static_cast<int>(std::min<long long>((tot + 255) / 256, static_cast<long long>(ctx->sm_count) * 32));
+  s = dev_alloc(ctx, extra_b, &extra);
+  if (s != GD_OK) {
+    if (pre) dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
+    return s;
+  }
+  char *xp = static_cast<char *>(extra);
+  uint32_t *d_adj = reinterpret_cast<uint32_t *>(xp + extra_b - al(adj_b));
+  int *d_sizes = reinterpret_cast<int *>(xp + extra_b - al(adj_b) - al(sz_b));
+  e = cudaMemsetAsync(extra, 0, extra_b, st);
+  if (e == cudaSuccess && postings) {
+    int *d_kc = static_cast<int *>(pre);
+    int *d_psz = reinterpret_cast<int *>(static_cast<char *>(pre) + al(kc_b));
+    int *d_offs = reinterpret_cast<int *>(xp);
+    int *d_cur = reinterpret_cast<int *>(xp + al(off_b));
+    int *d_list = reinterpret_cast<int *>(xp + al(off_b) + al(cur_b));
+    uint32_t *d_common = reinterpret_cast<uint32_t *>(xp + al(off_b) + al(cur_b) + al(list_b));
+    e = cudaMemcpyAsync(d_sizes, d_psz, sz_b, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+      k_scan<<<1, 1024, 0, st>>>(d_kc, U, d_offs, d_offs + U);
+      k_post_fill<<<std::max(g3, 1), 256, 0, st>>>(d_bits, d_u, d_base, n, words, d_offs, d_cur, d_list);
+      k_post_pairs<<<std::max(1, std::min((U + 7) / 8, ctx->sm_count * 16)), 256, 0, st>>>(d_offs, d_kc, d_list, U, n,
+                                                                                          d_common);
+      k_post_decide<<<std::min(n, ctx->sm_count * 16), 256, 0, st>>>(d_common, d_sizes, n, cfg.fcc_cutoff,
+                                                                     cfg.fcc_cutoff * cfg.strictness, d_adj, aw);
+      e = cudaGetLastError();
+    }
+  } else if (e == cudaSuccess) {
+    unsigned long long *d_compact = reinterpret_cast<unsigned long long *>(xp);
     k_compact<<<std::max(g3, 1), 256, 0, st>>>(d_bits, d_u, d_base, n, words, W, d_compact, d_sizes);
     FccParams fp{};
     fp.bits = d_compact;
@@ -1109,10 +1279,12 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   std::vector<uint32_t> adj(static_cast<size_t>(n) * aw);
   if (e == cudaSuccess) e = cudaMemcpyAsync(adj.data(), d_adj, adj_b, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  dev_free(ctx, extra, al(compact_b) + al(sz_b) + al(adj_b));
+  dev_free(ctx, extra, extra_b);
+  if (pre) dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC on the device");
   const auto t_fcc = std::chrono::steady_clock::now();
-  trace("cluster (device): compact + fcc", std::chrono::duration<double>(t_fcc - t_union).count());
+  trace(postings ? "cluster (device): postings + fcc" : "cluster (device): compact + fcc",
+        std::chrono::duration<double>(t_fcc - t_union).count());
   *n_clusters = greedy_clusters(adj, n, aw, cfg.min_cluster_size, centers, sizes, members);
   trace("cluster (device): greedy (host)", std::chrono::duration<double>(std::chrono::steady_clock::now() - t_fcc).count());
   return GD_OK;

@@ -128,6 +128,7 @@ struct gd_context {
   int tune_f32_slots = 0;  // 0: automatic (kDefaultF32Tune)
   int tune_split = 0;      // GD_TUNE_SPLIT: 0 automatic, 1 whole poses, 2 always split
   int tune_fault = 0;      // GD_TUNE_FAULT: 1 = drop one stage copy (failure-detection tests)
+  int tune_fcc = 0;        // GD_TUNE_FCC: 0 automatic, 1 bitsets, 2 contact postings
 };
 
 struct gd_complex {

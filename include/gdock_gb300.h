@@ -117,8 +117,15 @@ gd_status gd_context_destroy(gd_context *ctx);
  *                      kernel issues no copy for one receptor stage, so that
  *                      stage's bounded wait (2 s) runs out, the kernel drains
  *                      its other copies (bounded) and the call reports
- *                      GD_ERR_TIMEOUT; the context stays usable.  0 = off. */
-enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2 };
+ *                      GD_ERR_TIMEOUT; the context stays usable.  0 = off.
+ *   GD_TUNE_FCC:       pair counts of the device FCC: 0 = automatic (by the
+ *                      estimated work of each), 1 = popcount over the
+ *                      compacted contact bitsets of every pose pair, 2 =
+ *                      per-contact lists of the poses that make it (the
+ *                      pairs of each list counted with atomics: little work
+ *                      when the contacts are spread over many poses, at most
+ *                      16,384 poses).  Clusters are identical either way. */
+enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2, GD_TUNE_FCC = 3 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 /* The FP32 scoring autotuner: times every candidate (GD_TUNE_F32_SLOTS,
  * GD_TUNE_SPLIT) = (20,1) (66,1) (68,1) (322,1) (324,1) (324,2) on n

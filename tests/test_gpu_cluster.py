@@ -101,3 +101,27 @@ def test_multichain_receptor_contacts(oracle):
     got = cx.pose_contacts(genes)
     for g, keys in zip(genes, got):
         np.testing.assert_array_equal(keys, oracle.pose_contacts(rec, lig, g))
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_cluster_device_fcc_paths(oracle, setup, mode):
+    """Both ways of counting common contacts on the device (GD_TUNE_FCC:
+    bitsets, contact postings) give the oracle's clusters, from converged to
+    spread-out poses and at extreme cutoffs."""
+    from gdock_gb300 import _lib
+    c, lig = setup
+    ctx = gd.Context(0)
+    ctx.set_tuning(_lib.GD_TUNE_FCC, mode)
+    cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+    rng = np.random.default_rng(40 + mode)
+    for spread in (0.3, 1.0, 6.0):
+        genes = near_genes(rng, 80, spread)
+        sets = [oracle.pose_contacts(c.receptor, lig, g) for g in genes]
+        for ms in (1, 4):
+            got = cx.cluster(genes, gd.ClusteringConfig(min_cluster_size=ms))
+            assert [(r.center_idx, r.members) for r in got] == oracle.cluster(sets, min_size=ms), (spread, ms)
+        for cut, strict in ((0.0, 0.75), (1.0, 1.0), (0.3, 0.5)):
+            cfg = gd.ClusteringConfig(fcc_cutoff=cut, strictness=strict, min_cluster_size=1)
+            got = cx.cluster(genes, cfg)
+            want = oracle.cluster(sets, fcc_cutoff=cut, strictness=strict, min_size=1)
+            assert [(r.center_idx, r.members) for r in got] == want, (spread, cut, strict)

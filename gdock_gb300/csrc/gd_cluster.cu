@@ -1214,7 +1214,8 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
     dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
     pre = nullptr;
   }
-  const size_t compact_b = postings ? 0 : sizeof(unsigned long long) * static_cast<size_t>(W) * n;
+  auto compact_bytes = [&]() { return sizeof(unsigned long long) * static_cast<size_t>(W) * n; };
+  size_t compact_b = postings ? 0 : compact_bytes();
   // postings: offsets and cursors per contact, the lists (one entry per
   // (pose, contact)), the n x n common counts
   const size_t off_b = sizeof(int) * (static_cast<size_t>(U) + 1), cur_b = kc_b;
@@ -1231,10 +1232,19 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   }
   const size_t list_b = sizeof(int) * std::max<size_t>(memberships, 1),
                common_b = postings ? sizeof(uint32_t) * static_cast<size_t>(n) * n : 0;
-  const size_t extra_b = postings ? al(off_b) + al(cur_b) + al(list_b) + al(common_b) + al(sz_b) + al(adj_b)
-                                  : al(compact_b) + al(sz_b) + al(adj_b);
+  size_t extra_b = postings ? al(off_b) + al(cur_b) + al(list_b) + al(common_b) + al(sz_b) + al(adj_b)
+                            : al(compact_b) + al(sz_b) + al(adj_b);
   void *extra = nullptr;
   s = dev_alloc(ctx, extra_b, &extra);
+  if (s != GD_OK && postings && ctx->tune_fcc != 2) {
+    // no room for the n x n counts: the bitsets after all
+    dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
+    pre = nullptr;
+    postings = false;
+    compact_b = compact_bytes();
+    extra_b = al(compact_b) + al(sz_b) + al(adj_b);
+    s = dev_alloc(ctx, extra_b, &extra);
+  }
   if (s != GD_OK) {
     if (pre) dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
     return s;

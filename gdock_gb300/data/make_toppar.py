@@ -8,9 +8,11 @@ The values are data that must be identical for parity, so this script reads
 them out of the reference's source once and writes them as JSON; the JSON
 is what the package ships.
 
-Usage: python gdock_gb300/data/make_toppar.py /root/reference/src/toppar.rs
+Usage: python gdock_gb300/data/make_toppar.py [path/to/gdock/src/toppar.rs]
+(default: $GDOCK_REF/src/toppar.rs, GDOCK_REF naming a gdock checkout)
 """
 import json
+import os
 import re
 import sys
 from pathlib import Path
@@ -45,7 +47,8 @@ def _residue_table(src: str) -> dict:
     return out
 
 
-def main(path: str) -> None:
+def extract(path: str) -> dict:
+    """The parameter and residue tables of ``toppar.rs`` as the JSON document."""
     src = Path(path).read_text()
     tables = {k: _type_table(src, k) for k in
               ("get_epsilon", "get_rmin2", "get_eps_1_4", "get_rmin2_1_4", "get_charge")}
@@ -58,10 +61,20 @@ def main(path: str) -> None:
         "types": dict(sorted(types.items())),
         "residues": _residue_table(src),
     }
+    return doc
+
+
+def main(path: str) -> None:
+    doc = extract(path)
     out = Path(__file__).with_name("toppar.json")
     out.write_text(json.dumps(doc, indent=1, sort_keys=True) + "\n")
     print(f"wrote {out}: {len(doc['types'])} types, {len(doc['residues'])} residues")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/toppar.rs")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    elif os.environ.get("GDOCK_REF"):
+        main(str(Path(os.environ["GDOCK_REF"]) / "src" / "toppar.rs"))
+    else:
+        sys.exit("usage: make_toppar.py path/to/src/toppar.rs (or set GDOCK_REF to a gdock checkout)")

@@ -9,8 +9,9 @@ energies of seeded poses and of the 100 MODELs of the `score` example,
 contacts, clusters and the evaluator's metrics.  The GPU tests compare against these files, so they
 need neither the reference checkout nor the oracle at run time.
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py [path/to/gdock]  (default: $GDOCK_REF)
 """
+import os
 import sys
 from pathlib import Path
 
@@ -89,4 +90,7 @@ def main(ref: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GDOCK_REF")
+    if not ref:
+        sys.exit("usage: make_golden.py path/to/gdock (or set GDOCK_REF to a gdock checkout)")
+    main(Path(ref))

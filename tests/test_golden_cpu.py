@@ -1,6 +1,7 @@
 """The committed golden fixtures against the oracle (regression of both), and
-the fixture's parsed arrays against gdock's test structures when the
-reference checkout is present."""
+the fixture's parsed arrays against gdock's test structures when a gdock
+checkout is named by the environment variable GDOCK_REF."""
+import os
 from pathlib import Path
 
 import numpy as np
@@ -28,9 +29,11 @@ def test_1h590_score_models(oracle):
 
 
 def test_fixture_matches_reference_structures():
-    ref = Path("/root/reference/data")
+    if not os.environ.get("GDOCK_REF"):
+        pytest.skip("GDOCK_REF (a gdock checkout) not set")
+    ref = Path(os.environ["GDOCK_REF"]) / "data"
     if not ref.exists():
-        pytest.skip("reference checkout not present")
+        pytest.skip(f"no data directory under GDOCK_REF={os.environ['GDOCK_REF']}")
     from gdock_gb300 import pdb
     d, rec, lig = load("2oob.npz")
     r = pdb.read_pdb(ref / "2oob_A.pdb")[0]

@@ -225,9 +225,13 @@ def test_cluster_greedy_semantics(oracle):
 
 def test_contacts_real_data(oracle):  # src/clustering.rs:365-392
     from gdock_gb300 import pdb
-    ref = pytest.importorskip("pathlib").Path("/root/reference/data/2oob_A.pdb")
+    import os
+    from pathlib import Path
+    if not os.environ.get("GDOCK_REF"):
+        pytest.skip("GDOCK_REF (a gdock checkout) not set")
+    ref = Path(os.environ["GDOCK_REF"]) / "data" / "2oob_A.pdb"
     if not ref.exists():
-        pytest.skip("reference data not present on this machine")
+        pytest.skip(f"no data/2oob_A.pdb under GDOCK_REF={os.environ['GDOCK_REF']}")
     r = pdb.read_pdb(ref)[0]
     l = pdb.read_pdb(ref.with_name("2oob_B.pdb"))[0]
     keys = oracle.contacts(pdb.combine_molecules(r, l))

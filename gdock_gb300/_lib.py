@@ -39,6 +39,9 @@ GD_TUNE_F32_SLOTS = 0
 GD_TUNE_SPLIT = 1
 GD_TUNE_FAULT = 2
 GD_TUNE_FCC = 3
+GD_TUNE_CONTACTS = 4
+GD_INFO_LAST_FCC = 16
+GD_INFO_LAST_CONTACTS = 17
 
 
 class GdAtoms(C.Structure):
@@ -220,6 +223,10 @@ class Context:
 
     def set_tuning(self, knob: int, value: int):
         self.check(self.lib.gd_context_set_tuning(self.h, knob, value))
+
+    def get_tuning(self, knob: int) -> int:
+        """A knob's value, or a read-only GD_INFO_* value."""
+        return int(self.lib.gd_context_get_tuning(self.h, knob))
 
     @property
     def bytes_in_use(self) -> int:

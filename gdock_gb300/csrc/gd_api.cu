@@ -47,6 +47,10 @@ gd_status dev_alloc(gd_context *ctx, uint64_t bytes, void **p) {
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
     *p = nullptr;
+    // a failed allocation is not a sticky error: clear it, so that a caller
+    // that falls back to a smaller plan does not read it back from
+    // cudaGetLastError() after its next launch
+    (void)cudaGetLastError();
     return cuda_fail(ctx, e, "cudaMalloc");
   }
   ctx->in_use += bytes;
@@ -419,6 +423,14 @@ gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
     ctx->tune_fcc = value;
     return GD_OK;
   }
+  if (knob == GD_TUNE_CONTACTS) {
+    if (value < 0 || value > 1)
+      return fail(ctx, GD_ERR_INVALID_ARG, "contacts tuning: 0 (automatic), 1 (per-residue lists)");
+    ctx->tune_contacts = value;
+    return GD_OK;
+  }
+  if (knob == GD_INFO_LAST_FCC || knob == GD_INFO_LAST_CONTACTS)
+    return fail(ctx, GD_ERR_INVALID_ARG, "read-only knob");
   return fail(ctx, GD_ERR_INVALID_ARG, "unknown tuning knob");
 }
 
@@ -428,6 +440,9 @@ int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob) {
   if (knob == GD_TUNE_SPLIT) return ctx->tune_split;
   if (knob == GD_TUNE_FAULT) return ctx->tune_fault;
   if (knob == GD_TUNE_FCC) return ctx->tune_fcc;
+  if (knob == GD_TUNE_CONTACTS) return ctx->tune_contacts;
+  if (knob == GD_INFO_LAST_FCC) return ctx->last_fcc;
+  if (knob == GD_INFO_LAST_CONTACTS) return ctx->last_contacts;
   return -1;
 }
 

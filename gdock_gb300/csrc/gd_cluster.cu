@@ -458,6 +458,65 @@ __global__ void __launch_bounds__(kContactWarps * 32) k_contact_bits(const BitsP
   }
 }
 
+// Set bits of each pose's contact bitmap (one block per pose at a time).
+__global__ void __launch_bounds__(256) k_bits_count(const uint32_t *bits, int n, long long words, int *counts) {
+  __shared__ int s_w[8];
+  for (int pose = blockIdx.x; pose < n; pose += gridDim.x) {
+    const uint32_t *row = bits + static_cast<size_t>(pose) * words;
+    int c = 0;
+    for (long long w = threadIdx.x; w < words; w += blockDim.x) c += __popc(row[w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int k = 0; k < 8; ++k) tot += s_w[k];
+      counts[pose] = tot;
+    }
+    __syncthreads();
+  }
+}
+
+// The set bits' indices (rg * GL + lg) of each pose's bitmap, in ascending
+// order, from offs[pose] on: blocks of 256 words, a block-wide exclusive scan
+// of their popcounts placing each word's bits.
+__global__ void __launch_bounds__(256) k_bits_lists(const uint32_t *bits, int n, long long words,
+                                                    const long long *offs, uint32_t *out) {
+  __shared__ int s_w[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int pose = blockIdx.x; pose < n; pose += gridDim.x) {
+    const uint32_t *row = bits + static_cast<size_t>(pose) * words;
+    long long o = offs[pose];
+    for (long long w0 = 0; w0 < words; w0 += blockDim.x) {
+      const long long w = w0 + threadIdx.x;
+      uint32_t v = w < words ? row[w] : 0u;
+      const int c = __popc(v);
+      int inc = c;  // inclusive scan within the warp
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += y;
+      }
+      if (lane == 31) s_w[wid] = inc;
+      __syncthreads();
+      int before = 0, tot = 0;
+      for (int k = 0; k < 8; ++k) {
+        before += k < wid ? s_w[k] : 0;
+        tot += s_w[k];
+      }
+      long long pos = o + before + inc - c;
+      while (v) {
+        const int b = __ffs(v) - 1;
+        v &= v - 1;
+        out[pos++] = static_cast<uint32_t>(w * 32 + b);
+      }
+      o += tot;
+      __syncthreads();
+    }
+  }
+}
+
 // Union over poses and set-bit count of each bitmap word.
 __global__ void k_union(const uint32_t *bits, int n, long long words, uint32_t *ubits, int *ucount) {
   for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < words;
@@ -896,7 +955,69 @@ void free_cluster_cache(gd_complex *cx) {
   cx->cluster_cache = nullptr;
 }
 
-// Contact keys of n poses (sorted per pose) into a host vector + offsets.
+bool bits_path_ok(const ClusterTopo *t, int n);
+long long bits_words(const ClusterTopo *t);
+gd_status launch_contact_bits(gd_complex *cx, ClusterTopo *t, const gd_pose_frame *d_frames, int n, double cutoff,
+                              double maxd, uint32_t *d_bits, long long words, cudaStream_t st);
+double max_displacement(const double *genes, int n);
+
+// Contacts of n poses through the contact bitmaps: k_contact_bits, then the
+// set bits of every pose as (receptor residue group * GL + ligand residue
+// group) entries, flat with per-pose offsets loffs (n + 1 entries).
+static gd_status contacts_via_bits(gd_complex *cx, ClusterTopo *t, const std::vector<gd_pose_frame> &frames, int n,
+                                   double cutoff, double maxd, std::vector<uint32_t> &flat,
+                                   std::vector<long long> &loffs) {
+  gd_context *ctx = cx->ctx;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const long long words = bits_words(t);
+  const size_t fb = sizeof(gd_pose_frame) * n, bits_b = sizeof(uint32_t) * static_cast<size_t>(words) * n,
+               cb = sizeof(int) * n, ob = sizeof(long long) * (n + 1);
+  gd_status s = ensure_scratch(ctx, al(fb) + al(bits_b) + al(cb) + al(ob), 0);
+  if (s != GD_OK) return s;
+  char *base = static_cast<char *>(ctx->d_scratch);
+  gd_pose_frame *d_frames = reinterpret_cast<gd_pose_frame *>(base);
+  uint32_t *d_bits = reinterpret_cast<uint32_t *>(base + al(fb));
+  int *d_counts = reinterpret_cast<int *>(base + al(fb) + al(bits_b));
+  long long *d_offs = reinterpret_cast<long long *>(base + al(fb) + al(bits_b) + al(cb));
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(d_frames, frames.data(), fb, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contacts setup");
+  s = launch_contact_bits(cx, t, d_frames, n, cutoff, maxd, d_bits, words, st);
+  if (s != GD_OK) return s;
+  const int grid = std::max(1, std::min(n, ctx->sm_count * 8));
+  k_bits_count<<<grid, 256, 0, st>>>(d_bits, n, words, d_counts);
+  std::vector<int> counts(n);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counts.data(), d_counts, cb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps");
+  s = check_device_error(ctx);
+  if (s != GD_OK) return s;
+  loffs.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) loffs[i + 1] = loffs[i] + counts[i];
+  flat.resize(static_cast<size_t>(loffs[n]));
+  ctx->last_contacts = 2;
+  if (loffs[n] == 0) return GD_OK;
+  void *d_flat = nullptr;
+  const size_t flat_b = sizeof(uint32_t) * flat.size();
+  s = dev_alloc(ctx, flat_b, &d_flat);
+  if (s != GD_OK) return s;
+  e = cudaMemcpyAsync(d_offs, loffs.data(), ob, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_bits_lists<<<grid, 256, 0, st>>>(d_bits, n, words, d_offs, static_cast<uint32_t *>(d_flat));
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(flat.data(), d_flat, flat_b, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  dev_free(ctx, d_flat, flat_b);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmap lists");
+  return GD_OK;
+}
+
+// Contact keys of n poses (sorted per pose) into a host vector + offsets:
+// through the contact bitmaps when the topology allows it (and
+// GD_TUNE_CONTACTS does not ask for the lists), else through per-residue
+// contact lists (k_contacts_rl).  Both decide every atom pair exactly.
 gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double cutoff, std::vector<int64_t> &keys,
                              std::vector<int64_t> &offs) {
   gd_context *ctx = cx->ctx;
@@ -918,7 +1039,14 @@ gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double 
   std::vector<int> counts(n);
   std::vector<uint32_t> flat;
   std::vector<long long> loffs(n + 1, 0);
-  for (int attempt = 0; attempt < 2; ++attempt) {
+  const bool via_bits = ctx->tune_contacts != 1 && n > 0 && bits_path_ok(t, n);
+  if (via_bits) {
+    s = contacts_via_bits(cx, t, frames, n, cutoff, max_displacement(genes, n), flat, loffs);
+    if (s != GD_OK) return s;
+  } else {
+    ctx->last_contacts = 1;
+  }
+  for (int attempt = 0; attempt < 2 && !via_bits; ++attempt) {
     const size_t fb = sizeof(gd_pose_frame) * n, cb = sizeof(int) * n,
                  lb = sizeof(uint32_t) * static_cast<size_t>(n) * cap, ob = sizeof(long long) * (n + 1);
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -1080,43 +1208,32 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
 // ligand that share no residue: contact bitmaps, union, compaction, FCC; the
 // greedy pass runs on the host.  Returns GD_ERR_STATE when the topology or the
 // bitmap size calls for the general path.
-gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cluster_cfg &cfg, int32_t *n_clusters,
-                         int32_t *centers, int32_t *sizes, int32_t *members) {
-  gd_context *ctx = cx->ctx;
-  PhaseTimer pt_all("cluster (device): total");
-  ClusterTopo *t = nullptr;
-  gd_status s = get_topo(cx, &t);
-  if (s != GD_OK) return s;
-  if (t->multi_chain_rec || t->multi_chain_lig || t->mixed) return GD_ERR_STATE;
+// The contact-bitmap path (k_contact_bits) serves single-chain receptors and
+// ligands that share no residue, with every ligand residue staged whole, at
+// most 8 GiB of bitmaps and bit indices that fit 32 bits.
+bool bits_path_ok(const ClusterTopo *t, int n) {
+  if (t->multi_chain_rec || t->multi_chain_lig || t->mixed) return false;
   for (int g = 0; g < t->GL; ++g)
-    if (t->lg_off[g + 1] - t->lg_off[g] > kMaxGroupAtoms) return GD_ERR_STATE;  // residues staged whole
+    if (t->lg_off[g + 1] - t->lg_off[g] > kMaxGroupAtoms) return false;  // residues staged whole
   const long long pairs = static_cast<long long>(t->GR) * t->GL;
+  if (pairs > static_cast<long long>(UINT32_MAX)) return false;
   const long long words = std::max<long long>(1, (pairs + 31) / 32);
-  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-  const size_t bits_b = sizeof(uint32_t) * words * static_cast<size_t>(n);
-  if (bits_b > (static_cast<size_t>(8) << 30)) return GD_ERR_STATE;  // > 8 GiB of bitmaps
-  const Thresholds thr = make_thresholds(cfg.contact_distance);
-  std::vector<gd_pose_frame> frames(n);
-  gd_make_frames(genes, n, frames.data());
-  double maxd = 0.0;
-  for (int i = 0; i < n; ++i)
-    for (int k = 3; k < 6; ++k) maxd = std::max(maxd, std::fabs(genes[6 * static_cast<size_t>(i) + k]));
-  const size_t fb = sizeof(gd_pose_frame) * n, ub = sizeof(uint32_t) * words, cb = sizeof(int) * words;
-  // the compacted universe is at most min(pairs, sum of sizes); size it after the scan
-  auto t_step = std::chrono::steady_clock::now();
-  s = ensure_scratch(ctx, al(fb) + al(bits_b) + al(ub) + 2 * al(cb) + al(sizeof(int)), 0);
-  if (s != GD_OK) return s;
-  char *base = static_cast<char *>(ctx->d_scratch);
-  gd_pose_frame *d_frames = reinterpret_cast<gd_pose_frame *>(base);
-  uint32_t *d_bits = reinterpret_cast<uint32_t *>(base + al(fb));
-  uint32_t *d_u = reinterpret_cast<uint32_t *>(base + al(fb) + al(bits_b));
-  int *d_cnt = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub));
-  int *d_base = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub) + al(cb));
-  int *d_total = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub) + 2 * al(cb));
-  cudaStream_t st = ctx->stream;
-  cudaError_t e = cudaMemcpyAsync(d_frames, frames.data(), fb, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_bits, 0, bits_b, st);
-  trace_step("cluster (device):   scratch + frames + clear", st, t_step);
+  return sizeof(uint32_t) * static_cast<size_t>(words) * static_cast<size_t>(n) <= (static_cast<size_t>(8) << 30);
+}
+
+long long bits_words(const ClusterTopo *t) {
+  return std::max<long long>(1, (static_cast<long long>(t->GR) * t->GL + 31) / 32);
+}
+
+// Contact bitmaps of n device-resident poses: d_bits (n rows of `words`
+// words, bit rg * GL + lg) is cleared and filled by k_contact_bits on st.
+// maxd bounds the poses' |displacement| components (it sizes the FP32 guard
+// band, as for the scoring kernels).
+gd_status launch_contact_bits(gd_complex *cx, ClusterTopo *t, const gd_pose_frame *d_frames, int n, double cutoff,
+                              double maxd, uint32_t *d_bits, long long words, cudaStream_t st) {
+  gd_context *ctx = cx->ctx;
+  const Thresholds thr = make_thresholds(cutoff);
+  cudaError_t e = cudaMemsetAsync(d_bits, 0, sizeof(uint32_t) * static_cast<size_t>(words) * n, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps setup");
   BitsParams p{};
   p.r32 = t->d_r32;
@@ -1147,24 +1264,69 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   p.t32 = static_cast<float>(thr.contact_le);
   {
     // FP32 error bound of d2 near the cutoff (as for the scoring guard bands)
-    const double u = std::ldexp(1.0, -24), c = cfg.contact_distance;
+    const double u = std::ldexp(1.0, -24), c = cutoff;
     const double M = std::max(cx->rec_extent, cx->lig_radius + maxd +
                                                   std::max({std::fabs(cx->cx - cx->ox), std::fabs(cx->cy - cx->oy),
                                                             std::fabs(cx->cz - cx->oz)})) + 1.0;
     const double err = 2.0 * c * std::sqrt(3.0) * (2.0 * M * u + c * u) + 4.0 * c * c * u;
     p.guard = static_cast<float>(4.0 * err + 1e-6);
   }
-  p.reach = static_cast<float>(cfg.contact_distance) + 0.05f;
+  p.reach = static_cast<float>(cutoff) + 0.05f;
   p.bits = d_bits;
   p.words = words;
   p.err = ctx->d_err;
+  const long long pairs = static_cast<long long>(t->GR) * t->GL;
   if (pairs > 0 && n > 0) {
     const long long items = static_cast<long long>(n) * ((t->GL + kLigBlock - 1) / kLigBlock);
     const int grid = static_cast<int>(std::min<long long>((items + kContactWarps - 1) / kContactWarps,
                                                           static_cast<long long>(ctx->sm_count) * 16));
     k_contact_bits<<<grid, kContactWarps * 32, 0, st>>>(p);
-    trace_step("cluster (device):   k_contact_bits", st, t_step);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps launch");
   }
+  return GD_OK;
+}
+
+double max_displacement(const double *genes, int n) {
+  double maxd = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int k = 3; k < 6; ++k) maxd = std::max(maxd, std::fabs(genes[6 * static_cast<size_t>(i) + k]));
+  return maxd;
+}
+
+gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cluster_cfg &cfg, int32_t *n_clusters,
+                         int32_t *centers, int32_t *sizes, int32_t *members) {
+  gd_context *ctx = cx->ctx;
+  PhaseTimer pt_all("cluster (device): total");
+  ClusterTopo *t = nullptr;
+  gd_status s = get_topo(cx, &t);
+  if (s != GD_OK) return s;
+  if (!bits_path_ok(t, n)) return GD_ERR_STATE;
+  const long long words = bits_words(t);
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t bits_b = sizeof(uint32_t) * words * static_cast<size_t>(n);
+  std::vector<gd_pose_frame> frames(n);
+  gd_make_frames(genes, n, frames.data());
+  const double maxd = max_displacement(genes, n);
+  const size_t fb = sizeof(gd_pose_frame) * n, ub = sizeof(uint32_t) * words, cb = sizeof(int) * words;
+  // the compacted universe is at most min(pairs, sum of sizes); size it after the scan
+  auto t_step = std::chrono::steady_clock::now();
+  s = ensure_scratch(ctx, al(fb) + al(bits_b) + al(ub) + 2 * al(cb) + al(sizeof(int)), 0);
+  if (s != GD_OK) return s;
+  char *base = static_cast<char *>(ctx->d_scratch);
+  gd_pose_frame *d_frames = reinterpret_cast<gd_pose_frame *>(base);
+  uint32_t *d_bits = reinterpret_cast<uint32_t *>(base + al(fb));
+  uint32_t *d_u = reinterpret_cast<uint32_t *>(base + al(fb) + al(bits_b));
+  int *d_cnt = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub));
+  int *d_base = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub) + al(cb));
+  int *d_total = reinterpret_cast<int *>(base + al(fb) + al(bits_b) + al(ub) + 2 * al(cb));
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(d_frames, frames.data(), fb, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contact bitmaps setup");
+  trace_step("cluster (device):   scratch + frames", st, t_step);
+  s = launch_contact_bits(cx, t, d_frames, n, cfg.contact_distance, maxd, d_bits, words, st);
+  if (s != GD_OK) return s;
+  ctx->last_contacts = 2;
+  trace_step("cluster (device):   k_contact_bits", st, t_step);
   const int g2 = static_cast<int>(std::min<long long>((words + 255) / 256, static_cast<long long>(ctx->sm_count) * 8));
   k_union<<<std::max(g2, 1), 256, 0, st>>>(d_bits, n, words, d_u, d_cnt);
   k_scan<<<1, 1024, 0, st>>>(d_cnt, words, d_base, d_total);
@@ -1244,11 +1406,13 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
     compact_b = compact_bytes();
     extra_b = al(compact_b) + al(sz_b) + al(adj_b);
     s = dev_alloc(ctx, extra_b, &extra);
+    if (s == GD_OK) ctx->last_error.clear();  // the refused allocation is not this call's failure
   }
   if (s != GD_OK) {
     if (pre) dev_free(ctx, pre, al(kc_b) + al(sz_b) + al(8));
     return s;
   }
+  ctx->last_fcc = postings ? 2 : 1;
   char *xp = static_cast<char *>(extra);
   uint32_t *d_adj = reinterpret_cast<uint32_t *>(xp + extra_b - al(adj_b));
   int *d_sizes = reinterpret_cast<int *>(xp + extra_b - al(adj_b) - al(sz_b));

@@ -129,6 +129,9 @@ struct gd_context {
   int tune_split = 0;      // GD_TUNE_SPLIT: 0 automatic, 1 whole poses, 2 always split
   int tune_fault = 0;      // GD_TUNE_FAULT: 1 = drop one stage copy (failure-detection tests)
   int tune_fcc = 0;        // GD_TUNE_FCC: 0 automatic, 1 bitsets, 2 contact postings
+  int tune_contacts = 0;   // GD_TUNE_CONTACTS: 0 automatic (bitmaps where possible), 1 per-residue lists
+  int last_fcc = 0;        // GD_INFO_LAST_FCC: pair counts of the last device clustering (1 bitsets, 2 postings)
+  int last_contacts = 0;   // GD_INFO_LAST_CONTACTS: kernel of the last contact pass (1 lists, 2 bitmaps)
 };
 
 struct gd_complex {

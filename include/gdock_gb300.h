@@ -124,8 +124,20 @@ gd_status gd_context_destroy(gd_context *ctx);
  *                      per-contact lists of the poses that make it (the
  *                      pairs of each list counted with atomics: little work
  *                      when the contacts are spread over many poses, at most
- *                      16,384 poses).  Clusters are identical either way. */
-enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2, GD_TUNE_FCC = 3 };
+ *                      16,384 poses).  Clusters are identical either way.
+ *   GD_TUNE_CONTACTS:  contact pass of gd_pose_contacts: 0 = automatic (the
+ *                      per-pose residue-pair bitmaps of the clustering path
+ *                      whenever receptor and ligand are single chains that
+ *                      share no residue, else per-residue contact lists),
+ *                      1 = per-residue contact lists always.  Both decide
+ *                      every atom pair exactly; the keys are identical.
+ * Read-only (gd_context_get_tuning; set_tuning refuses them):
+ *   GD_INFO_LAST_FCC:      pair counts of the context's last device
+ *                          clustering: 1 bitsets, 2 postings, 0 none yet.
+ *   GD_INFO_LAST_CONTACTS: contact pass of the last gd_pose_contacts or
+ *                          gd_cluster: 1 lists, 2 bitmaps, 0 none yet. */
+enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2, GD_TUNE_FCC = 3, GD_TUNE_CONTACTS = 4,
+       GD_INFO_LAST_FCC = 16, GD_INFO_LAST_CONTACTS = 17 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 /* The FP32 scoring autotuner: times every candidate (GD_TUNE_F32_SLOTS,
  * GD_TUNE_SPLIT) = (20,1) (66,1) (68,1) (322,1) (324,1) (324,2) on n

@@ -175,6 +175,15 @@ def pose_contacts(rec, lig, genes, cutoff=5.0) -> np.ndarray:
     return keys[: min(n, cap)].copy()
 
 
+def pose_contacts_many(rec, lig, genes, cutoff=5.0, nthreads=None):
+    """pose_contacts of every gene vector, on a pool of host threads (the C
+    restatement releases the interpreter lock while it runs)."""
+    from concurrent.futures import ThreadPoolExecutor
+    g = np.asarray(genes, dtype=np.float64).reshape(-1, 6)
+    with ThreadPoolExecutor(max_workers=nthreads or os.cpu_count() or 1) as ex:
+        return list(ex.map(lambda row: pose_contacts(rec, lig, row, cutoff), g))
+
+
 def _flatten_sets(sets):
     offs = np.zeros(len(sets) + 1, dtype=np.int64)
     for i, s in enumerate(sets):

@@ -138,24 +138,38 @@ def test_reference_kats_through_abi(oracle):
 
 
 def test_cutoff_boundaries_f32_matches_f64(oracle):
-    """Ligand atoms placed within a few ulps of every cutoff: the FP32 form's
-    guard band must reproduce the exact FP64 decisions."""
+    """Ligand atoms placed within a few ulps of every cutoff (1, 8, 12 and
+    15 A), each as a model of its own, so that every single pair decision
+    shows in the energies: the FP32 form's guard band must reproduce the
+    exact FP64 decisions.  Desolvation is a sum of table entries picked by
+    exact counts (<= 1e-12); an elec or vdW decision that flipped would add or
+    drop a whole pair term (0.8 kcal/mol for elec at 15 A, 3e-4 for vdW at
+    12 A), far above the FP32 rounding of one term allowed here."""
     rec = make_mol([tatom(0, 0, 0, "O", charge=0.8, serial=1)])
+    lig = make_mol([tatom(0, 0, 0, "N", charge=-0.7, serial=100)])
     pts = []
     for c in (1.0, 8.0, 12.0, 15.0):
         for k in (-3, -1, 0, 1, 3):
             d = c * (1 + k * 2.0 ** -52)
-            u = np.array([1.0, 2.0, 2.0]) / 3.0
-            pts.append(tatom(*(d * u), "N", charge=-0.7, serial=100 + len(pts)))
-    lig = make_mol(pts)
+            for u in ((1.0, 2.0, 2.0), (0.0, 0.0, 1.0), (0.6, -0.8, 0.0)):
+                pts.append(d * np.asarray(u) / np.linalg.norm(u))
+    xyz = np.asarray(pts)[:, None, :]
     cx = gd.Complex(rec, lig, [])
-    xyz = lig.xyz()[None]
     e64 = cx.score_models(xyz, gd.GD_PREC_F64)
     e32 = cx.score_models(xyz, gd.GD_PREC_F32)
     ref = oracle.score_models(rec, lig, [], xyz)
     check(e64, ref, F64_TOL)
-    for name in ("vdw", "elec", "desolv"):
-        assert abs(e32[name][0] - e64[name][0]) <= 1e-5 * max(1.0, abs(e64[name][0])), name
+    # the reference's decisions (src/fitness.rs): which models have a term
+    for k, name in ((1, "vdw"), (2, "elec"), (3, "desolv")):
+        np.testing.assert_array_equal(e32[name] != 0.0, ref[:, k] != 0.0, err_msg=name)
+    assert np.any(ref[:, 2] == 0.0) and np.any(ref[:, 2] != 0.0)
+    np.testing.assert_array_less(rel_err(e32["desolv"], e64["desolv"], 1e-300), 1e-12 + 1e-300)
+    # FP32 rounding of one term: relative for elec; for vdW against a floor of
+    # 0.01 kcal/mol (at 1 A its soft-core value is a difference of nearly
+    # equal numbers), still 30x below a flipped 12 A term
+    for name, floor in (("vdw", 1e-2), ("elec", 1e-300)):
+        err = rel_err(e32[name], e64[name], floor)
+        assert err.max() <= 1e-5, (name, float(err.max()), int(err.argmax()))
 
 
 def test_elec_cutoff_band_in_far_rows(oracle):

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
 FILES = ["test_gpu_golden.py", "test_gpu_scoring.py", "test_gpu_ga.py", "test_gpu_cluster.py",
          "test_gpu_evaluator.py", "test_gpu_server.py", "test_gpu_full_size.py",
-         "test_gpu_edge_cases.py"]
+         "test_gpu_edge_cases.py", "test_gpu_contact_boundary.py", "test_gpu_cluster_large.py"]
 
 
 def test_gpu_suite_under_debug_library():

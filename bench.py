@@ -185,28 +185,34 @@ def replica_throughput(t_step: float, units: int, world: int, device: str = "cpu
 
 
 def run_reference(args):
-    import torch.distributed as dist  # noqa: F401  (imported for parity with the GPU arm)
+    """The reference arm: gdock's scoring path on the host cores, on the same
+    workload, metric and config as the GPU arm.  gdock is Rust and cannot be
+    built here, so its CPU path is the oracle (the C restatement of its FP64
+    scoring), threaded per pose like its rayon map.  Each step scores a
+    bounded sample of the workload's poses; ms_per_step is that sample's
+    measured time and value the sampled poses/s."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     c, lig, genes = workload()
     threads = os.cpu_count() or 1
-    n_sample = max(4, int(os.environ.get("GD_REF_SAMPLE", "32")))
+    n_sample = max(4, int(os.environ.get("GD_REF_SAMPLE", "128")))
     for _ in range(args.warmup):
         cpu_sample(c, lig, genes, min(n_sample, 8), threads)
     vals = [cpu_sample(c, lig, genes[i * n_sample:], n_sample, threads) for i in range(args.steps)]
     v = float(np.median(vals))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "poses/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": N_POSES / v * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n_sample / v * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config(c, lig, {"sample_poses_per_step": n_sample}),
+            "config": config(c, lig, {"parallelism": "replicas" if args.gpus > 1 else "single GPU",
+                                      "poses_per_step": N_POSES}),
             "cpu_baseline": {"value": v, "unit": "poses/s", "cores": threads, "kind": "port",
-                             "sample": f"{n_sample} poses of the workload per step, extrapolated per pose"},
+                             "sample": f"each step scores {n_sample} of the workload's {N_POSES} poses "
+                                       "(ms_per_step is that sample's time)"},
             "e2e": {"value": v, "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "gdock is Rust and cargo is not available: the CPU oracle (C restatement of its FP64 "
                     "scoring, threaded per pose like its rayon map) stands in for it"}
     print(json.dumps(line), flush=True)
-
 
 
 # --------------------------------------------------------------------------
@@ -327,19 +333,27 @@ def run_c1(args):
     print(json.dumps(line), flush=True)
 
 
-def run_c3(args):
+C3_WORKLOAD = ("64 synthetic complexes, receptor 100-800 residues, ligand 50-300 residues (log-uniform), "
+               "6-20 restraints; GA pop 150 x 50 generations with the Hall of Fame, then FCC clustering of "
+               "each Hall of Fame")
+
+
+def measure_c3(split: str = "auto", steps: int = 1) -> dict:
+    """The batched uneven GA: 64 complexes, pop 150 x 50 generations per
+    complex in one persistent launch per generation (CUDA graphs), the Hall of
+    Fame on the device, then FCC clustering of each Hall of Fame."""
     import gdock_gb300 as gd
     from gdock_gb300 import _lib
     ctx = gd.Context(0)
-    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[split])
     jobs = _uneven_complexes(64, 33)
     G, pop = 50, 150
     cxs = [gd.Complex(r, l, p, ctx=ctx) for r, l, p in jobs]
     cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=G, early_stopping=0, seed=3)
     gd.run_ga(cxs[:2], _lib.ga_default_cfg(pop_size=pop, max_generations=2, early_stopping=0), ctx=ctx)  # warm
-    tuned = autotune_ga(gd, _lib, ctx, cxs, pop, {"auto": 0, "never": 1, "always": 2}[args.split])
+    tuned = autotune_ga(gd, _lib, ctx, cxs, pop, {"auto": 0, "never": 1, "always": 2}[split])
     times = []
-    for _ in range(max(1, args.steps)):
+    for _ in range(max(1, steps)):
         t0 = time.perf_counter()
         res = gd.run_ga(cxs, cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
         times.append(time.perf_counter() - t0)
@@ -367,15 +381,13 @@ def run_c3(args):
     t_gen = (time.perf_counter() - t0) / 4
     pair_frac = sum(len(r) * len(l) for r, l, _ in jobs) / (16 * sum(len(r) * len(l) for r, l, _ in jobs[:4]))
     cpu_docks = 1.0 / (t_gen * (G + 1) * pair_frac)
-    line = {"metric": "docks/s (batched uneven GA, 64 complexes, pop 150, 50 generations, CUDA graphs)",
-            "value": len(jobs) / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": 1,
-            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "64 synthetic complexes, receptor 100-800 residues, ligand 50-300 residues "
-                                   "(log-uniform), 6-20 restraints; GA pop 150 x 50 generations with the Hall "
-                                   "of Fame, then FCC clustering of each Hall of Fame",
-                       "receptor_atoms": [min(len(r) for r, _, _ in jobs), max(len(r) for r, _, _ in jobs)],
-                       "ligand_atoms": [min(len(l) for _, l, _ in jobs), max(len(l) for _, l, _ in jobs)]},
+    for cx in cxs:
+        cx.close()
+    ctx.close()
+    return {"docks_per_s": len(jobs) / t, "seconds_per_64_docks": t, "steps": len(times),
+            "workload": C3_WORKLOAD,
+            "receptor_atoms": [min(len(r) for r, _, _ in jobs), max(len(r) for r, _, _ in jobs)],
+            "ligand_atoms": [min(len(l) for _, l, _ in jobs), max(len(l) for _, l, _ in jobs)],
             "poses_per_s": evals / t, "pair_evals_per_s": pairs / t,
             "fcc_clustering": {"seconds_for_64_halls_of_fame": t_fcc, "clusters_found": int(sum(n_clusters)),
                                "hall_of_fame_entries": int(sum(len(h) for h in res.hall_of_fame))},
@@ -385,18 +397,37 @@ def run_c3(args):
             "cpu_baseline": {"value": cpu_docks, "unit": "docks/s", "cores": threads, "kind": "port",
                              "sample": "the oracle scoring one generation (150 poses) of 4 of the 64 complexes, "
                                        "extrapolated by pair count to 64 docks x 51 evaluations"}}
+
+
+def run_c3(args):
+    m = measure_c3(args.split, args.steps)
+    line = {"metric": "docks/s (batched uneven GA, 64 complexes, pop 150, 50 generations, CUDA graphs)",
+            "value": m["docks_per_s"], "unit": "docks/s", "n_gpus": 1, "steps": m["steps"], "warmup": 1,
+            "ms_per_step": m["seconds_per_64_docks"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": C3_WORKLOAD, "receptor_atoms": m["receptor_atoms"],
+                       "ligand_atoms": m["ligand_atoms"]},
+            **{k: m[k] for k in ("poses_per_s", "pair_evals_per_s", "fcc_clustering", "autotune",
+                                 "plain_fp64_pair_evals_per_s", "f32_batched_over_plain_f64", "cpu_baseline")}}
     print(json.dumps(line), flush=True)
 
 
-def run_c4(args):
+C4_WORKLOAD = ("Poisson arrivals of synthetic complexes (receptor 100-800, ligand 50-300 residues, log-uniform), "
+               "GA pop 150, early stopping after 10 stagnant generations, cap 200; 64 slots")
+
+
+def measure_c4(split: str = "auto", rates=(1.0, 8.0, 32.0, 200.0), per_rate: int = 32, fp64_jobs: int = 2) -> dict:
+    """Served docking jobs: for each offered rate, Poisson arrivals into the
+    server (continuous batching over 64 slots) until max(per_rate, rate x 1 s)
+    jobs are in; jobs/s over the whole run and p50/p99 submit -> done latency.
+    Beside it the plain FP64 form running jobs one at a time, and the CPU
+    oracle's jobs/s."""
     import gdock_gb300 as gd
     from gdock_gb300 import _lib
     ctx = gd.Context(0)
-    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[split])
     pool = _uneven_complexes(48, 44)
     ga = _lib.ga_default_cfg(pop_size=150, max_generations=200, early_stopping=1)
-    rates = [float(r) for r in os.environ.get("GD_C4_RATES", "1,8,32,200").split(",")]
-    per_rate = int(os.environ.get("GD_C4_JOBS", "32"))
     sweep = []
     for rate in rates:
         srv = gd.Server(ctx, max_slots=64, ga=ga)
@@ -427,14 +458,13 @@ def run_c4(args):
     # plain FP64 beside it: sample jobs run one at a time to completion (same
     # GA settings, early stopping), no batching
     t64 = []
-    for k, (r, l, p) in enumerate(pool[:2]):
+    for k, (r, l, p) in enumerate(pool[:fp64_jobs]):
         cx64 = gd.Complex(r, l, p, ctx=ctx)
         cfg64 = _lib.ga_default_cfg(pop_size=150, max_generations=200, early_stopping=1, seed=1000 + k)
         t0 = time.perf_counter()
         gd.run_ga([cx64], cfg64, gd.GD_PREC_F64, use_graph=False, ctx=ctx)
         t64.append(time.perf_counter() - t0)
         cx64.close()
-    dt64, pairs64 = _fp64_ga_cost(gd, _lib, ctx, pool[:2], 150, 3)
     # CPU leg: the oracle scoring one generation (150 poses) of 4 of the pool's
     # complexes on all host threads, times the served jobs' mean generations
     # (+1 evaluation), one job after another
@@ -451,20 +481,30 @@ def run_c4(args):
     pair_frac = sum(len(r) * len(l) for r, l, _ in pool) / (len(pool) / 4 * sum(len(r) * len(l) for r, l, _ in pool[:4]))
     mean_gens = float(np.mean([x["mean_generations"] for x in sweep]))
     cpu_jobs = 1.0 / (t_gen * pair_frac * (mean_gens + 1))
+    ctx.close()
     best = max(sweep, key=lambda x: x["jobs_per_s"])
-    line = {"metric": "served docking jobs/s with p50/p99 latency (continuous batching)",
-            "value": best["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "Poisson arrivals of synthetic complexes (C3 sizes) swept over "
-                                   f"{rates} jobs/s, max({per_rate}, rate x 1 s) jobs per rate, GA pop 150, early "
-                                   "stopping after 10 stagnant generations, cap 200", "slots": 64},
-            "sweep": sweep, "plain_fp64_pair_evals_per_s": pairs64 / dt64,
+    return {"jobs_per_s": best["jobs_per_s"], "at_rate_jobs_per_s": best["rate_jobs_per_s"],
+            "latency_p50_s": best["latency_p50_s"], "latency_p99_s": best["latency_p99_s"],
+            "workload": C4_WORKLOAD, "sweep": sweep,
             "plain_fp64_one_job_at_a_time": {"jobs": len(t64), "seconds_per_job": float(np.mean(t64)),
                                              "jobs_per_s": len(t64) / float(np.sum(t64))},
             "cpu_baseline": {"value": cpu_jobs, "unit": "jobs/s", "cores": threads, "kind": "port",
                              "sample": "the oracle scoring one generation (150 poses) of 4 of the 48 complexes, "
                                        "extrapolated by pair count and the served jobs' mean generations"}}
+
+
+def run_c4(args):
+    rates = tuple(float(r) for r in os.environ.get("GD_C4_RATES", "1,8,32,200").split(","))
+    per_rate = int(os.environ.get("GD_C4_JOBS", "32"))
+    m = measure_c4(args.split, rates, per_rate)
+    line = {"metric": "served docking jobs/s with p50/p99 latency (continuous batching)",
+            "value": m["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{C4_WORKLOAD}; offered rates {list(rates)} jobs/s, max({per_rate}, rate x 1 s) "
+                                   "jobs per rate", "slots": 64},
+            **{k: m[k] for k in ("latency_p50_s", "latency_p99_s", "sweep", "plain_fp64_one_job_at_a_time",
+                                 "cpu_baseline")}}
     print(json.dumps(line), flush=True)
 
 
@@ -633,6 +673,9 @@ def main():
                     help="work items of the FP32 kernel (GD_TUNE_SPLIT): whole poses or ligand chunks")
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
+    ap.add_argument("--extras", default="all", choices=["all", "none"],
+                    help="c2 line: also measure the batched GA (docks/s) and the served jobs (jobs/s, p50/p99) "
+                         "after the scoring steps (all), or the scoring workload alone (none)")
     args = ap.parse_args()
     NP = args.poses
     if args.impl == "reference":
@@ -781,9 +824,15 @@ def main():
                              "sample": f"{args.cpu_sample} poses of the workload"},
             "clocks": clk.summary(),
         }
-        print(json.dumps(line), flush=True)
     cx.close()
     ctx.close()
+    if rank == 0 and world == 1 and args.extras == "all":
+        # the other half of the headline metric, measured in the same run:
+        # docks/s of the batched GA and served jobs/s with p50/p99 latency
+        line["batched_ga"] = measure_c3(args.split, 1)
+        line["served"] = measure_c4(args.split, rates=(32.0, 200.0), per_rate=32, fp64_jobs=2)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
 

@@ -314,6 +314,55 @@ static std::vector<int> slot_order(const double *x, const double *y, const doubl
   return order;
 }
 
+// Receptor atoms grouped into spatially compact segments of kRecSeg (the FP32
+// kernel's ring stage): recursive bisection along the longest extent of the
+// bounding box, the left part always a whole number of segments, so every
+// segment but the last is full.  Deterministic (a stable sort per level).
+// Returns order[k] = original index of the atom at position k.
+static std::vector<int> segment_order(const double *x, const double *y, const double *z, int n) {
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  struct Span { int lo, hi; };
+  std::vector<Span> todo{{0, n}};
+  while (!todo.empty()) {
+    const Span sp = todo.back();
+    todo.pop_back();
+    const int m = sp.hi - sp.lo;
+    if (m <= kRecSeg) continue;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = sp.lo; k < sp.hi; ++k) {
+      const double v[3] = {x[order[k]], y[order[k]], z[order[k]]};
+      for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], v[a]), hi[a] = std::max(hi[a], v[a]);
+    }
+    int ax = 0;
+    for (int a = 1; a < 3; ++a)
+      if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+    const double *c = ax == 0 ? x : (ax == 1 ? y : z);
+    std::stable_sort(order.begin() + sp.lo, order.begin() + sp.hi, [c](int a, int b) { return c[a] < c[b]; });
+    const int nseg = (m + kRecSeg - 1) / kRecSeg;
+    const int mid = sp.lo + (nseg / 2) * kRecSeg;
+    todo.push_back({mid, sp.hi});
+    todo.push_back({sp.lo, mid});
+  }
+  return order;
+}
+
+// Bounding sphere (centroid, largest distance) of points, widened so that
+// FP32 images of the points and of the centre stay inside it.
+static float4 fp32_sphere(const std::vector<double> &x, const std::vector<double> &y, const std::vector<double> &z,
+                          const double o[3]) {
+  const size_t n = x.size();
+  double c[3] = {0, 0, 0};
+  for (size_t i = 0; i < n; ++i) c[0] += x[i], c[1] += y[i], c[2] += z[i];
+  for (double &v : c) v /= static_cast<double>(std::max<size_t>(n, 1));
+  double r = 0.0;
+  for (size_t i = 0; i < n; ++i)
+    r = std::max(r, std::sqrt((x[i] - c[0]) * (x[i] - c[0]) + (y[i] - c[1]) * (y[i] - c[1]) +
+                              (z[i] - c[2]) * (z[i] - c[2])));
+  return make_float4(static_cast<float>(c[0] - o[0]), static_cast<float>(c[1] - o[1]),
+                     static_cast<float>(c[2] - o[2]), static_cast<float>(r * (1.0 + 1e-6) + 0.01));
+}
+
 static void centroid(const double *x, const double *y, const double *z, int n, double *c) {
   double sx = -0.0, sy = -0.0, sz = -0.0;  // left folds, as Molecule::center_of_mass
   for (int i = 0; i < n; ++i) sx += x[i];
@@ -520,15 +569,31 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   std::vector<int2> rmeta(cx->nr_pad, make_int2(0, 0));
   std::vector<double> rdes(static_cast<size_t>(std::max(rec->n, 1)) * 11, 0.0);
   double ext = 0.0;
-  for (int i = 0; i < rec->n; ++i) {
-    rp32[i] = make_float4(static_cast<float>(rec->x[i] - o[0]), static_cast<float>(rec->y[i] - o[1]),
+  // receptor in compact segments (sums are order-free; the burial tables
+  // follow the same order)
+  const std::vector<int> rperm = segment_order(rec->x, rec->y, rec->z, rec->n);
+  for (int k = 0; k < rec->n; ++k) {
+    const int i = rperm[k];
+    rp32[k] = make_float4(static_cast<float>(rec->x[i] - o[0]), static_cast<float>(rec->y[i] - o[1]),
                           static_cast<float>(rec->z[i] - o[2]), static_cast<float>(332.0636 * rec->charge[i]));
-    rp64[i] = D4{rec->x[i], rec->y[i], rec->z[i], rec->charge[i]};
-    rmeta[i] = make_int2(rtype[i] * nt, rec->serial[i]);
-    desolv_row(rec->element[i], rec->vdw_radius[i], &rdes[static_cast<size_t>(i) * 11]);
+    rp64[k] = D4{rec->x[i], rec->y[i], rec->z[i], rec->charge[i]};
+    rmeta[k] = make_int2(rtype[i] * nt, rec->serial[i]);
+    desolv_row(rec->element[i], rec->vdw_radius[i], &rdes[static_cast<size_t>(k) * 11]);
     ext = std::max({ext, std::fabs(rec->x[i] - o[0]), std::fabs(rec->y[i] - o[1]), std::fabs(rec->z[i] - o[2])});
   }
   cx->rec_extent = ext;
+  // bounding sphere of each segment (FP32, relative to O)
+  cx->nseg = (rec->n + kRecSeg - 1) / kRecSeg;
+  std::vector<float4> rseg(std::max(cx->nseg, 1), make_float4(0.f, 0.f, 0.f, -1.f));
+  for (int g = 0; g < cx->nseg; ++g) {
+    std::vector<double> sx, sy, sz;
+    for (int k = g * kRecSeg; k < std::min(rec->n, (g + 1) * kRecSeg); ++k) {
+      sx.push_back(rec->x[rperm[k]]);
+      sy.push_back(rec->y[rperm[k]]);
+      sz.push_back(rec->z[rperm[k]]);
+    }
+    rseg[g] = fp32_sphere(sx, sy, sz, o);
+  }
   // ligand on the device in slot order (sums are order-free; restraint and
   // model indices go through the permutation)
   const std::vector<int> perm = slot_order(lig->x, lig->y, lig->z, lig->n);
@@ -551,6 +616,21 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
     rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
   }
   cx->lig_radius = rad;
+  // bounding sphere of each 32-atom slot in the positioned frame: a pose moves
+  // it rigidly, so its transformed centre and the same radius bound the
+  // slot's atoms in every pose
+  std::vector<D4> lslot(std::max((lig->n + 31) / 32, 1), D4{0.0, 0.0, 0.0, -1.0});
+  for (int s0 = 0; s0 < lig->n; s0 += 32) {
+    const int s1 = std::min(lig->n, s0 + 32);
+    double cs[3] = {0, 0, 0};
+    for (int k = s0; k < s1; ++k) cs[0] += lx[k], cs[1] += ly[k], cs[2] += lz[k];
+    for (double &v : cs) v /= (s1 - s0);
+    double r = 0.0;
+    for (int k = s0; k < s1; ++k)
+      r = std::max(r, std::sqrt((lx[k] - cs[0]) * (lx[k] - cs[0]) + (ly[k] - cs[1]) * (ly[k] - cs[1]) +
+                                (lz[k] - cs[2]) * (lz[k] - cs[2])));
+    lslot[s0 / 32] = D4{cs[0], cs[1], cs[2], r * (1.0 + 1e-6) + 0.01};
+  }
   {
     // equal receptor/ligand serials (vdW pairs skipped): disjoint serial
     // ranges, the usual case, settle it without a search
@@ -601,6 +681,8 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   pack.add(rr, &cx->restr_rec);
   pack.add(rl, &cx->restr_lig);
   pack.add(perm, &cx->lig_perm);
+  pack.add(rseg, &cx->rec_seg);
+  pack.add(lslot, &cx->lig_slot_sph);
   if ((s = pack.commit(cx)) != GD_OK) {
     gd_complex_destroy(cx);
     return s;

@@ -19,6 +19,10 @@ struct alignas(32) D4 {
 
 // Receptor atoms per tile staged in shared memory by one bulk (TMA) copy.
 constexpr int kTile = 256;
+// Receptor atoms per segment of the FP32 kernel's ring: the receptor is
+// stored as spatially compact segments of this many atoms, each with a
+// bounding sphere.
+constexpr int kRecSeg = 64;
 constexpr int kStages = 3;
 // Upper bounds of a device-side wait before it gives up: polls and wall time.
 constexpr uint32_t kSpinLimit = 1u << 26;
@@ -74,9 +78,11 @@ struct ScoreParams {
   const D4 *rec_pos64; // (x, y, z, q) FP64
   const int2 *rec_meta;     // (type, serial)
   const double *rec_desolv; // [nr * 11] energy contribution at burial count 0..10
-  int nr, n_tiles;
+  const float4 *rec_seg;    // per kRecSeg-atom segment: bounding sphere (centre - O, radius) FP32
+  int nr, n_tiles, nseg;
   // ligand in slot order (spatially compact runs of 32 atoms)
   const int *lig_perm;      // slot position -> original atom index
+  const D4 *lig_slot_sph;   // per 32-atom slot: bounding sphere in the positioned frame (centre, radius)
   const double *lig_x, *lig_y, *lig_z;
   const double *lig_q;
   const int *lig_type, *lig_serial;
@@ -156,6 +162,9 @@ struct gd_complex {
   D4 *restr_rec = nullptr;
   int *restr_lig = nullptr;
   int *lig_perm = nullptr;  // slot position -> original ligand atom index
+  float4 *rec_seg = nullptr;  // receptor segment spheres (FP32, relative to O)
+  D4 *lig_slot_sph = nullptr;  // ligand slot spheres (positioned frame)
+  int nseg = 0;
   std::vector<void *> allocs;
   uint64_t bytes = 0;
   // host copies used by clustering

@@ -243,6 +243,9 @@ ScoreParams make_params(gd_complex *cx, const gd_pose_frame *d_frames, const dou
   p.nr = cx->nr;
   p.n_tiles = cx->nr_pad / kTile;
   p.lig_perm = cx->lig_perm;
+  p.lig_slot_sph = cx->lig_slot_sph;
+  p.rec_seg = cx->rec_seg;
+  p.nseg = cx->nseg;
   p.lig_x = cx->lig_x;
   p.lig_y = cx->lig_y;
   p.lig_z = cx->lig_z;

@@ -12,8 +12,12 @@
 //      stored in spatially compact slot order) and a bounding sphere and box
 //      per slot;
 //   3. streams the receptor through its own two-stage shared-memory ring,
-//      each stage filled by one bulk (TMA) copy of 64 atoms and guarded by a
-//      per-warp mbarrier with a bounded wait;
+//      each stage filled by one bulk (TMA) copy of a 64-atom segment and
+//      guarded by a per-warp mbarrier with a bounded wait; the receptor is
+//      stored as spatially compact segments with bounding spheres, and only
+//      the segments within reach of the chunk's slot spheres are copied and
+//      tested (the slot spheres are precomputed and move rigidly with the
+//      pose);
 //   4. row test: each lane takes one (receptor atom, slot) row of an 8 x 4
 //      round; a row whose atom lies beyond the 15 A reach of the slot's
 //      sphere or box is dropped (every pair of it contributes exactly
@@ -50,6 +54,8 @@ constexpr int kMaxS = 4;       // ligand slots per lane, at most (one row-test r
 constexpr int kList = kSeg + 8;  // row-list entries per slot: a segment's atoms + two paddings of 4 rows
 constexpr int kFar = kWS * kSeg; // shared-memory index of the far-away dummy receptor atom
 constexpr int kCntSmemMax = 4096;  // burial counters kept in shared memory up to this many receptor atoms
+constexpr int kSegListMax = 512;   // receptor segments a chunk's culled list holds (more: every segment)
+static_assert(kSeg == kRecSeg, "the ring stage is one receptor segment");
 
 struct BatchParams {
   const ScoreParams *descs;       // one per complex
@@ -77,7 +83,7 @@ struct BatchParams {
 };
 
 struct WarpSmem {
-  size_t pos, meta, list, fixq, cmask, cidx, lfix, bars, desc, frame, blob, box, rc, cnt, total;
+  size_t pos, meta, list, fixq, cmask, cidx, lfix, bars, desc, frame, blob, box, rc, ssph, segl, cnt, total;
 };
 
 __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
@@ -119,6 +125,11 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   o += sizeof(float4) * 2 * kMaxS;
   L.rc = o;
   o += sizeof(int) * kSeg;
+  L.ssph = o;  // the chunk's slot spheres (culling test of the receptor segments)
+  o += sizeof(float4) * kMaxS;
+  L.segl = o;  // the chunk's receptor segments within reach
+  o += sizeof(uint16_t) * kSegListMax;
+  al(16);
   L.cnt = o;
   o += smem_cnt;
   al(128);
@@ -262,15 +273,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   int2 *s_meta = reinterpret_cast<int2 *>(base + L.meta);
   uint16_t *s_list = reinterpret_cast<uint16_t *>(base + L.list);  // kept rows per slot, as stage indices
   uint16_t *s_fixq = reinterpret_cast<uint16_t *>(base + L.fixq);  // flagged steps: list position | slot << 8
-  int *s_lfix = reinterpret_cast<int *>(base + L.lfix);            // ligand burial corrections per slot and lane
   unsigned *s_cmask = reinterpret_cast<unsigned *>(base + L.cmask);  // near rows' burial ballots (this segment)
   uint16_t *s_cidx = reinterpret_cast<uint16_t *>(base + L.cidx);
+  int *s_lfix = reinterpret_cast<int *>(base + L.lfix);            // ligand burial corrections per slot and lane
   uint64_t *s_bar = reinterpret_cast<uint64_t *>(base + L.bars);
   ScoreParams *s_desc = reinterpret_cast<ScoreParams *>(base + L.desc);
   gd_pose_frame *s_frame = reinterpret_cast<gd_pose_frame *>(base + L.frame);
   float4 *s_blob = reinterpret_cast<float4 *>(base + L.blob);
   float4 *s_box = reinterpret_cast<float4 *>(base + L.box);  // per slot: (centre, hx), (hy, hz, -, -)
   int *s_rc = reinterpret_cast<int *>(base + L.rc);  // receptor burial counts of the current segment
+  float4 *s_ssph = reinterpret_cast<float4 *>(base + L.ssph);
+  uint16_t *s_segl = reinterpret_cast<uint16_t *>(base + L.segl);
   const int gwarp = static_cast<int>(blockIdx.x) * kWarps + wib;
   uint8_t *cnt = bp.smem_cnt ? reinterpret_cast<uint8_t *>(base + L.cnt)
                              : bp.gcounts + static_cast<size_t>(gwarp) * bp.gcount_stride;
@@ -326,12 +339,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     __syncwarp();
     const gd_pose_frame &f = *s_frame;
     const int nseg = (p.nr + kSeg - 1) / kSeg;
-    const long long Qi = static_cast<long long>(ch1 - ch0) * nseg;
-    const long long q0 = q;
-    if (lane == 0)
-      for (long long k = 0; k < Qi && k < kWS; ++k)
-        if (!(bp.drop_copy && item == 0 && k == 0))
-          issue_seg(q0 + k, static_cast<int>(k % nseg), p, s_pos, s_meta, s_bar);
+    long long q_issued = q;  // ring uses issued so far (lane 0 issues; read on failure)
     const float gv = p.guard_v, ge = p.guard_e, gdd = p.guard_d;
     // a row (receptor atom, ligand slot) whose atom lies farther than this
     // from the slot's bounding sphere has every FP32 d2 beyond the elec
@@ -346,6 +354,56 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     bool failed = false;
 
     for (int ch = ch0; ch < ch1 && !failed; ++ch) {
+      // Receptor segments within reach of the chunk: each slot's precomputed
+      // sphere moves rigidly with the pose (its centre transformed exactly),
+      // and a segment whose sphere lies beyond the elec reach of every slot
+      // sphere holds only rows the row test would drop.  Explicit model
+      // coordinates (no rigid pose) keep every segment.
+      const bool cull = p.models == nullptr && p.lig_slot_sph != nullptr && p.rec_seg != nullptr;
+      if (cull && lane < S) {
+        const int sl = ch * S + lane;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        if (sl * 32 < p.nl) {
+          const D4 sp = p.lig_slot_sph[sl];
+          double X, Y, Z;
+          transform_atom(f, p.cx, p.cy, p.cz, sp.x, sp.y, sp.z, X, Y, Z);
+          v = make_float4(static_cast<float>(X - p.ox), static_cast<float>(Y - p.oy), static_cast<float>(Z - p.oz),
+                          static_cast<float>(sp.w));
+        }
+        s_ssph[lane] = v;
+      }
+      __syncwarp();
+      int nk = nseg;
+      bool listed = false;
+      if (cull) {
+        nk = 0;
+        for (int g0 = 0; g0 < nseg; g0 += 32) {
+          const int g = g0 + lane;
+          bool keep = false;
+          if (g < nseg) {
+            const float4 sg = __ldg(&p.rec_seg[g]);
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) {
+              const float4 ss = s_ssph[s2];
+              const float dx = sg.x - ss.x, dy = sg.y - ss.y, dz = sg.z - ss.z;
+              const float lim = sg.w + ss.w + reach + 0.1f + 1e-3f * (sg.w + ss.w);
+              keep = keep || (ss.w >= 0.0f && dx * dx + dy * dy + dz * dz < lim * lim);
+            }
+          }
+          const unsigned m = __ballot_sync(kFull, keep);
+          const int pos = nk + __popc(m & lt_mask);
+          if (keep && pos < kSegListMax) s_segl[pos] = static_cast<uint16_t>(g);
+          nk += __popc(m);
+        }
+        listed = nk <= kSegListMax;
+        if (!listed) nk = nseg;  // too many to list: every segment
+        __syncwarp();
+      }
+      if (lane == 0)
+        for (int k = 0; k < nk && k < kWS; ++k)
+          if (!(bp.drop_copy && item == 0 && ch == ch0 && k == 0))
+            issue_seg(q + k, listed ? s_segl[k] : k, p, s_pos, s_meta, s_bar);
+      q_issued = q + min(nk, kWS);
       float lx[S], ly[S], lz[S], lq[S];
       int lt[S], lser[S], lcnt[S];
 #pragma unroll
@@ -422,7 +480,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
       // per segment: flagged steps (high 16 bits) and recorded near rows (low 16)
       int seg_cnt = 0;
-      for (int g = 0; g < nseg; ++g, ++q) {
+      for (int kk = 0; kk < nk; ++kk, ++q) {
+        const int g = listed ? s_segl[kk] : kk;
         const int st = static_cast<int>(q % kWS);
         const bool ok = __all_sync(kFull, mbar_wait(&s_bar[st], static_cast<uint32_t>((q / kWS) & 1)));
         if (!ok) {
@@ -458,6 +517,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           const int pf = nf_mine + __popc(Mf & my_group & lt_mask), pn = kList - 1 - nn_mine - __popc(Mn & my_group & lt_mask);
           if (keep && !nearr && GD_DCHECK(bp.err, pf >= 0 && pf < kList, 1)) my_list[pf] = idx;
           if (keep && nearr && GD_DCHECK(bp.err, pn >= 0 && pn < kList, 2)) my_list[pn] = idx;
+
           nf_mine += __popc(Mf & my_group);
           nn_mine += __popc(Mn & my_group);
         }
@@ -590,9 +650,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           }
         }
         __syncwarp();
-        const long long k = q - q0;  // index of this use within the item
-        if (lane == 0 && k + kWS < Qi)
-          issue_seg(q + kWS, static_cast<int>((k + kWS) % nseg), p, s_pos, s_meta, s_bar);
+        if (lane == 0 && kk + kWS < nk) {
+          issue_seg(q + kWS, listed ? s_segl[kk + kWS] : kk + kWS, p, s_pos, s_meta, s_bar);
+          q_issued = q + kWS + 1;
+        }
       }
       if (failed) break;
       __syncwarp();
@@ -625,8 +686,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       // copies this warp still has in flight, and stop this warp
       if (lane == 0) {
         atomicExch(bp.err, kDevTimeout);
-        const long long issued = q0 + (Qi < q - q0 + kWS ? Qi : q - q0 + kWS);
-        for (long long u = q; u < issued; ++u) mbar_wait(&s_bar[u % kWS], static_cast<uint32_t>((u / kWS) & 1));
+        for (long long u = q; u < q_issued; ++u) mbar_wait(&s_bar[u % kWS], static_cast<uint32_t>((u / kWS) & 1));
       }
       __syncwarp();
       return;

@@ -453,7 +453,8 @@ def measure_c4(split: str = "auto", rates=(1.0, 8.0, 32.0, 200.0), per_rate: int
         srv.stop()
         sweep.append({"rate_jobs_per_s": rate, "jobs": jobs, "jobs_per_s": jobs / t_all,
                       "latency_p50_s": st.latency_p50_s, "latency_p99_s": st.latency_p99_s,
-                      "mean_generations": float(np.mean(gens)), "poses_scored": int(st.poses_scored)})
+                      "mean_generations": float(np.mean(gens)), "poses_scored": int(st.poses_scored),
+                      "gpu_busy_frac": st.gpu_busy_s / t_all})
         srv.close()
     # plain FP64 beside it: sample jobs run one at a time to completion (same
     # GA settings, early stopping), no batching
@@ -485,6 +486,7 @@ def measure_c4(split: str = "auto", rates=(1.0, 8.0, 32.0, 200.0), per_rate: int
     best = max(sweep, key=lambda x: x["jobs_per_s"])
     return {"jobs_per_s": best["jobs_per_s"], "at_rate_jobs_per_s": best["rate_jobs_per_s"],
             "latency_p50_s": best["latency_p50_s"], "latency_p99_s": best["latency_p99_s"],
+            "gpu_busy_frac": best["gpu_busy_frac"],
             "workload": C4_WORKLOAD, "sweep": sweep,
             "plain_fp64_one_job_at_a_time": {"jobs": len(t64), "seconds_per_job": float(np.mean(t64)),
                                              "jobs_per_s": len(t64) / float(np.sum(t64))},

@@ -240,6 +240,8 @@ pub struct gd_server_stats {
     pub latency_p50_s: f64,
     pub latency_p99_s: f64,
     pub latency_max_s: f64,
+    pub gpu_busy_s: f64,
+    pub elapsed_s: f64,
 }
 
 // ------------------------------------------------------------- entry points

@@ -85,7 +85,8 @@ class GdJobResult(C.Structure):
 class GdServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("queued", C.c_int64), ("resident", C.c_int64),
                 ("generations_run", C.c_int64), ("poses_scored", C.c_int64), ("device_bytes", C.c_uint64),
-                ("latency_p50_s", C.c_double), ("latency_p99_s", C.c_double), ("latency_max_s", C.c_double)]
+                ("latency_p50_s", C.c_double), ("latency_p99_s", C.c_double), ("latency_max_s", C.c_double),
+                ("gpu_busy_s", C.c_double), ("elapsed_s", C.c_double)]
 
 
 POSE_ENERGY_DTYPE = np.dtype([(k, np.float64) for k in

@@ -102,11 +102,15 @@ void draw_initial(Rng &rng, const gd_ga_cfg &c, double *genes) {
 
 // Pose frames from genes on the device (CUDA's sin/cos; the composite
 // entries in the reference's operation order).
+// slots (may be null): the k-th group of n poses belongs to slot slots[k / n]
+// (the server's resident jobs); else pose k belongs to job job_of[k].
 __global__ void k_frames(const double *genes, gd_pose_frame *frames, const int *job_of, const GaJobState *state,
-                         int total) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= total) return;
-  if (state[job_of[k]].stop) return;
+                         int total, const int *slots, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int job = slots ? slots[t / n] : job_of[t];
+  const int k = slots ? job * n + t % n : t;
+  if (state[job].stop) return;
   const double *g = genes + 6 * static_cast<size_t>(k);
   double sa, ca, sb, cb, sg, cg;
   sincos(g[0], &sa, &ca);
@@ -144,6 +148,7 @@ struct GaStepParams {
   gd_dock_metrics *best_metrics;   // [jobs][max_gen]
   double *mean_dockq;              // [jobs][max_gen]
   int *err;                        // the context's error word (index checks of the debug library)
+  const int *slots;                // block b runs job slots[b] (the server's resident jobs); null: job b
   gd_ga_cfg cfg;
 };
 
@@ -397,7 +402,7 @@ inline size_t ga_step_smem(int n) {
 __global__ void __launch_bounds__(256) k_ga_step(const GaStepParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const gd_ga_cfg &c = P.cfg;
-  const int job = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int job = P.slots ? P.slots[blockIdx.x] : static_cast<int>(blockIdx.x), tid = threadIdx.x, nt = blockDim.x;
   const int n = c.pop_size, m = 2 * (n / 2), P2 = pow2_at_least(n);
   double *f = reinterpret_cast<double *>(smem);                            // [n] fitness of the population
   unsigned long long *kb = reinterpret_cast<unsigned long long *>(f + n);  // [P2] sort keys
@@ -761,7 +766,7 @@ extern "C" gd_status gd_ga_run(gd_context *ctx, gd_complex *const *complexes, in
     cudaStream_t st = ctx->stream;
     auto generation = [&]() -> gd_status {
       const int total = static_cast<int>(jn);
-      k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total);
+      k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total, nullptr, n);
       cudaError_t ee = cudaGetLastError();
       if (ee != cudaSuccess) return cuda_fail(ctx, ee, "frames kernel");
       if (prec == GD_PREC_F32) {
@@ -946,6 +951,14 @@ struct gd_server {
   // host time per tick phase (GD_TRACE prints the totals when the server is destroyed)
   double t_admit = 0, t_load = 0, t_prepare = 0, t_gpu = 0, t_retire = 0;
   bool started_clock = false;
+  // admission beside the running generation: uploads go to their own stream,
+  // the next generation waits for them (ev_up)
+  cudaStream_t up = nullptr;
+  cudaEvent_t ev_up = nullptr, ev0 = nullptr, ev1 = nullptr;
+  bool upload_pending = false;
+  gd::GaJobState *h_states = nullptr;  // pinned: the slots' states after a generation
+  int *d_slots = nullptr;              // the slots of the resident jobs (k_frames, k_ga_step)
+  double gpu_busy = 0;                 // device time of the generations (CUDA events), seconds
 };
 
 namespace gd {
@@ -996,6 +1009,14 @@ gd_status server_alloc(gd_server *S) {
     if ((s = A(hb, &p)) != GD_OK) return s;
     R.hof_tmp = static_cast<gd_hof_entry *>(p);
   }
+  if ((s = A(sizeof(int) * J, &p)) != GD_OK) return s;
+  S->d_slots = static_cast<int *>(p);
+  cudaError_t ce = cudaMallocHost(reinterpret_cast<void **>(&S->h_states), sizeof(GaJobState) * J);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&S->up, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&S->ev_up, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&S->ev0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&S->ev1);
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "server streams and events");
   std::vector<int> job_of(jn);
   for (size_t k = 0; k < jn; ++k) job_of[k] = static_cast<int>(k / n);
   std::vector<GaJobState> st(J, GaJobState{0, kStopFree, 0, 0, 0.0, 0, 0});
@@ -1004,6 +1025,17 @@ gd_status server_alloc(gd_server *S) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "server arena");
   S->slot_job.assign(J, nullptr);
   return GD_OK;
+}
+
+void server_free_host(gd_server *S) {
+  if (S->h_states) cudaFreeHost(S->h_states);
+  if (S->up) cudaStreamDestroy(S->up);
+  if (S->ev_up) cudaEventDestroy(S->ev_up);
+  if (S->ev0) cudaEventDestroy(S->ev0);
+  if (S->ev1) cudaEventDestroy(S->ev1);
+  S->h_states = nullptr;
+  S->up = nullptr;
+  S->ev_up = S->ev0 = S->ev1 = nullptr;
 }
 
 // Upload a job's draws and initial state into slot j.
@@ -1030,7 +1062,9 @@ gd_status server_load_slot(gd_server *S, int j, Job *job) {
   const size_t gT = static_cast<size_t>(c.tournament_size) * n, gC = 6 * static_cast<size_t>(n / 2),
                gM = 6 * static_cast<size_t>(m);
   const size_t Gs = static_cast<size_t>(G);
-  cudaStream_t st = S->ctx->stream;
+  // the admission stream: slot j is not part of the generation that may be
+  // running on the context's stream, and the next one waits for these copies
+  cudaStream_t st = S->up;
   cudaError_t e = cudaMemcpyAsync(R.genes + static_cast<size_t>(j) * n * 6, job->d_init.data(),
                                   sizeof(double) * job->d_init.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && G > 0) {
@@ -1060,15 +1094,16 @@ gd_status server_load_slot(gd_server *S, int j, Job *job) {
   return GD_OK;
 }
 
-// One tick: admit, run one generation of every resident job, retire.
-gd_status server_tick(gd_server *S, int *active_out) {
-  gd::NvtxRange nvtx_range("server_tick");
+// Admission: queued jobs, first come first served, into free slots while the
+// HBM budget allows.  Each admitted job's complex is created (host packing,
+// one allocation and one copy) and its draws and state are uploaded on the
+// admission stream; the generation that is running meanwhile does not touch
+// free slots.
+gd_status server_admit(gd_server *S) {
   gd_context *ctx = S->ctx;
-  const gd_ga_cfg &c = S->cfg.ga;
-  GaRun &R = S->arena;
-  const int J = S->cfg.max_slots, n = c.pop_size;
+  const int J = S->cfg.max_slots;
   gd_status s = GD_OK;
-  // 1. admission: FIFO into free slots while the HBM budget allows
+  bool uploaded = false;
   for (;;) {
     int free_slot = -1;
     for (int j = 0; j < J; ++j)
@@ -1089,7 +1124,10 @@ gd_status server_tick(gd_server *S, int *active_out) {
     s = gd_complex_create(ctx, &ra, &la, job->pairs.empty() ? nullptr : job->pairs.data(),
                           static_cast<int32_t>(job->pairs.size() / 2), &job->w, &cx);
     S->t_admit += std::chrono::duration<double>(Clock::now() - ta).count();
-    if (s == GD_ERR_OOM) break;  // wait for a resident job to finish
+    if (s == GD_ERR_OOM) {  // wait for a resident job to finish
+      s = GD_OK;
+      break;
+    }
     const uint64_t bytes = ctx->in_use - before;
     if (s == GD_OK && S->cfg.hbm_budget && S->job_bytes + bytes > S->cfg.hbm_budget && S->job_bytes > 0) {
       gd_complex_destroy(cx);  // over the server's budget: admit later
@@ -1103,6 +1141,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
         job->error = s;
         job->t_done = Clock::now();
         S->cv.notify_all();
+        s = GD_OK;
         continue;
       }
       job->cx = cx;
@@ -1117,98 +1156,149 @@ gd_status server_tick(gd_server *S, int *active_out) {
     s = server_load_slot(S, free_slot, job);
     S->t_load += std::chrono::duration<double>(Clock::now() - tl).count();
     if (s != GD_OK) return s;
+    uploaded = true;
   }
-  int active = 0;
-  for (Job *j : S->slot_job) active += j != nullptr;
-  if (active_out) *active_out = active;
-  if (active == 0) return GD_OK;
-  // 2. one generation for all resident jobs
-  std::vector<ScoreParams> descs(J);
-  bool serial = false, clamp = false;
-  for (int j = 0; j < J; ++j) {
-    Job *job = S->slot_job[j];
-    if (job) {
-      descs[j] = make_params(job->cx, R.frames + static_cast<size_t>(j) * n, nullptr, n,
-                             R.energies + static_cast<size_t>(j) * n, c.max_displacement);
-      descs[j].skip = &R.state[j].stop;
-      serial |= job->cx->serial_overlap;
-      clamp |= job->cx->need_clamp;
-    } else {
-      descs[j] = ScoreParams{};
-      descs[j].n_poses = 0;
-    }
+  if (uploaded) {
+    const cudaError_t e = cudaEventRecord(S->ev_up, S->up);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "server admission event");
+    S->upload_pending = true;
   }
+  return s;
+}
+
+// One tick: one generation of every resident job (continuous batching), the
+// admission of queued jobs while it runs, then the retirement of the jobs it
+// finished.  With no job resident the admission comes first, so that an idle
+// server starts new work in the same tick.
+gd_status server_tick(gd_server *S, int *active_out) {
+  gd::NvtxRange nvtx_range("server_tick");
+  gd_context *ctx = S->ctx;
+  const gd_ga_cfg &c = S->cfg.ga;
+  GaRun &R = S->arena;
+  const int J = S->cfg.max_slots, n = c.pop_size;
+  gd_status s = GD_OK;
+  auto resident = [&]() {
+    int a = 0;
+    for (Job *j : S->slot_job) a += j != nullptr;
+    return a;
+  };
+  if (resident() == 0) {
+    s = server_admit(S);
+    if (s != GD_OK) return s;
+  }
+  // 1. one generation for the resident jobs
+  std::vector<int> slots;
+  for (int j = 0; j < J; ++j)
+    if (S->slot_job[j]) slots.push_back(j);
+  const int active = static_cast<int>(slots.size());
   cudaStream_t st = ctx->stream;
-  const int total = J * n;
   const auto tg = Clock::now();
-  k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "frames kernel");
-  if (S->cfg.precision == GD_PREC_F32) {
-    // the argument block only changes when jobs enter or leave a slot
-    if (S->dirty || !S->bl) {
+  if (active > 0) {
+    cudaError_t e = cudaSuccess;
+    if (S->upload_pending) {  // the admitted jobs' uploads come first
+      e = cudaStreamWaitEvent(st, S->ev_up, 0);
+      S->upload_pending = false;
+    }
+    if (e == cudaSuccess && S->dirty)
+      e = cudaMemcpyAsync(S->d_slots, slots.data(), sizeof(int) * active, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "server tick set-up");
+    if (S->cfg.precision == GD_PREC_F32 && (S->dirty || !S->bl)) {
+      // the argument block only changes when jobs enter or leave a slot
+      std::vector<ScoreParams> descs(J);
+      bool serial = false, clamp = false;
+      for (int j = 0; j < J; ++j) {
+        Job *job = S->slot_job[j];
+        if (job) {
+          descs[j] = make_params(job->cx, R.frames + static_cast<size_t>(j) * n, nullptr, n,
+                                 R.energies + static_cast<size_t>(j) * n, c.max_displacement);
+          descs[j].skip = &R.state[j].stop;
+          serial |= job->cx->serial_overlap;
+          clamp |= job->cx->need_clamp;
+        } else {
+          descs[j] = ScoreParams{};
+          descs[j].n_poses = 0;
+        }
+      }
       if (S->bl) batch_free(ctx, S->bl);
       S->bl = nullptr;
       const auto tp = Clock::now();
       s = batch_prepare(ctx, descs, serial, clamp, ctx->tune_f32_slots ? ctx->tune_f32_slots : kDefaultF32Tune, &S->bl);
       S->t_prepare += std::chrono::duration<double>(Clock::now() - tp).count();
-      S->dirty = false;
+      if (s != GD_OK) return s;
     }
-    if (s == GD_OK) s = batch_launch(ctx, S->bl, st);
-  } else {
-    for (int j = 0; j < J && s == GD_OK; ++j)
-      if (S->slot_job[j])
-        s = launch_score(S->slot_job[j]->cx, descs[j].frames, nullptr, n, GD_PREC_F64, descs[j].out, st,
-                         c.max_displacement);
+    S->dirty = false;
+    const int total = active * n;
+    cudaEventRecord(S->ev0, st);
+    k_frames<<<(total + 255) / 256, 256, 0, st>>>(R.genes, R.frames, R.job_of, R.state, total, S->d_slots, n);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "frames kernel");
+    if (S->cfg.precision == GD_PREC_F32) {
+      s = batch_launch(ctx, S->bl, st);
+    } else {
+      for (int j : slots) {
+        if (s != GD_OK) break;
+        s = launch_score(S->slot_job[j]->cx, R.frames + static_cast<size_t>(j) * n, nullptr, n, GD_PREC_F64,
+                         R.energies + static_cast<size_t>(j) * n, st, c.max_displacement);
+      }
+    }
+    if (s != GD_OK) return s;
+    GaStepParams P{};
+    P.genes = R.genes;
+    P.genes_tmp = R.genes_tmp;
+    P.energies = R.energies;
+    P.state = R.state;
+    P.history = R.history;
+    P.tour = R.tour;
+    P.perm = R.perm;
+    P.cross_u = R.cross_u;
+    P.mut_u = R.mut_u;
+    P.mut_z = R.mut_z;
+    P.hof = R.hof;
+    P.hof_tmp = R.hof_tmp;
+    P.err = ctx->d_err;
+    P.slots = S->d_slots;
+    P.cfg = c;
+    const size_t ga_smem = ga_step_smem(n);
+    if (ga_smem > 48 * 1024)
+      cudaFuncSetAttribute(k_ga_step, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ga_smem));
+    k_ga_step<<<active, 256, ga_smem, st>>>(P);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "GA step kernel");
+    cudaEventRecord(S->ev1, st);
+    e = cudaMemcpyAsync(S->h_states, R.state, sizeof(GaJobState) * J, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "server tick");
+    // 2. admission while the generation runs
+    s = server_admit(S);
+    if (s != GD_OK) return s;
+    // 3. the generation's end
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "server tick");
+    s = check_device_error(ctx);
+    if (s != GD_OK) return s;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, S->ev0, S->ev1) == cudaSuccess) S->gpu_busy += 1e-3 * ms;
+    S->generations_run += 1;
+    S->poses_scored += static_cast<int64_t>(active) * n;
   }
-  if (s != GD_OK) return s;
-  GaStepParams P{};
-  P.genes = R.genes;
-  P.genes_tmp = R.genes_tmp;
-  P.energies = R.energies;
-  P.state = R.state;
-  P.history = R.history;
-  P.tour = R.tour;
-  P.perm = R.perm;
-  P.cross_u = R.cross_u;
-  P.mut_u = R.mut_u;
-  P.mut_z = R.mut_z;
-  P.hof = R.hof;
-  P.hof_tmp = R.hof_tmp;
-  P.err = ctx->d_err;
-  P.cfg = c;
-  const size_t ga_smem = ga_step_smem(n);
-  if (ga_smem > 48 * 1024)
-    cudaFuncSetAttribute(k_ga_step, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(ga_smem));
-  k_ga_step<<<J, 256, ga_smem, st>>>(P);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "GA step kernel");
-  std::vector<GaJobState> states(J);
-  e = cudaMemcpyAsync(states.data(), R.state, sizeof(GaJobState) * J, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "server tick");
-  s = check_device_error(ctx);
-  if (s != GD_OK) return s;
   S->t_gpu += std::chrono::duration<double>(Clock::now() - tg).count();
   const auto tr = Clock::now();
-  S->generations_run += 1;
-  S->poses_scored += static_cast<int64_t>(active) * n;
-  // 3. retire finished jobs
-  for (int j = 0; j < J; ++j) {
+  // 4. retire the jobs this generation finished (only the slots it ran)
+  for (int j : slots) {
     Job *job = S->slot_job[j];
-    if (!job || states[j].stop == 0) continue;
-    job->generations = states[j].gen;
+    const GaJobState &sj = S->h_states[j];
+    if (!job || sj.stop == 0) continue;
+    job->generations = sj.gen;
     job->genes.resize(static_cast<size_t>(n) * 6);
     job->energies.resize(n);
     job->history.resize(std::max(c.max_generations, 0));
-    e = cudaMemcpy(job->genes.data(), R.genes + static_cast<size_t>(j) * n * 6, sizeof(double) * n * 6,
-                   cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(job->genes.data(), R.genes + static_cast<size_t>(j) * n * 6, sizeof(double) * n * 6,
+                               cudaMemcpyDeviceToHost);
     if (e == cudaSuccess)
       e = cudaMemcpy(job->energies.data(), R.energies + static_cast<size_t>(j) * n, sizeof(gd_pose_energy) * n,
                      cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && c.max_generations > 0)
       e = cudaMemcpy(job->history.data(), R.history + static_cast<size_t>(j) * c.max_generations,
                      sizeof(double) * c.max_generations, cudaMemcpyDeviceToHost);
-    job->hof.resize(R.hof ? states[j].hof_n : 0);
+    job->hof.resize(R.hof ? sj.hof_n : 0);
     if (e == cudaSuccess && !job->hof.empty())
       e = cudaMemcpy(job->hof.data(), R.hof + static_cast<size_t>(j) * (c.hof_max_size + 1),
                      sizeof(gd_hof_entry) * job->hof.size(), cudaMemcpyDeviceToHost);
@@ -1220,7 +1310,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
     S->job_bytes -= std::min<uint64_t>(S->job_bytes, before - ctx->in_use);
     job->cx = nullptr;
     // history entries past the generations this job ran are not its own
-    const int valid = std::min(c.max_generations, states[j].stop == 1 ? states[j].gen + 1 : states[j].gen);
+    const int valid = std::min(c.max_generations, sj.stop == 1 ? sj.gen + 1 : sj.gen);
     for (int g = std::max(valid, 0); g < c.max_generations; ++g) job->history[g] = NAN;
     S->dirty = true;
     std::lock_guard<std::mutex> lock(S->mu);
@@ -1232,6 +1322,7 @@ gd_status server_tick(gd_server *S, int *active_out) {
     S->cv.notify_all();
   }
   S->t_retire += std::chrono::duration<double>(Clock::now() - tr).count();
+  if (active_out) *active_out = resident();
   return GD_OK;
 }
 
@@ -1267,6 +1358,7 @@ gd_status gd_server_create(gd_context *ctx, const gd_server_cfg *cfg, gd_server 
   gd_status s = gd::server_alloc(S);
   if (s != GD_OK) {
     gd::ga_release(ctx, S->arena);
+    gd::server_free_host(S);
     delete S;
     return s;
   }
@@ -1450,6 +1542,8 @@ gd_status gd_server_get_stats(gd_server *S, gd_server_stats *out) {
   out->latency_p50_s = pct(0.50);
   out->latency_p99_s = pct(0.99);
   out->latency_max_s = l.empty() ? 0.0 : l.back();
+  out->gpu_busy_s = S->gpu_busy;
+  out->elapsed_s = S->started_clock ? std::chrono::duration<double>(Clock::now() - S->t_first).count() : 0.0;
   return GD_OK;
 }
 
@@ -1463,10 +1557,12 @@ gd_status gd_server_destroy(gd_server *S) {
   gd::trace("server: retire", S->t_retire);
   cudaSetDevice(S->ctx->device);
   cudaStreamSynchronize(S->ctx->stream);
+  if (S->up) cudaStreamSynchronize(S->up);
   for (auto *j : S->slot_job)
     if (j && j->cx) gd_complex_destroy(j->cx);
   if (S->bl) gd::batch_free(S->ctx, S->bl);
   gd::ga_release(S->ctx, S->arena);
+  gd::server_free_host(S);
   for (auto &kv : S->jobs) delete kv.second;
   delete S;
   return GD_OK;

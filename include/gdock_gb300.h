@@ -354,6 +354,8 @@ typedef struct gd_server_stats {
   int64_t completed, queued, resident, generations_run, poses_scored;
   uint64_t device_bytes;
   double latency_p50_s, latency_p99_s, latency_max_s;
+  double gpu_busy_s;  /* device time of the generations run (CUDA events) */
+  double elapsed_s;   /* since the first submission */
 } gd_server_stats;
 
 gd_status gd_server_default_cfg(gd_server_cfg *cfg);

@@ -84,18 +84,48 @@ def test_server_matches_batched_ga_run():
     srv.close()
 
 
-def test_admission_by_hbm_budget_and_background_thread():
+def test_admission_by_hbm_budget_tick_by_tick():
+    """A budget of one byte holds one resident job at a time (the first job
+    is admitted even over it): driven tick by tick, at most one job is ever
+    resident, the jobs finish in submission order (first come first served),
+    and the device time of the generations is counted."""
     ctx = gd.Context(0)
     J = jobs(4)
-    srv = gd.Server(ctx, max_slots=4, hbm_budget=1, ga=ga_cfg())  # room for one resident job at a time
+    srv = gd.Server(ctx, max_slots=4, hbm_budget=1, ga=ga_cfg())
+    ids = [srv.submit(*J[i], seed=7 + i) for i in range(4)]
+    done_order, ticks = [], 0
+    while True:
+        resident = srv.step()
+        ticks += 1
+        assert resident <= 1, ticks
+        assert srv.stats().resident == resident
+        for jid in ids:
+            if jid not in done_order and srv.result(jid)[0].status == _lib.GD_JOB_DONE:
+                done_order.append(jid)
+        if len(done_order) == len(ids):
+            break
+        assert ticks < 4 * 40, "jobs did not finish"
+    assert done_order == ids
+    st = srv.stats()
+    assert st.completed == 4 and st.queued == 0 and st.resident == 0
+    assert 0.0 < st.gpu_busy_s <= st.elapsed_s
+    for jid in ids:
+        res = srv.result(jid)[0]
+        assert res.queue_s >= 0 and res.latency_s >= res.queue_s
+    srv.close()
+
+
+def test_background_thread_with_budget():
+    ctx = gd.Context(0)
+    J = jobs(4)
+    srv = gd.Server(ctx, max_slots=4, hbm_budget=1, ga=ga_cfg())
     srv.start()
     ids = [srv.submit(*J[i], seed=7 + i) for i in range(4)]
-    peak = 0
     for jid in ids:
         assert srv.wait(jid, 300.0) == _lib.GD_JOB_DONE
     st = srv.stats()
     srv.stop()
-    assert st.completed == 4
+    assert st.completed == 4 and st.resident == 0
     for jid in ids:
         res = srv.result(jid)[0]
         assert res.queue_s >= 0 and res.latency_s >= res.queue_s

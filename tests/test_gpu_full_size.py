@@ -79,3 +79,34 @@ def test_c5_size_against_oracle(oracle):
     check(e32, as_array(e64), 1e-5)
     ref = oracle.score_poses(c.receptor, lig, c.restraint_pairs, genes[:2])
     check(e64[:2], ref, 1e-12)
+
+
+def test_receptor_beyond_the_segment_list(oracle):
+    """A receptor of 35,946 atoms has 562 segments of 64, more than a chunk's
+    culled-segment list holds (512): such chunks take every segment.  FP32
+    (both work-item modes, bit-identical) against FP64 and FP64 against the
+    oracle, with poses inside, at the surface of and far from the receptor."""
+    from gdock_gb300 import _lib
+    c = synth.make_complex(4300, 60, 4, seed=9)
+    assert len(c.receptor) > 512 * 64
+    lig = position_ligand(c.receptor, c.ligand)
+    rng = np.random.default_rng(10)
+    genes = np.concatenate([synth.quaternion_genes(rng, 8, half_box=20.0),
+                            synth.random_genes(rng, 6, max_displacement=50.0)])
+    genes[-1, 3:] = (400.0, 0.0, 0.0)  # nothing within reach
+    ctx = gd.Context(0)
+    try:
+        cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+        out = {}
+        for mode in (1, 2):
+            ctx.set_tuning(_lib.GD_TUNE_SPLIT, mode)
+            out[mode] = cx.score_poses(genes, gd.GD_PREC_F32)
+        assert out[1].tobytes() == out[2].tobytes()
+        e64 = cx.score_poses(genes, gd.GD_PREC_F64)
+        check(out[1], as_array(e64), 1e-5)
+        ref = oracle.score_poses(c.receptor, lig, c.restraint_pairs, genes[[0, len(genes) - 1]])
+        check(e64[[0, len(genes) - 1]], ref, 1e-12)
+        assert e64["vdw"][-1] == 0.0 and e64["elec"][-1] == 0.0
+        cx.close()
+    finally:
+        ctx.close()

@@ -63,3 +63,33 @@ def test_debug_library_builds_and_exports_all_symbols():
     for name in declared_symbols():
         assert hasattr(lib, name), name
     assert lib.gd_abi_version() == 1
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """The header compiles as C99 with warnings as errors, and a C program that
+    takes the address of every entry point links against the library (no
+    call is made: no GPU is needed).  This is what an FFI binding generator
+    or a C host sees."""
+    import shutil
+    import subprocess
+    import pytest
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = build.build()
+    names = declared_symbols()
+    src = tmp_path / "use_abi.c"
+    src.write_text("#include \"gdock_gb300.h\"\n#include <stdio.h>\n"
+                   "typedef void (*any_fn)(void);\n"
+                   "int main(void) {\n  any_fn p[] = {\n"
+                   + "".join(f"    (any_fn)&{n},\n" for n in names)
+                   + "  };\n  printf(\"%d %d\\n\", (int)(sizeof(p) / sizeof(p[0])), (int)sizeof(gd_pose_frame));\n"
+                   "  return 0;\n}\n")
+    exe = tmp_path / "use_abi"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", f"-I{ROOT / 'include'}",
+                        str(src), "-o", str(exe), f"-L{lib.parent}", "-lgdock_gb300",
+                        f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == [str(len(names)), "128"]

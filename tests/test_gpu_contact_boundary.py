@@ -145,3 +145,21 @@ def test_cluster_on_boundary_contacts(oracle, fcc_mode):
             cx.close()
         finally:
             ctx.close()
+
+
+def test_hydrogens_make_no_contacts(oracle):
+    """calculate_contacts skips atoms whose element is H (src/clustering.rs:
+    67-70): hydrogens 3 A apart across the chains, or 3 A from a heavy atom,
+    make no contact; a heavy pair at 4 A does.  Both contact kernels."""
+    rec = make_mol([tatom(0.0, 0.0, 0.0, "C", name="CA", resseq=1, serial=1, chain="A"),
+                    tatom(0.0, 0.0, 20.0, "H", name="HA", resseq=2, serial=2, chain="A"),
+                    tatom(0.0, 30.0, 0.0, "N", name="N", resseq=3, serial=3, chain="A")])
+    lig = make_mol([tatom(0.0, 0.0, 23.0, "H", name="H", resseq=1, serial=11, chain="B"),
+                    tatom(4.0, 0.0, 0.0, "C", name="CB", resseq=2, serial=12, chain="B"),
+                    tatom(-3.0, 0.0, 0.0, "H", name="HB", resseq=3, serial=13, chain="B"),
+                    tatom(0.0, 27.0, 0.0, "H", name="H2", resseq=4, serial=14, chain="B")])
+    genes = np.zeros((2, 6))
+    genes[1, 3] = 0.5
+    want = contacts_all_paths(oracle, rec, lig, genes, [(0, 2), (1, 1)])
+    for keys in want:
+        assert keys.tolist() == [oracle.contact_key("A", 1, "B", 2)]

@@ -192,3 +192,25 @@ def test_integration_patches_are_unified_diffs(patch):
         o = sum(1 for l in lines if l[0] in " -")
         n = sum(1 for l in lines if l[0] in " +")
         assert (o, n) == (old_n, new_n), (patch.name, hunk.group(0)[:80])
+
+
+def test_integration_patches_apply_to_gdock(tmp_path):
+    """With a gdock checkout named by GDOCK_REF, the patches apply to a copy
+    of its sources in order, each without fuzz or offset complaints."""
+    import os
+    import shutil
+    import subprocess
+    ref = os.environ.get("GDOCK_REF")
+    if not ref or not (Path(ref) / "src").is_dir():
+        pytest.skip("GDOCK_REF (a gdock checkout) not set")
+    if shutil.which("patch") is None:
+        pytest.skip("no patch tool")
+    work = tmp_path / "gdock"
+    shutil.copytree(Path(ref) / "src", work / "src")
+    shutil.copy(Path(ref) / "Cargo.toml", work / "Cargo.toml")
+    for p in sorted((ROOT / "integration").glob("*.patch")):
+        r = subprocess.run(["patch", "-p1", "--no-backup-if-mismatch", "-i", str(p)], cwd=work,
+                           capture_output=True, text=True)
+        assert r.returncode == 0, (p.name, r.stdout, r.stderr)
+        assert "fuzz" not in r.stdout and "offset" not in r.stdout, (p.name, r.stdout)
+    assert (work / "src" / "gpu.rs").exists()

@@ -353,3 +353,24 @@ def test_hbm_budget_enforced(c1):
         gd.Complex(c1.receptor, positioned(c1), c1.restraint_pairs, ctx=ctx)
     assert ei.value.status == 2  # GD_ERR_OOM
     ctx.close()
+
+
+def test_clamped_lj_variant(oracle):
+    """Well depths above 50 kcal/mol make the soft-core LJ reach the
+    reference's clamp to [-50, 500] (src/fitness.rs:66-68): the kernels' clamp
+    variants, FP64 and FP32 (with segment culling on rigid poses), against the
+    oracle; equal serials on top select the variant with both."""
+    rng = np.random.default_rng(12)
+    for overlap in (False, True):
+        rec = make_mol([tatom(*rng.uniform(-6, 6, 3), "C", charge=rng.uniform(-0.5, 0.5), serial=1 + i,
+                              epsilon=-120.0 if i % 3 == 0 else -0.1, rmin2=2.2) for i in range(90)])
+        lig = make_mol([tatom(*rng.uniform(-4, 4, 3), "N", charge=rng.uniform(-0.5, 0.5),
+                              serial=(1 + i) if overlap else 500 + i, epsilon=-80.0 if i % 2 else -0.2, rmin2=1.9)
+                        for i in range(70)])
+        lig = gd.position_ligand(rec, lig)
+        genes = synth.random_genes(rng, 24, max_displacement=6.0)
+        cx = gd.Complex(rec, lig, [])
+        ref = oracle.score_poses(rec, lig, [], genes)
+        check(cx.score_poses(genes, gd.GD_PREC_F64), ref, F64_TOL)
+        check(cx.score_poses(genes, gd.GD_PREC_F32), ref, F32_TOL)
+        assert np.any(np.abs(ref[:, 1]) > 100.0)  # the clamp is reached

@@ -583,16 +583,22 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
               seg_cnt += 1 << 16;
             }
             // receptor burial counts of the step's rows: their ballots are
-            // recorded here and added up once per segment (below)
+            // recorded here and added up once per segment (below); a step
+            // with no pair within 8 A (about half of them) records nothing
+            int any_rc = 0;
 #pragma unroll
-            for (int i = 0; i < kAtoms; ++i) {
-              const unsigned bm = __ballot_sync(kFull, rc[i] != 0);
-              if (lane == i && GD_DCHECK(bp.err, (seg_cnt & 0xffff) + i < kMaxS * kList, 8)) {
-                s_cmask[(seg_cnt & 0xffff) + i] = bm;
-                s_cidx[(seg_cnt & 0xffff) + i] = static_cast<uint16_t>(ix[i]);
+            for (int i = 0; i < kAtoms; ++i) any_rc |= rc[i];
+            if (__any_sync(kFull, any_rc != 0)) {
+#pragma unroll
+              for (int i = 0; i < kAtoms; ++i) {
+                const unsigned bm = __ballot_sync(kFull, rc[i] != 0);
+                if (lane == i && GD_DCHECK(bp.err, (seg_cnt & 0xffff) + i < kMaxS * kList, 8)) {
+                  s_cmask[(seg_cnt & 0xffff) + i] = bm;
+                  s_cidx[(seg_cnt & 0xffff) + i] = static_cast<uint16_t>(ix[i]);
+                }
               }
+              seg_cnt += kAtoms;
             }
-            seg_cnt += kAtoms;
           }
           ae = __fmaf_rn(aes, lq[s], ae);
         }

@@ -146,15 +146,20 @@ __device__ __forceinline__ void issue_seg(long long q, int seg, const ScoreParam
   bulk_g2s(&s_meta[st * kSeg], p.rec_meta + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(int2), &s_bar[st]);
 }
 
-// acc += v when |t| < lim (one predicated add)
-// acc += v when t < 0
+// acc += v when t < 0 (one predicated add)
 __device__ __forceinline__ void add_if_lt0(float &acc, float t, float v) {
   asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, 0f00000000;\n\t@p add.f32 %0, %0, %2;\n\t}" : "+f"(acc)
       : "f"(t), "f"(v));
 }
-__device__ __forceinline__ void add_if_abs_lt(float &acc, float t, float lim, float v) {
-  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, %2;\n\t@p add.f32 %0, %0, %3;\n\t}" : "+f"(acc)
-      : "f"(fabsf(t)), "f"(lim), "f"(v));
+// acc = a * b + acc (one rounding) when t < 0
+__device__ __forceinline__ void fma_if_lt0(float &acc, float t, float a, float b) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, 0f00000000;\n\t@p fma.rn.f32 %0, %2, %3, %0;\n\t}" : "+f"(acc)
+      : "f"(t), "f"(a), "f"(b));
+}
+// acc = a * b + acc (one rounding) when |t| < lim
+__device__ __forceinline__ void fma_if_abs_lt(float &acc, float t, float lim, float a, float b) {
+  asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %1, %2;\n\t@p fma.rn.f32 %0, %3, %4, %0;\n\t}" : "+f"(acc)
+      : "f"(fabsf(t)), "f"(lim), "f"(a), "f"(b));
 }
 // a += 1 and b += 1 when d2 < 64
 __device__ __forceinline__ void count_if_lt64(int &a, int &b, float d2) {
@@ -191,29 +196,34 @@ __device__ __forceinline__ void pair32(const float4 &r, int rtrow, int rser, con
                                        float lz, int lt, int lser, float gv, float ge, float gdd, float &av,
                                        float &ae, int &lc, int &rc, bool &amb) {
   const float d2 = d2f(r, lx, ly, lz);
-  const float v = vdw_term<CLAMP>(d2, __ldg(&tab[rtrow + lt]));
+  const float2 tp = __ldg(&tab[rtrow + lt]);
   const float tv = __fsub_rn(d2, 144.0f);  // d2 < 144  <=>  tv < 0
-  if (SERIAL) {
-    av += (tv < 0.0f && rser != lser) ? v : 0.0f;
+  if (SERIAL || CLAMP) {
+    const float v = vdw_term<CLAMP>(d2, tp);
+    if (SERIAL) av += (tv < 0.0f && rser != lser) ? v : 0.0f;
+    else add_if_lt0(av, tv, v);
   } else {
-    add_if_lt0(av, tv, v);
+    // the well depth multiplies into the sum: one FMA (vdw_term without the
+    // product's own rounding)
+    const float x = rcp_approx(__fmaf_rn(d2 * d2 * d2, tp.x, 1.0f));
+    fma_if_lt0(av, tv, __fmaf_rn(x, x, -x), tp.y);
   }
-  const float e = r.w * rcp_approx(d2);
   const float te = __fsub_rn(d2, 113.0f);  // 1 < d2 < 225  <=>  |te| < 112
-  add_if_abs_lt(ae, te, 112.0f, e);
+  fma_if_abs_lt(ae, te, 112.0f, r.w, rcp_approx(d2));
   count_if_lt64(lc, rc, d2);
   amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge) | (fabsf(tv) < gv) | (fabsf(__fsub_rn(d2, 64.0f)) < gdd);
 }
 
 // One pair of a far row (no pair within the vdW cutoff): Coulomb only, the
-// same FP32 expressions and decision as pair32().
+// same FP32 expressions and decision as pair32().  Every FP32 d2 of a far
+// row exceeds 144, where d2 - 113 and d2 - 225 are exact (Sterbenz) and
+// |d2 - 113| < 112 is d2 < 225: one bound, one band.
 __device__ __forceinline__ void pair32_elec(const float4 &r, float lx, float ly, float lz, float ge, float &ae,
                                             bool &amb) {
   const float d2 = d2f(r, lx, ly, lz);
-  const float e = r.w * rcp_approx(d2);
-  const float te = __fsub_rn(d2, 113.0f);
-  add_if_abs_lt(ae, te, 112.0f, e);
-  amb = amb | (fabsf(__fsub_rn(fabsf(te), 112.0f)) < ge);
+  const float tf = __fsub_rn(d2, 225.0f);
+  fma_if_lt0(ae, tf, r.w, rcp_approx(d2));
+  amb = amb | (fabsf(tf) < ge);
 }
 
 __device__ __forceinline__ bool near_band(float d2, float gv, float ge, float gdd) {

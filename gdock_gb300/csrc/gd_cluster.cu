@@ -783,51 +783,6 @@ void group_atoms(const std::vector<uint8_t> &chain, const std::vector<int16_t> &
   }
 }
 
-// A small sphere enclosing atoms [a0, a1): the centre starts at the
-// centroid and moves toward the farthest atom with steps 1/(i + 1) (Badoiu
-// and Clarkson's iteration for the minimum enclosing ball), and the centre
-// with the smallest farthest-atom distance seen is kept, its radius being
-// that distance, so the sphere encloses every atom whatever the iteration
-// reached.  Sixteen steps bring protein residues' spheres within about 1 % of
-// the minimum, about 10 % smaller than the centroid's sphere.
-static void enclosing_sphere(const double *x, const double *y, const double *z, int a0, int a1, double c[3],
-                             double &r) {
-  c[0] = c[1] = c[2] = 0.0;
-  r = 0.0;
-  if (a1 <= a0) return;
-  double m[3] = {0.0, 0.0, 0.0};
-  for (int a = a0; a < a1; ++a) {
-    m[0] += x[a];
-    m[1] += y[a];
-    m[2] += z[a];
-  }
-  for (int k = 0; k < 3; ++k) m[k] /= (a1 - a0);
-  double best = -1.0;
-  for (int i = 1; i <= 16; ++i) {
-    int f = a0;
-    double d2max = -1.0;
-    for (int a = a0; a < a1; ++a) {
-      const double d2 = (x[a] - m[0]) * (x[a] - m[0]) + (y[a] - m[1]) * (y[a] - m[1]) + (z[a] - m[2]) * (z[a] - m[2]);
-      if (d2 > d2max) {
-        d2max = d2;
-        f = a;
-      }
-    }
-    if (best < 0.0 || d2max < best) {
-      best = d2max;
-      c[0] = m[0];
-      c[1] = m[1];
-      c[2] = m[2];
-    }
-    if (a1 - a0 == 1) break;
-    const double step = 1.0 / (i + 1);
-    m[0] += (x[f] - m[0]) * step;
-    m[1] += (y[f] - m[1]) * step;
-    m[2] += (z[f] - m[2]) * step;
-  }
-  r = std::sqrt(best);
-}
-
 gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
   gd_context *ctx = cx->ctx;
   ClusterTopo *t = new ClusterTopo();
@@ -861,7 +816,8 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
   std::vector<uint8_t> rch(t->GR), lch(t->GL);
   for (int g = 0; g < t->GR; ++g) {
     double c[3], r;
-    enclosing_sphere(rx.data(), ry.data(), rz.data(), t->rg_off[g], t->rg_off[g + 1], c, r);
+    const int a0 = t->rg_off[g];
+    enclosing_ball(rx.data() + a0, ry.data() + a0, rz.data() + a0, nullptr, t->rg_off[g + 1] - a0, c, r);
     rsph[g] = make_float4(static_cast<float>(c[0] - cx->ox), static_cast<float>(c[1] - cx->oy),
                           static_cast<float>(c[2] - cx->oz), static_cast<float>(r * (1 + 1e-6) + 1e-3));
     rch[g] = static_cast<uint8_t>(t->rg_key[g] >> 16);
@@ -869,7 +825,8 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
   std::vector<D4> lsph(t->GL);
   for (int g = 0; g < t->GL; ++g) {
     double c[3], r;
-    enclosing_sphere(lx.data(), ly.data(), lz.data(), t->lg_off[g], t->lg_off[g + 1], c, r);
+    const int a0 = t->lg_off[g];
+    enclosing_ball(lx.data() + a0, ly.data() + a0, lz.data() + a0, nullptr, t->lg_off[g + 1] - a0, c, r);
     lsph[g] = D4{c[0], c[1], c[2], r * (1 + 1e-6) + 1e-3};
     lch[g] = static_cast<uint8_t>(t->lg_key[g] >> 16);
   }
@@ -880,7 +837,8 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
   for (int b = 0; b < nb; ++b) {
     const int g0 = b * kLigBlock, g1 = std::min(t->GL, g0 + kLigBlock);
     double c[3], r;
-    enclosing_sphere(lx.data(), ly.data(), lz.data(), t->lg_off[g0], t->lg_off[g1], c, r);
+    const int a0 = t->lg_off[g0];
+    enclosing_ball(lx.data() + a0, ly.data() + a0, lz.data() + a0, nullptr, t->lg_off[g1] - a0, c, r);
     lbsph[b] = D4{c[0], c[1], c[2], r * (1 + 1e-6) + 1e-3};
   }
   gd_status s;

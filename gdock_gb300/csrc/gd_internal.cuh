@@ -200,6 +200,11 @@ void guard_widths(const gd_complex *cx, double max_disp, float *gv, float *ge, f
 gd_status launch_score(gd_complex *cx, const gd_pose_frame *d_frames, const double *d_models, int n,
                        gd_precision prec, gd_pose_energy *d_out, cudaStream_t stream, double max_disp);
 void free_cluster_cache(gd_complex *cx);
+// A small sphere enclosing n points (x[i], y[i], z[i]) for i = idx[k], or
+// i = k when idx is null; the radius is the largest distance from the
+// returned centre, so every point is enclosed (gd_api.cu).
+void enclosing_ball(const double *x, const double *y, const double *z, const int *idx, int n, double c[3],
+                    double &r);
 gd_status ensure_batch_scratch(gd_context *ctx, size_t dev_bytes);
 ScoreParams make_params(gd_complex *cx, const gd_pose_frame *d_frames, const double *d_models, int n,
                         gd_pose_energy *d_out, double max_disp);

@@ -438,23 +438,28 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           lt[s] = 0;
           lser[s] = 0;
         }
-        // bounding sphere of the slot's 32 atoms
+        // bounding sphere of the slot's 32 atoms: with a rigid pose the
+        // precomputed small enclosing sphere moved with it (s_ssph, smaller
+        // than the centroid's sphere), else the centroid's of these atoms
         const unsigned on_mask = __ballot_sync(kFull, on);
-        float cx = on ? lx[s] : 0.f, cy = on ? ly[s] : 0.f, cz = on ? lz[s] : 0.f;
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f, rr = 0.0f;
+        if (!cull) {
+          cx = on ? lx[s] : 0.f, cy = on ? ly[s] : 0.f, cz = on ? lz[s] : 0.f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          cx += __shfl_xor_sync(kFull, cx, o);
-          cy += __shfl_xor_sync(kFull, cy, o);
-          cz += __shfl_xor_sync(kFull, cz, o);
+          for (int o = 16; o > 0; o >>= 1) {
+            cx += __shfl_xor_sync(kFull, cx, o);
+            cy += __shfl_xor_sync(kFull, cy, o);
+            cz += __shfl_xor_sync(kFull, cz, o);
+          }
+          const float inv = on_mask ? 1.0f / static_cast<float>(__popc(on_mask)) : 0.0f;
+          cx *= inv;
+          cy *= inv;
+          cz *= inv;
+          rr = on ? sqrtf((lx[s] - cx) * (lx[s] - cx) + (ly[s] - cy) * (ly[s] - cy) + (lz[s] - cz) * (lz[s] - cz))
+                  : 0.0f;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) rr = fmaxf(rr, __shfl_xor_sync(kFull, rr, o));
         }
-        const float inv = on_mask ? 1.0f / static_cast<float>(__popc(on_mask)) : 0.0f;
-        cx *= inv;
-        cy *= inv;
-        cz *= inv;
-        float rr = on ? sqrtf((lx[s] - cx) * (lx[s] - cx) + (ly[s] - cy) * (ly[s] - cy) + (lz[s] - cz) * (lz[s] - cz))
-                      : 0.0f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) rr = fmaxf(rr, __shfl_xor_sync(kFull, rr, o));
         // axis-aligned bounding box of the same atoms (half-widths widened
         // like the radius so that FP32 rounding never shrinks it)
         float lo_x = on ? lx[s] : 3.0e38f, lo_y = on ? ly[s] : 3.0e38f, lo_z = on ? lz[s] : 3.0e38f;
@@ -469,7 +474,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           hi_z = fmaxf(hi_z, __shfl_xor_sync(kFull, hi_z, o));
         }
         if (lane == 0) {
-          s_blob[s] = make_float4(cx, cy, cz, on_mask ? rr * 1.0001f + 0.01f : -1.0e30f);
+          s_blob[s] = !on_mask ? make_float4(0.0f, 0.0f, 0.0f, -1.0e30f)
+                               : (cull ? s_ssph[s] : make_float4(cx, cy, cz, rr * 1.0001f + 0.01f));
           if (on_mask) {
             s_box[2 * s] = make_float4(0.5f * (lo_x + hi_x), 0.5f * (lo_y + hi_y), 0.5f * (lo_z + hi_z),
                                        0.5f * (hi_x - lo_x) * 1.0001f + 0.01f);

@@ -601,6 +601,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   std::vector<float4> rp32(cx->nr_pad, make_float4(1e9f, 1e9f, 1e9f, 0.f));
   std::vector<D4> rp64(cx->nr_pad, D4{1e30, 1e30, 1e30, 0.0});
   std::vector<int2> rmeta(cx->nr_pad, make_int2(0, 0));
+  std::vector<int4> rmeta16(cx->nr_pad, make_int4(0, 0, 0, 0));
   std::vector<double> rdes(static_cast<size_t>(std::max(rec->n, 1)) * 11, 0.0);
   double ext = 0.0;
   // receptor in compact segments (sums are order-free; the burial tables
@@ -612,6 +613,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
                           static_cast<float>(rec->z[i] - o[2]), static_cast<float>(332.0636 * rec->charge[i]));
     rp64[k] = D4{rec->x[i], rec->y[i], rec->z[i], rec->charge[i]};
     rmeta[k] = make_int2(rtype[i] * nt, rec->serial[i]);
+    rmeta16[k] = make_int4(rtype[i] * nt, rec->serial[i], 0, 0);
     desolv_row(rec->element[i], rec->vdw_radius[i], &rdes[static_cast<size_t>(k) * 11]);
     ext = std::max({ext, std::fabs(rec->x[i] - o[0]), std::fabs(rec->y[i] - o[1]), std::fabs(rec->z[i] - o[2])});
   }
@@ -696,6 +698,7 @@ gd_status gd_complex_create(gd_context *ctx, const gd_atoms *rec, const gd_atoms
   pack.add(rp32, &cx->rec_pos32);
   pack.add(rp64, &cx->rec_pos64);
   pack.add(rmeta, &cx->rec_meta);
+  pack.add(rmeta16, &cx->rec_meta16);
   pack.add(rdes, &cx->rec_desolv);
   pack.add(lx, &cx->lig_x);
   pack.add(ly, &cx->lig_y);

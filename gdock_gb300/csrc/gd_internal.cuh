@@ -77,6 +77,7 @@ struct ScoreParams {
   const float4 *rec_pos32;  // (x-O, y-O, z-O, 332.0636*q) FP32
   const D4 *rec_pos64; // (x, y, z, q) FP64
   const int2 *rec_meta;     // (type, serial)
+  const int4 *rec_meta16;   // (type, serial, 0, 0): the FP32 kernel's copy, as wide as a position
   const double *rec_desolv; // [nr * 11] energy contribution at burial count 0..10
   const float4 *rec_seg;    // per kRecSeg-atom segment: bounding sphere (centre - O, radius) FP32
   int nr, n_tiles, nseg;
@@ -153,6 +154,7 @@ struct gd_complex {
   float4 *rec_pos32 = nullptr;
   D4 *rec_pos64 = nullptr;
   int2 *rec_meta = nullptr;
+  int4 *rec_meta16 = nullptr;
   double *rec_desolv = nullptr;
   double *lig_x = nullptr, *lig_y = nullptr, *lig_z = nullptr, *lig_q = nullptr;
   int *lig_type = nullptr, *lig_serial = nullptr;

@@ -239,6 +239,7 @@ ScoreParams make_params(gd_complex *cx, const gd_pose_frame *d_frames, const dou
   p.rec_pos32 = cx->rec_pos32;
   p.rec_pos64 = cx->rec_pos64;
   p.rec_meta = cx->rec_meta;
+  p.rec_meta16 = cx->rec_meta16;
   p.rec_desolv = cx->rec_desolv;
   p.nr = cx->nr;
   p.n_tiles = cx->nr_pad / kTile;

@@ -93,8 +93,8 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   L.pos = o;
   o += sizeof(float4) * (kWS * kSeg + 1);  // + the far dummy atom
   al(16);
-  L.meta = o;
-  o += sizeof(int2) * (kWS * kSeg + 1);
+  L.meta = o;  // at a fixed distance from pos: one address serves both
+  o += sizeof(int4) * (kWS * kSeg + 1);
   al(16);
   L.list = o;
   o += sizeof(uint16_t) * kMaxS * kList;
@@ -137,13 +137,13 @@ __host__ __device__ inline WarpSmem warp_layout(int smem_cnt) {
   return L;
 }
 
-__device__ __forceinline__ void issue_seg(long long q, int seg, const ScoreParams &p, float4 *s_pos, int2 *s_meta,
+__device__ __forceinline__ void issue_seg(long long q, int seg, const ScoreParams &p, float4 *s_pos, int4 *s_meta,
                                           uint64_t *s_bar) {
   const int st = static_cast<int>(q % kWS);
-  constexpr uint32_t kBytes = kSeg * (sizeof(float4) + sizeof(int2));
+  constexpr uint32_t kBytes = kSeg * (sizeof(float4) + sizeof(int4));
   mbar_expect_tx(&s_bar[st], kBytes);
   bulk_g2s(&s_pos[st * kSeg], p.rec_pos32 + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(float4), &s_bar[st]);
-  bulk_g2s(&s_meta[st * kSeg], p.rec_meta + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(int2), &s_bar[st]);
+  bulk_g2s(&s_meta[st * kSeg], p.rec_meta16 + static_cast<size_t>(seg) * kSeg, kSeg * sizeof(int4), &s_bar[st]);
 }
 
 // acc += v when t < 0 (one predicated add)
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
   const WarpSmem L = warp_layout(bp.smem_cnt);
   unsigned char *base = smem + static_cast<size_t>(wib) * L.total;
   float4 *s_pos = reinterpret_cast<float4 *>(base + L.pos);
-  int2 *s_meta = reinterpret_cast<int2 *>(base + L.meta);
+  int4 *s_meta = reinterpret_cast<int4 *>(base + L.meta);
   uint16_t *s_list = reinterpret_cast<uint16_t *>(base + L.list);  // kept rows per slot, as stage indices
   uint16_t *s_fixq = reinterpret_cast<uint16_t *>(base + L.fixq);  // flagged steps: list position | slot << 8
   unsigned *s_cmask = reinterpret_cast<unsigned *>(base + L.cmask);  // near rows' burial ballots (this segment)
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     for (int s = 0; s < kWS; ++s) mbar_init(&s_bar[s], 1);
     fence_mbar_init();
     s_pos[kFar] = make_float4(1.0e9f, 1.0e9f, 1.0e9f, 0.0f);  // far from real and idle ligand lanes
-    s_meta[kFar] = make_int2(0, 0);
+    s_meta[kFar] = make_int4(0, 0, 0, 0);
   }
   if (!SPLIT)
     for (int i = lane; i < bp.max_nr; i += 32) cnt[i] = 0;
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
               ix[i] = lst[k0 + i];
               if (!GD_DCHECK(bp.err, ix[i] <= kFar, 4)) ix[i] = kFar;
               r[i] = s_pos[ix[i]];
-              const int2 mt = s_meta[ix[i]];
+              const int4 mt = s_meta[ix[i]];
               rt[i] = mt.x;
               if (!GD_DCHECK(bp.err, rt[i] >= 0 && rt[i] + lt[s] < p.nt * p.nt, 5)) rt[i] = 0;
               rs[i] = mt.y;
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
             if (ixi == kFar || !GD_DCHECK(bp.err, ixi < kFar, 4)) continue;
             const float4 ri = s_pos[ixi];
             if (!near_band(d2f(ri, fx, fy, fz), gv, ge, gdd)) continue;
-            const int2 mt = s_meta[ixi];
+            const int4 mt = s_meta[ixi];
             const FixOut fo = fix_pair<SERIAL, CLAMP>(p, X, Y, Z, ri, gbase + ixi - sbase, mt.x, mt.y, fx, fy, fz, fq,
                                                       ft, fs);
             av += fo.dv;

@@ -317,18 +317,22 @@ static std::vector<int> slot_order(const double *x, const double *y, const doubl
 // Receptor atoms grouped into spatially compact segments of kRecSeg (the FP32
 // kernel's ring stage): recursive bisection along the longest extent of the
 // bounding box, the left part always a whole number of segments, so every
-// segment but the last is full.  Deterministic (a stable sort per level).
-// Returns order[k] = original index of the atom at position k.
+// segment but the last is full; inside a segment the bisection goes on down
+// to compact runs of 8 (one row-test round).  Deterministic (a stable sort
+// per level).  Returns order[k] = original index of the atom at position k.
 static std::vector<int> segment_order(const double *x, const double *y, const double *z, int n) {
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
-  struct Span { int lo, hi; };
-  std::vector<Span> todo{{0, n}};
+  struct Span { int lo, hi, unit; };
+  std::vector<Span> todo{{0, n, kRecSeg}};
   while (!todo.empty()) {
     const Span sp = todo.back();
     todo.pop_back();
     const int m = sp.hi - sp.lo;
-    if (m <= kRecSeg) continue;
+    if (m <= sp.unit) {
+      if (sp.unit > 8 && m > 8) todo.push_back({sp.lo, sp.hi, 8});
+      continue;
+    }
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int k = sp.lo; k < sp.hi; ++k) {
       const double v[3] = {x[order[k]], y[order[k]], z[order[k]]};
@@ -339,10 +343,10 @@ static std::vector<int> segment_order(const double *x, const double *y, const do
       if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
     const double *c = ax == 0 ? x : (ax == 1 ? y : z);
     std::stable_sort(order.begin() + sp.lo, order.begin() + sp.hi, [c](int a, int b) { return c[a] < c[b]; });
-    const int nseg = (m + kRecSeg - 1) / kRecSeg;
-    const int mid = sp.lo + (nseg / 2) * kRecSeg;
-    todo.push_back({mid, sp.hi});
-    todo.push_back({sp.lo, mid});
+    const int nseg = (m + sp.unit - 1) / sp.unit;
+    const int mid = sp.lo + (nseg / 2) * sp.unit;
+    todo.push_back({mid, sp.hi, sp.unit});
+    todo.push_back({sp.lo, mid, sp.unit});
   }
   return order;
 }

@@ -38,8 +38,8 @@ N_REC_RES, N_LIG_RES, N_RESTRAINTS, N_POSES, SEED = 300, 150, 12, 65536, 2026
 FLOP_PER_PAIR = 37  # convention: d2 8, LJ 18, Coulomb 4, cutoff tests 5, burial 2
 # DRAM bytes per pose of the FP32 scoring kernel: dram__bytes_read.sum +
 # dram__bytes_write.sum of one ncu capture of the split-mode kernel on 4,096
-# poses of this workload, 43.12 MB + 9.77 MB (profiles/k_score_f32w_single_complex.md)
-TRAFFIC_PER_POSE = (43.124224e6 + 9.765632e6) / 4096
+# poses of this workload, 43.11 MB + 9.77 MB (profiles/k_score_f32w_single_complex.md)
+TRAFFIC_PER_POSE = (43.109888e6 + 9.772288e6) / 4096
 METRIC = "poses/s (batched FP32 scoring, single complex)"
 
 
@@ -520,8 +520,9 @@ def run_c5(args):
     lig = position_ligand(c.receptor, c.ligand)
     cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
     G = int(os.environ.get("GD_C5_GENERATIONS", "100"))
-    cfg = _lib.ga_default_cfg(pop_size=4096, max_generations=G, early_stopping=0, seed=9)
-    tuned = autotune_ga(gd, _lib, ctx, [cx], 4096, {"auto": 0, "never": 1, "always": 2}[args.split], generations=2)
+    POP = int(os.environ.get("GD_C5_POP", "4096"))  # smaller for profiling captures
+    cfg = _lib.ga_default_cfg(pop_size=POP, max_generations=G, early_stopping=0, seed=9)
+    tuned = autotune_ga(gd, _lib, ctx, [cx], POP, {"auto": 0, "never": 1, "always": 2}[args.split], generations=2)
     t0 = time.perf_counter()
     res = gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx)
     t_ga = time.perf_counter() - t0
@@ -534,7 +535,7 @@ def run_c5(args):
     general = gd.cluster_sets(cx.pose_contacts(res.genes[0]), ctx=ctx)
     t_general = time.perf_counter() - t0
     same = [(r.center_idx, r.members) for r in clusters] == [(r.center_idx, r.members) for r in general]
-    pairs = len(c.receptor) * len(lig) * 4096 * (G + 1)
+    pairs = len(c.receptor) * len(lig) * POP * (G + 1)
     # CPU leg: the oracle on 4 poses of the final population, all host threads
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
@@ -544,14 +545,14 @@ def run_c5(args):
     oracle.score_poses(c.receptor, lig, c.restraint_pairs, res.genes[0][:4], nthreads=threads)
     cpu_pps = 4 / (time.perf_counter() - t0)
     line = {"metric": "poses/s (large complex GA, pop 4096) and FCC clustering time over 4096 poses",
-            "value": 4096 * (G + 1) / t_ga, "unit": "poses/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "value": POP * (G + 1) / t_ga, "unit": "poses/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": t_ga * 1e3 / (G + 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "synthetic receptor 2000 residues x ligand 500 residues, 30 restraints, "
-                                   f"GA pop 4096 x {G} generations", "receptor_atoms": len(c.receptor),
+                                   f"GA pop {POP} x {G} generations", "receptor_atoms": len(c.receptor),
                        "ligand_atoms": len(lig)},
             "pair_evals_per_s": pairs / t_ga, "ga_seconds": t_ga,
-            "fcc": {"poses": 4096, "seconds": t_fcc, "fcc_pairs_per_s": 4096 * 4096 / t_fcc,
+            "fcc": {"poses": POP, "seconds": t_fcc, "fcc_pairs_per_s": POP * POP / t_fcc,
                     "clusters": len(clusters), "same_as_general_path": same,
                     "general_path_seconds": t_general},
             "autotune": tuned,

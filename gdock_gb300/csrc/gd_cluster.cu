@@ -45,6 +45,13 @@ struct ClusterTopo {
   float4 *d_r32 = nullptr;  // receptor heavy atoms (x-O, y-O, z-O, 0) FP32, grouped
   std::vector<int64_t> rr_keys;         // receptor-only inter-chain contacts (pose independent)
   double rr_cutoff = -1.0;
+  // ligand-only inter-chain contacts in the positioned frame: their count,
+  // and whether some residue pair's closest atom pair lies so near the cutoff
+  // that FP64 rounding of a pose's transform could flip it (then the count is
+  // not pose independent and the per-pose host path decides)
+  long long ll_count = 0;
+  bool ll_unstable = false;
+  double ll_cutoff = -1.0;
   // device
   double *d_rx = nullptr, *d_ry = nullptr, *d_rz = nullptr;
   double *d_lx = nullptr, *d_ly = nullptr, *d_lz = nullptr;
@@ -193,6 +200,7 @@ struct FccParams {
   double c, cs;  // fcc_cutoff and fcc_cutoff * strictness
   uint32_t *adj; // n rows of ceil(n/32) words; bit j of row i: edge i -> j
   int adj_words;
+  int c0;        // contacts every pose has (inter-chain ones within one molecule), not in the bitsets
 };
 
 constexpr int kFT = 64;   // pose tile
@@ -253,13 +261,13 @@ __global__ void __launch_bounds__(256) k_fcc(const FccParams p) {
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tx + 16 * b;
       if (j >= p.n) continue;
-      const int si = p.sizes[i], sj = p.sizes[j];
+      const int si = p.sizes[i] + p.c0, sj = p.sizes[j] + p.c0;
       // calculate_fcc (src/clustering.rs:122-132) and the first test of
       // create_elements (src/clustering.rs:171); the second test for the
       // pair (j, i) is the same condition, evaluated in that pair's thread.
       bool edge = false, back = false;
       if (si > 0 && sj > 0) {
-        const double common = static_cast<double>(cnt[a][b]);
+        const double common = static_cast<double>(cnt[a][b] + p.c0);
         const double fcc = common / static_cast<double>(si);
         const double fcc_v = common / static_cast<double>(sj);
         edge = fcc >= p.c && fcc_v >= p.cs;  // i -> j
@@ -692,14 +700,15 @@ __global__ void k_post_pairs(const int *offs, const int *kc, const int *post, in
 // common counts of the pairs i <= j (the diagonal: the pose's own size), as
 // k_fcc decides them.
 __global__ void k_post_decide(const uint32_t *common, const int *sizes, int n, double c, double cs, uint32_t *adj,
-                              int adj_words) {
+                              int adj_words, int c0) {
   for (int i = blockIdx.x; i < n; i += gridDim.x) {
-    const int si = sizes[i];
+    const int si = sizes[i] + c0;
     for (int j = i + threadIdx.x; j < n; j += blockDim.x) {
-      const int sj = sizes[j];
+      const int sj = sizes[j] + c0;
       bool edge = false, back = false;
       if (si > 0 && sj > 0) {
-        const double cm = static_cast<double>(i == j ? si : static_cast<int>(common[static_cast<size_t>(i) * n + j]));
+        const double cm =
+            static_cast<double>(i == j ? si : static_cast<int>(common[static_cast<size_t>(i) * n + j]) + c0);
         const double fcc = cm / static_cast<double>(si);
         const double fcc_v = cm / static_cast<double>(sj);
         edge = fcc >= c && fcc_v >= cs;
@@ -730,25 +739,39 @@ inline int64_t canon(int64_t ka, int64_t kb) {
   return ((ka >> 16) << 48) | ((ka & 0xffff) << 32) | ((kb >> 16) << 16) | (kb & 0xffff);
 }
 
-// inter-chain contacts among the residues of one molecule (host; used for
-// multi-chain receptors once and multi-chain ligands per pose)
+// Inter-chain contacts among the residues of one molecule at coordinates x,
+// y, z (host; multi-chain receptors once, multi-chain ligands per pose):
+// residue pairs on different chains with an atom pair at d2 <= t_le.  Pairs
+// whose enclosing spheres are beyond the cutoff are skipped.  When unstable is
+// given it is set if some residue pair's closest atom pair lies within a
+// relative 1e-6 of t_le: a decision that the FP64 rounding of a rigid
+// transform (some 1e-12 A^2 on d2) could not flip lies far outside that.
 void intra_contacts(const std::vector<int64_t> &gkey, const std::vector<int> &goff, const std::vector<int> &atoms,
-                    const double *x, const double *y, const double *z, double t_le, std::vector<int64_t> &out) {
+                    const double *x, const double *y, const double *z, double t_le, std::vector<int64_t> &out,
+                    bool *unstable = nullptr) {
   const int G = static_cast<int>(gkey.size());
+  std::vector<double> c(3 * static_cast<size_t>(G)), r(G);
+  for (int g = 0; g < G; ++g)
+    enclosing_ball(x, y, z, atoms.data() + goff[g], goff[g + 1] - goff[g], &c[3 * static_cast<size_t>(g)], r[g]);
+  // a skipped pair's closest atoms lie beyond the cutoff by more than the band
+  const double band = 1e-6 * t_le, reach = std::sqrt(t_le) + 1e-4;
   for (int g = 0; g < G; ++g)
     for (int h = g + 1; h < G; ++h) {
       if ((gkey[g] >> 16) == (gkey[h] >> 16)) continue;
-      bool found = false;
-      for (int a = goff[g]; a < goff[g + 1] && !found; ++a)
+      const double *cg = &c[3 * static_cast<size_t>(g)], *ch = &c[3 * static_cast<size_t>(h)];
+      const double ex = cg[0] - ch[0], ey = cg[1] - ch[1], ez = cg[2] - ch[2];
+      const double lim = r[g] + r[h] + reach;
+      if (ex * ex + ey * ey + ez * ez > lim * lim * (1.0 + 1e-9)) continue;
+      double best = INFINITY;
+      for (int a = goff[g]; a < goff[g + 1] && !(best < t_le - band); ++a)
         for (int b = goff[h]; b < goff[h + 1]; ++b) {
           const int ia = atoms[a], ib = atoms[b];
           const double dx = x[ia] - x[ib], dy = y[ia] - y[ib], dz = z[ia] - z[ib];
-          if (dx * dx + dy * dy + dz * dz <= t_le) {
-            found = true;
-            break;
-          }
+          best = std::min(best, dx * dx + dy * dy + dz * dz);
+          if (best < t_le - band) break;
         }
-      if (found) out.push_back(canon(gkey[g], gkey[h]));
+      if (best <= t_le) out.push_back(canon(gkey[g], gkey[h]));
+      if (unstable && std::fabs(best - t_le) <= band) *unstable = true;
     }
 }
 
@@ -966,7 +989,7 @@ void free_cluster_cache(gd_complex *cx) {
   cx->cluster_cache = nullptr;
 }
 
-bool bits_path_ok(const ClusterTopo *t, int n);
+bool bits_path_ok(const ClusterTopo *t, int n, bool multi_chain = false);
 long long bits_words(const ClusterTopo *t);
 gd_status launch_contact_bits(gd_complex *cx, ClusterTopo *t, const gd_pose_frame *d_frames, int n, double cutoff,
                               double maxd, uint32_t *d_bits, long long words, cudaStream_t st);
@@ -1219,11 +1242,13 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
 // ligand that share no residue: contact bitmaps, union, compaction, FCC; the
 // greedy pass runs on the host.  Returns GD_ERR_STATE when the topology or the
 // bitmap size calls for the general path.
-// The contact-bitmap path (k_contact_bits) serves single-chain receptors and
-// ligands that share no residue, with every ligand residue staged whole, at
-// most 8 GiB of bitmaps and bit indices that fit 32 bits.
-bool bits_path_ok(const ClusterTopo *t, int n) {
-  if (t->multi_chain_rec || t->multi_chain_lig || t->mixed) return false;
+// The contact-bitmap path (k_contact_bits) serves receptors and ligands that
+// share no residue, with every ligand residue staged whole, at most 8 GiB of
+// bitmaps and bit indices that fit 32 bits; single-chain ones only unless
+// multi_chain (clustering adds the inter-chain contacts within each molecule
+// as a constant; per-pose contact lists take the host path for them).
+bool bits_path_ok(const ClusterTopo *t, int n, bool multi_chain) {
+  if (t->mixed || (!multi_chain && (t->multi_chain_rec || t->multi_chain_lig))) return false;
   for (int g = 0; g < t->GL; ++g)
     if (t->lg_off[g + 1] - t->lg_off[g] > kMaxGroupAtoms) return false;  // residues staged whole
   const long long pairs = static_cast<long long>(t->GR) * t->GL;
@@ -1311,7 +1336,36 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
   ClusterTopo *t = nullptr;
   gd_status s = get_topo(cx, &t);
   if (s != GD_OK) return s;
-  if (!bits_path_ok(t, n)) return GD_ERR_STATE;
+  if (!bits_path_ok(t, n, true)) return GD_ERR_STATE;
+  // contacts within one molecule across its chains are the same in every
+  // pose (the receptor does not move; the ligand moves rigidly and its
+  // decisions are checked to be far from the cutoff): a constant c0 in every
+  // set size and pair count, outside the bitmaps
+  const Thresholds thr = make_thresholds(cfg.contact_distance);
+  long long c0 = 0;
+  if (t->multi_chain_rec) {
+    if (t->rr_cutoff != cfg.contact_distance) {
+      t->rr_keys.clear();
+      intra_contacts(t->rg_key, t->rg_off, t->r_atoms, cx->h_rx.data(), cx->h_ry.data(), cx->h_rz.data(),
+                     thr.contact_le, t->rr_keys);
+      t->rr_cutoff = cfg.contact_distance;
+    }
+    c0 += static_cast<long long>(t->rr_keys.size());
+  }
+  if (t->multi_chain_lig) {
+    if (t->ll_cutoff != cfg.contact_distance) {
+      std::vector<int64_t> ll;
+      bool unstable = false;
+      intra_contacts(t->lg_key, t->lg_off, t->l_atoms, cx->h_lx.data(), cx->h_ly.data(), cx->h_lz.data(),
+                     thr.contact_le, ll, &unstable);
+      t->ll_count = static_cast<long long>(ll.size());
+      t->ll_unstable = unstable;
+      t->ll_cutoff = cfg.contact_distance;
+    }
+    if (t->ll_unstable) return GD_ERR_STATE;
+    c0 += t->ll_count;
+  }
+  if (c0 > (1 << 30)) return GD_ERR_STATE;
   const long long words = bits_words(t);
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t bits_b = sizeof(uint32_t) * words * static_cast<size_t>(n);
@@ -1441,8 +1495,8 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
       k_post_fill<<<std::max(g3, 1), 256, 0, st>>>(d_bits, d_u, d_base, n, words, d_offs, d_cur, d_list);
       k_post_pairs<<<std::max(1, std::min((U + 7) / 8, ctx->sm_count * 16)), 256, 0, st>>>(d_offs, d_kc, d_list, U, n,
                                                                                           d_common);
-      k_post_decide<<<std::min(n, ctx->sm_count * 16), 256, 0, st>>>(d_common, d_sizes, n, cfg.fcc_cutoff,
-                                                                     cfg.fcc_cutoff * cfg.strictness, d_adj, aw);
+      k_post_decide<<<std::min(n, ctx->sm_count * 16), 256, 0, st>>>(
+          d_common, d_sizes, n, cfg.fcc_cutoff, cfg.fcc_cutoff * cfg.strictness, d_adj, aw, static_cast<int>(c0));
       e = cudaGetLastError();
     }
   } else if (e == cudaSuccess) {
@@ -1457,6 +1511,7 @@ gd_status cluster_device(gd_complex *cx, const double *genes, int n, const gd_cl
     fp.cs = cfg.fcc_cutoff * cfg.strictness;
     fp.adj = d_adj;
     fp.adj_words = aw;
+    fp.c0 = static_cast<int>(c0);
     dim3 grid((n + kFT - 1) / kFT, (n + kFT - 1) / kFT);
     k_fcc<<<grid, 256, 0, st>>>(fp);
     e = cudaGetLastError();

@@ -125,3 +125,34 @@ def test_cluster_device_fcc_paths(oracle, setup, mode):
             got = cx.cluster(genes, cfg)
             want = oracle.cluster(sets, fcc_cutoff=cut, strictness=strict, min_size=1)
             assert [(r.center_idx, r.members) for r in got] == want, (spread, cut, strict)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_multichain_cluster_on_device(oracle, mode):
+    """Receptor and ligand of two chains each: the device clusters them (the
+    contact bitmaps for receptor-ligand pairs, the inter-chain contacts within
+    each molecule as a count every pose shares) and gives the oracle's
+    clusters of the oracle's contact sets, with both ways of counting common
+    contacts (GD_TUNE_FCC)."""
+    from gdock_gb300 import _lib
+    c = synth.make_complex(40, 30, 3, seed=8)
+    rec, lig0 = c.receptor, c.ligand
+    rec = gd.Molecule(**{**rec.__dict__, "chainid": ["A" if i < len(rec) // 2 else "C" for i in range(len(rec))]})
+    lig0 = gd.Molecule(**{**lig0.__dict__, "chainid": ["B" if i < len(lig0) // 2 else "D" for i in range(len(lig0))]})
+    lig = gd.position_ligand(rec, lig0)
+    ctx = gd.Context(0)
+    try:
+        ctx.set_tuning(_lib.GD_TUNE_FCC, mode)
+        cx = gd.Complex(rec, lig, c.restraint_pairs, ctx=ctx)
+        rng = np.random.default_rng(70 + mode)
+        for spread in (0.3, 1.0, 4.0):
+            genes = near_genes(rng, 60, spread)
+            sets = [oracle.pose_contacts(rec, lig, g) for g in genes]
+            for ms in (1, 4):
+                got = cx.cluster(genes, gd.ClusteringConfig(min_cluster_size=ms))
+                assert ctx.get_tuning(_lib.GD_INFO_LAST_CONTACTS) == 2  # the bitmap kernel ran
+                assert ctx.get_tuning(_lib.GD_INFO_LAST_FCC) == mode
+                assert [(r.center_idx, r.members) for r in got] == oracle.cluster(sets, min_size=ms), (spread, ms)
+        cx.close()
+    finally:
+        ctx.close()

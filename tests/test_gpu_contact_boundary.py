@@ -123,16 +123,16 @@ def test_boundary_away_from_the_origin(oracle):
 
 @pytest.mark.parametrize("fcc_mode", [1, 2])
 def test_cluster_on_boundary_contacts(oracle, fcc_mode):
-    """gd_cluster on the boundary geometry (contact bitmaps, then both FCC
-    pair counts) and on its multi-chain variant (contact lists, then the FCC
-    of the keys): the oracle's clusters of the oracle's contact sets."""
+    """gd_cluster on the boundary geometry and on its variant with a
+    two-chain receptor (contact bitmaps both, then both FCC pair counts): the
+    oracle's clusters of the oracle's contact sets."""
     rec1 = make_mol([tatom(0.0, 0.0, 0.0, "C", name="CA", resseq=1, serial=1, chain="A")])
     rec2 = make_mol([tatom(0.0, 0.0, 0.0, "C", name="CA", resseq=1, serial=1, chain="A"),
                      tatom(0.0, 0.0, 60.0, "C", name="CA", resseq=2, serial=2, chain="C")])
     lig, _ = boundary_ligand()
     genes = np.zeros((9, 6))
     genes[6:, 3] = (100.0, 200.0, 300.0)  # empty contact sets
-    for rec, kernel in ((rec1, 2), (rec2, 1)):
+    for rec, kernel in ((rec1, 2), (rec2, 2)):
         ctx = gd.Context(0)
         try:
             ctx.set_tuning(_lib.GD_TUNE_FCC, fcc_mode)
@@ -163,3 +163,36 @@ def test_hydrogens_make_no_contacts(oracle):
     want = contacts_all_paths(oracle, rec, lig, genes, [(0, 2), (1, 1)])
     for keys in want:
         assert keys.tolist() == [oracle.contact_key("A", 1, "B", 2)]
+
+
+def two_chain_ligand(half):
+    """Two ligand atoms on chains B and D at (0, 0, +-half): mirrored, so the
+    centroid is exactly 0 and the identity pose keeps their distance 2 * half."""
+    return make_mol([tatom(0.0, 0.0, half, "C", name="CB", resseq=1, serial=101, chain="B"),
+                     tatom(0.0, 0.0, -half, "C", name="CB", resseq=1, serial=102, chain="D")])
+
+
+def test_cluster_ligand_chains_constant_or_per_pose(oracle):
+    """A two-chain ligand's own inter-chain contact is in every pose's set.
+    Far from the cutoff (4 A) it is a constant and the device path clusters;
+    at exactly 5 A the FP64 rounding of a pose's transform can put it on
+    either side, so the per-pose host path decides it (contact lists).  Both
+    give the oracle's clusters."""
+    rng = np.random.default_rng(5)
+    genes = np.zeros((12, 6))
+    genes[:, :3] = rng.uniform(0.0, 2 * np.pi, (12, 3))
+    genes[1:, 3:] = rng.normal(0.0, 0.4, (11, 3))
+    rec = make_mol([tatom(0.0, 0.0, 6.5, "C", name="CA", resseq=1, serial=1, chain="A"),
+                    tatom(0.0, 0.0, -6.5, "N", name="N", resseq=2, serial=2, chain="A")])
+    for half, kernel in ((2.0, 2), (2.5, 1)):
+        lig = two_chain_ligand(half)
+        ctx = gd.Context(0)
+        try:
+            cx = gd.Complex(rec, lig, [], ctx=ctx)
+            sets = [oracle.pose_contacts(rec, lig, g) for g in genes]
+            got = cx.cluster(genes, gd.ClusteringConfig(min_cluster_size=1))
+            assert ctx.get_tuning(_lib.GD_INFO_LAST_CONTACTS) == kernel, half
+            assert [(r.center_idx, r.members) for r in got] == oracle.cluster(sets, min_size=1), half
+            cx.close()
+        finally:
+            ctx.close()

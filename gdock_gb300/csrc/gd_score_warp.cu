@@ -1145,5 +1145,3 @@ extern "C" gd_status gd_score_frames_device_noalloc(gd_complex *cx, const gd_pos
   return launch_args(ctx, 1, pl, L, arg, cx->serial_overlap, cx->need_clamp, st);
 }
 
-namespace gd {
-}  // namespace gd

@@ -135,7 +135,7 @@ class Complex:
         g = np.ascontiguousarray(genes, dtype=np.float64).reshape(-1, 6)
         n = g.shape[0]
         offs = np.zeros(n + 1, dtype=np.int64)
-        cap = 1 << 16
+        cap = max(1 << 16, 1024 * n)  # a second call only when poses average over 1,024 contacts
         for _ in range(2):
             keys = np.zeros(cap, dtype=np.int64)
             st = self.lib.gd_pose_contacts(self.h, ptr(g), n, ptr(keys), cap, ptr(offs))

@@ -27,7 +27,9 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <functional>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "gd_internal.cuh"
@@ -1153,30 +1155,49 @@ gd_status pose_contacts_host(gd_complex *cx, const double *genes, int n, double 
     break;
   }
   PhaseTimer pt_keys("contacts: host keys");
-  keys.clear();
-  offs.assign(1, 0);
-  std::vector<int64_t> pk;
-  std::vector<double> tx, ty, tz;
-  for (int i = 0; i < n; ++i) {
-    pk.clear();
-    for (long long k = loffs[i]; k < loffs[i + 1]; ++k) {
-      const uint32_t v = flat[k];
-      pk.push_back(canon(t->rg_key[v / t->GL], t->lg_key[v % t->GL]));
+  // each pose's keys on up to 16 threads (contiguous pose ranges), then
+  // concatenated in pose order
+  const int nth = n >= 256 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) : 1;
+  std::vector<std::vector<int64_t>> part(nth);
+  std::vector<int64_t> cnt(n, 0);
+  auto work = [&](int q) {
+    const int i0 = static_cast<int>(static_cast<long long>(n) * q / nth),
+              i1 = static_cast<int>(static_cast<long long>(n) * (q + 1) / nth);
+    std::vector<int64_t> pk;
+    std::vector<double> tx, ty, tz;
+    for (int i = i0; i < i1; ++i) {
+      pk.clear();
+      for (long long k = loffs[i]; k < loffs[i + 1]; ++k) {
+        const uint32_t v = flat[k];
+        pk.push_back(canon(t->rg_key[v / t->GL], t->lg_key[v % t->GL]));
+      }
+      pk.insert(pk.end(), t->rr_keys.begin(), t->rr_keys.end());
+      if (t->multi_chain_lig) {
+        tx.resize(cx->nl);
+        ty.resize(cx->nl);
+        tz.resize(cx->nl);
+        for (int a : t->l_atoms)
+          xform_host(frames[i], cx->cx, cx->cy, cx->cz, cx->h_lx[a], cx->h_ly[a], cx->h_lz[a], tx[a], ty[a], tz[a]);
+        intra_contacts(t->lg_key, t->lg_off, t->l_atoms, tx.data(), ty.data(), tz.data(), thr.contact_le, pk);
+      }
+      std::sort(pk.begin(), pk.end());
+      pk.erase(std::unique(pk.begin(), pk.end()), pk.end());
+      part[q].insert(part[q].end(), pk.begin(), pk.end());
+      cnt[i] = static_cast<int64_t>(pk.size());
     }
-    pk.insert(pk.end(), t->rr_keys.begin(), t->rr_keys.end());
-    if (t->multi_chain_lig) {
-      tx.resize(cx->nl);
-      ty.resize(cx->nl);
-      tz.resize(cx->nl);
-      for (int a : t->l_atoms)
-        xform_host(frames[i], cx->cx, cx->cy, cx->cz, cx->h_lx[a], cx->h_ly[a], cx->h_lz[a], tx[a], ty[a], tz[a]);
-      intra_contacts(t->lg_key, t->lg_off, t->l_atoms, tx.data(), ty.data(), tz.data(), thr.contact_le, pk);
-    }
-    std::sort(pk.begin(), pk.end());
-    pk.erase(std::unique(pk.begin(), pk.end()), pk.end());
-    keys.insert(keys.end(), pk.begin(), pk.end());
-    offs.push_back(static_cast<int64_t>(keys.size()));
+  };
+  if (nth == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int q = 0; q < nth; ++q) th.emplace_back(work, q);
+    for (auto &x : th) x.join();
   }
+  offs.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) offs[i + 1] = offs[i] + cnt[i];
+  keys.clear();
+  keys.reserve(static_cast<size_t>(offs[n]));
+  for (const auto &v : part) keys.insert(keys.end(), v.begin(), v.end());
   return GD_OK;
 }
 
@@ -1185,54 +1206,156 @@ gd_status cluster_sets(gd_context *ctx, const int64_t *keys, const int64_t *offs
   *n_clusters = 0;
   if (n <= 0) return GD_OK;
   PhaseTimer pt_all("fcc: total");
-  // compacted contact universe
-  std::vector<int64_t> uni(keys, keys + offs[n]);
-  std::sort(uni.begin(), uni.end());
-  uni.erase(std::unique(uni.begin(), uni.end()), uni.end());
-  const int W = std::max(1, static_cast<int>((uni.size() + 63) / 64));
-  std::vector<unsigned long long> bits(static_cast<size_t>(n) * W, 0ull);
-  std::vector<int> sz(n);
-  for (int i = 0; i < n; ++i) {
-    sz[i] = static_cast<int>(offs[i + 1] - offs[i]);
-    for (int64_t k = offs[i]; k < offs[i + 1]; ++k) {
-      const size_t u = std::lower_bound(uni.begin(), uni.end(), keys[k]) - uni.begin();
-      bits[static_cast<size_t>(i) * W + u / 64] |= 1ull << (u % 64);
-    }
+  // compacted contact universe, each pose's contacts as universe indices
+  // (distinct, ascending) and the number of poses per contact; the host work
+  // runs on up to 16 threads (poses split in contiguous ranges)
+  const size_t nk = static_cast<size_t>(offs[n]);
+  const int nth = nk >= (1u << 16) ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) : 1;
+  auto parallel = [nth](int count, const std::function<void(int, int, int)> &f) {
+    if (nth == 1) return f(0, 0, count);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t)
+      th.emplace_back(f, t, static_cast<int>(static_cast<long long>(count) * t / nth),
+                      static_cast<int>(static_cast<long long>(count) * (t + 1) / nth));
+    for (auto &x : th) x.join();
+  };
+  std::vector<int64_t> uni(keys, keys + nk);
+  {
+    // sorted runs per thread, then pairwise merges
+    std::vector<size_t> cut(nth + 1);
+    for (int t = 0; t <= nth; ++t) cut[t] = nk * t / nth;
+    parallel(nth, [&](int, int t0, int t1) {
+      for (int t = t0; t < t1; ++t) std::sort(uni.begin() + cut[t], uni.begin() + cut[t + 1]);
+    });
+    for (int w = 1; w < nth; w *= 2)
+      for (int t = 0; t + w < nth; t += 2 * w)
+        std::inplace_merge(uni.begin() + cut[t], uni.begin() + cut[t + w], uni.begin() + cut[std::min(nth, t + 2 * w)]);
+    uni.erase(std::unique(uni.begin(), uni.end()), uni.end());
   }
+  const int U = static_cast<int>(uni.size());
+  std::vector<int> ui(nk);
+  std::vector<int64_t> uoff(n + 1, 0);
+  std::vector<int> sz(n), kc(std::max(U, 1), 0);
+  parallel(n, [&](int, int i0, int i1) {
+    for (int i = i0; i < i1; ++i) {
+      const size_t o = static_cast<size_t>(offs[i]);
+      size_t m = o;
+      for (int64_t k = offs[i]; k < offs[i + 1]; ++k)
+        ui[m++] = static_cast<int>(std::lower_bound(uni.begin(), uni.end(), keys[k]) - uni.begin());
+      if (!std::is_sorted(ui.begin() + o, ui.begin() + m)) std::sort(ui.begin() + o, ui.begin() + m);
+      sz[i] = static_cast<int>(std::unique(ui.begin() + o, ui.begin() + m) - (ui.begin() + o));
+    }
+  });
+  // each pose's distinct indices packed to the front of its range
+  for (int i = 0; i < n; ++i) {
+    const size_t o = static_cast<size_t>(offs[i]), d = static_cast<size_t>(uoff[i]);
+    if (d != o) std::copy(ui.begin() + o, ui.begin() + o + sz[i], ui.begin() + d);
+    for (int k = 0; k < sz[i]; ++k) ++kc[ui[d + k]];
+    uoff[i + 1] = uoff[i] + sz[i];
+  }
+  const int W = std::max(1, (U + 63) / 64);
   const int aw = (n + 31) / 32;
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-  const size_t bb = sizeof(unsigned long long) * bits.size(), sb = sizeof(int) * n,
-               ab = sizeof(uint32_t) * static_cast<size_t>(n) * aw;
-  gd_status s = ensure_scratch(ctx, al(bb) + al(sb) + al(ab), 0);
-  if (s != GD_OK) return s;
-  char *base = static_cast<char *>(ctx->d_scratch);
-  unsigned long long *d_bits = reinterpret_cast<unsigned long long *>(base);
-  int *d_sz = reinterpret_cast<int *>(base + al(bb));
-  uint32_t *d_adj = reinterpret_cast<uint32_t *>(base + al(bb) + al(sb));
-  trace("fcc: universe + bitsets (host)",
-        std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
-  const auto t_k = std::chrono::steady_clock::now();
-  cudaError_t e = cudaMemcpyAsync(d_bits, bits.data(), bb, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_sz, sz.data(), sb, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_adj, 0, ab, ctx->stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC setup");
-  FccParams p{};
-  p.bits = d_bits;
-  p.sizes = d_sz;
-  p.n = n;
-  p.W = W;
-  p.c = cfg.fcc_cutoff;
-  p.cs = cfg.fcc_cutoff * cfg.strictness;
-  p.adj = d_adj;
-  p.adj_words = aw;
-  dim3 grid((n + kFT - 1) / kFT, (n + kFT - 1) / kFT);
-  k_fcc<<<grid, 256, 0, ctx->stream>>>(p);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel launch");
+  // pair counts: bitsets, or the poses of each contact (postings) when the
+  // contacts are spread thin (GD_TUNE_FCC; the same cost model as the device
+  // clustering path)
+  double work = 0.0;
+  for (int u = 0; u < U; ++u) work += 0.5 * static_cast<double>(kc[u]) * (kc[u] - 1);
+  const double bits_work = 0.5 * static_cast<double>(n) * (n + 1) * W;
+  bool postings = n <= 16384 && (ctx->tune_fcc == 2 || (ctx->tune_fcc == 0 && bits_work > 2e10 && 80.0 * work < bits_work));
+  const size_t sb = sizeof(int) * n, ab = sizeof(uint32_t) * static_cast<size_t>(n) * aw;
   std::vector<uint32_t> adj(static_cast<size_t>(n) * aw);
-  e = cudaMemcpyAsync(adj.data(), d_adj, ab, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel");
-  trace("fcc: kernel + transfers", std::chrono::duration<double>(std::chrono::steady_clock::now() - t_k).count());
+  cudaStream_t st = ctx->stream;
+  if (postings) {
+    const size_t memb = static_cast<size_t>(uoff[n]);
+    std::vector<int> poff(U + 1, 0), list(std::max<size_t>(memb, 1));
+    for (int u = 0; u < U; ++u) poff[u + 1] = poff[u] + kc[u];
+    std::vector<int> cur(poff.begin(), poff.end() - 1);
+    for (int i = 0; i < n; ++i)
+      for (int64_t k = uoff[i]; k < uoff[i + 1]; ++k) list[cur[ui[k]]++] = i;
+    const size_t ob = sizeof(int) * (U + 1), kb = sizeof(int) * std::max(U, 1), lb = sizeof(int) * list.size(),
+                 cb = sizeof(uint32_t) * static_cast<size_t>(n) * n;
+    const size_t total = al(ob) + al(kb) + al(lb) + al(cb) + al(sb) + al(ab);
+    void *buf = nullptr;
+    gd_status s = dev_alloc(ctx, total, &buf);
+    if (s != GD_OK && ctx->tune_fcc != 2) {
+      postings = false;  // no room for the n x n counts: the bitsets
+      ctx->last_error.clear();
+    } else if (s != GD_OK) {
+      return s;
+    }
+    if (postings) {
+      trace("fcc: universe + postings (host)",
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+      const auto t_k = std::chrono::steady_clock::now();
+      char *b = static_cast<char *>(buf);
+      int *d_off = reinterpret_cast<int *>(b);
+      int *d_kc = reinterpret_cast<int *>(b + al(ob));
+      int *d_list = reinterpret_cast<int *>(b + al(ob) + al(kb));
+      uint32_t *d_common = reinterpret_cast<uint32_t *>(b + al(ob) + al(kb) + al(lb));
+      int *d_sz = reinterpret_cast<int *>(b + al(ob) + al(kb) + al(lb) + al(cb));
+      uint32_t *d_adj = reinterpret_cast<uint32_t *>(b + al(ob) + al(kb) + al(lb) + al(cb) + al(sb));
+      cudaError_t e = cudaMemcpyAsync(d_off, poff.data(), ob, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_kc, kc.data(), kb, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_list, list.data(), lb, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_sz, sz.data(), sb, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(d_common, 0, cb, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(d_adj, 0, ab, st);
+      if (e == cudaSuccess && U > 0)
+        k_post_pairs<<<std::max(1, std::min((U + 7) / 8, ctx->sm_count * 16)), 256, 0, st>>>(d_off, d_kc, d_list, U, n,
+                                                                                            d_common);
+      if (e == cudaSuccess) {
+        k_post_decide<<<std::min(n, ctx->sm_count * 16), 256, 0, st>>>(d_common, d_sz, n, cfg.fcc_cutoff,
+                                                                       cfg.fcc_cutoff * cfg.strictness, d_adj, aw, 0);
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) e = cudaMemcpyAsync(adj.data(), d_adj, ab, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      dev_free(ctx, buf, total);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC postings");
+      ctx->last_fcc = 2;
+      trace("fcc: kernels + transfers", std::chrono::duration<double>(std::chrono::steady_clock::now() - t_k).count());
+    }
+  }
+  if (!postings) {
+    std::vector<unsigned long long> bits(static_cast<size_t>(n) * W, 0ull);
+    parallel(n, [&](int, int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (int64_t k = uoff[i]; k < uoff[i + 1]; ++k)
+          bits[static_cast<size_t>(i) * W + ui[k] / 64] |= 1ull << (ui[k] % 64);
+    });
+    const size_t bb = sizeof(unsigned long long) * bits.size();
+    gd_status s = ensure_scratch(ctx, al(bb) + al(sb) + al(ab), 0);
+    if (s != GD_OK) return s;
+    char *base = static_cast<char *>(ctx->d_scratch);
+    unsigned long long *d_bits = reinterpret_cast<unsigned long long *>(base);
+    int *d_sz = reinterpret_cast<int *>(base + al(bb));
+    uint32_t *d_adj = reinterpret_cast<uint32_t *>(base + al(bb) + al(sb));
+    trace("fcc: universe + bitsets (host)",
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - pt_all.t0).count());
+    const auto t_k = std::chrono::steady_clock::now();
+    cudaError_t e = cudaMemcpyAsync(d_bits, bits.data(), bb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_sz, sz.data(), sb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_adj, 0, ab, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC setup");
+    FccParams p{};
+    p.bits = d_bits;
+    p.sizes = d_sz;
+    p.n = n;
+    p.W = W;
+    p.c = cfg.fcc_cutoff;
+    p.cs = cfg.fcc_cutoff * cfg.strictness;
+    p.adj = d_adj;
+    p.adj_words = aw;
+    dim3 grid((n + kFT - 1) / kFT, (n + kFT - 1) / kFT);
+    k_fcc<<<grid, 256, 0, st>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel launch");
+    e = cudaMemcpyAsync(adj.data(), d_adj, ab, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "FCC kernel");
+    ctx->last_fcc = 1;
+    trace("fcc: kernel + transfers", std::chrono::duration<double>(std::chrono::steady_clock::now() - t_k).count());
+  }
   PhaseTimer pt_g("fcc: greedy clustering (host)");
   *n_clusters = greedy_clusters(adj, n, aw, cfg.min_cluster_size, centers, sizes, members);
   return GD_OK;

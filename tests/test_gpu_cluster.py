@@ -156,3 +156,59 @@ def test_multichain_cluster_on_device(oracle, mode):
         cx.close()
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_cluster_sets_both_pair_counts(oracle, mode):
+    """gd_cluster_sets counts common contacts with bitsets or with postings
+    built on the host (GD_TUNE_FCC): the oracle's clusters either way, for
+    dense groups, spread-out sets and empty ones."""
+    from gdock_gb300 import _lib
+    ctx = gd.Context(0)
+    try:
+        ctx.set_tuning(_lib.GD_TUNE_FCC, mode)
+        rng = np.random.default_rng(90 + mode)
+        protos = [np.unique(rng.integers(0, 5000, 80)) for _ in range(4)]
+        sets = []
+        for k in range(260):
+            if k % 13 == 0:
+                sets.append(np.zeros(0, np.int64))
+            elif k < 200:
+                base = protos[k % 4]
+                sets.append(np.unique(np.concatenate([base[rng.random(base.size) > 0.15],
+                                                      rng.integers(0, 5000, 4)])).astype(np.int64))
+            else:
+                sets.append(np.unique(rng.integers(0, 200000, int(rng.integers(1, 60)))).astype(np.int64))
+        for ms in (1, 4):
+            got = gd.cluster_sets(sets, gd.ClusteringConfig(min_cluster_size=ms), ctx=ctx)
+            assert ctx.get_tuning(_lib.GD_INFO_LAST_FCC) == mode
+            assert [(r.center_idx, r.members) for r in got] == oracle.cluster(sets, min_size=ms), ms
+        cfg = gd.ClusteringConfig(fcc_cutoff=0.3, strictness=0.5, min_cluster_size=1)
+        got = gd.cluster_sets(sets, cfg, ctx=ctx)
+        assert [(r.center_idx, r.members) for r in got] == oracle.cluster(sets, fcc_cutoff=0.3, strictness=0.5,
+                                                                          min_size=1)
+        # over 65,536 keys: the host side runs on several threads
+        big = [np.unique(np.concatenate([protos[k % 4][rng.random(protos[k % 4].size) > 0.2],
+                                         rng.integers(0, 50000, 8)])).astype(np.int64) for k in range(1100)]
+        assert sum(len(b) for b in big) > 65536
+        got = gd.cluster_sets(big, gd.ClusteringConfig(min_cluster_size=4), ctx=ctx)
+        assert [(r.center_idx, r.members) for r in got] == oracle.cluster(big, min_size=4)
+    finally:
+        ctx.close()
+
+
+def test_multichain_pose_contacts_many_poses(oracle):
+    """Per-pose contact keys of a two-chain receptor and a two-chain ligand
+    over 300 poses (the host builds the keys on several threads from 256
+    poses up): each pose's keys are the oracle's."""
+    c = synth.make_complex(40, 30, 3, seed=12)
+    rec, lig0 = c.receptor, c.ligand
+    rec = gd.Molecule(**{**rec.__dict__, "chainid": ["A" if i < len(rec) // 2 else "C" for i in range(len(rec))]})
+    lig0 = gd.Molecule(**{**lig0.__dict__, "chainid": ["B" if i < len(lig0) // 2 else "D" for i in range(len(lig0))]})
+    lig = gd.position_ligand(rec, lig0)
+    genes = near_genes(np.random.default_rng(13), 300, 2.0)
+    cx = gd.Complex(rec, lig, c.restraint_pairs)
+    got = cx.pose_contacts(genes)
+    assert len(got) == 300
+    for g, keys in zip(genes, got):
+        np.testing.assert_array_equal(keys, oracle.pose_contacts(rec, lig, g))

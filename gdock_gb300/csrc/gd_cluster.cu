@@ -777,21 +777,38 @@ void intra_contacts(const std::vector<int64_t> &gkey, const std::vector<int> &go
     }
 }
 
-template <typename T>
-gd_status topo_upload(gd_context *ctx, ClusterTopo *t, const std::vector<T> &h, T **d) {
-  void *p = nullptr;
-  const size_t bytes = sizeof(T) * std::max<size_t>(h.size(), 1);
-  gd_status s = dev_alloc(ctx, bytes, &p);
-  if (s != GD_OK) return s;
-  t->allocs.push_back(p);
-  t->bytes += bytes;
-  *d = static_cast<T *>(p);
-  if (!h.empty()) {
-    cudaError_t e = cudaMemcpy(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy (contact topology)");
+// The topology's device arrays, staged on the host and copied in one piece
+// (each 256-byte aligned): one cudaMalloc and one cudaMemcpy per complex.
+struct TopoPack {
+  struct Item {
+    const void *src;
+    size_t bytes, off;
+    std::function<void(char *)> bind;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  template <typename T>
+  void add(const std::vector<T> &h, T **d) {
+    const size_t off = total;
+    items.push_back(Item{h.empty() ? nullptr : h.data(), sizeof(T) * h.size(), off,
+                         [d, off](char *base) { *d = reinterpret_cast<T *>(base + off); }});
+    total += (sizeof(T) * std::max<size_t>(h.size(), 1) + 255) / 256 * 256;
   }
-  return GD_OK;
-}
+  gd_status commit(gd_context *ctx, ClusterTopo *t) {
+    void *p = nullptr;
+    gd_status s = dev_alloc(ctx, total, &p);
+    if (s != GD_OK) return s;
+    t->allocs.push_back(p);
+    t->bytes += total;
+    std::vector<char> h(total, 0);
+    for (const Item &it : items)
+      if (it.bytes) std::memcpy(h.data() + it.off, it.src, it.bytes);
+    const cudaError_t e = cudaMemcpy(p, h.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy (contact topology)");
+    for (const Item &it : items) it.bind(static_cast<char *>(p));
+    return GD_OK;
+  }
+};
 
 void group_atoms(const std::vector<uint8_t> &chain, const std::vector<int16_t> &res, const std::vector<uint8_t> &elem,
                  std::vector<int64_t> &gkey, std::vector<int> &goff, std::vector<int> &atoms) {
@@ -866,21 +883,25 @@ gd_status build_topo(gd_complex *cx, ClusterTopo **out) {
     enclosing_ball(lx.data() + a0, ly.data() + a0, lz.data() + a0, nullptr, t->lg_off[g1] - a0, c, r);
     lbsph[b] = D4{c[0], c[1], c[2], r * (1 + 1e-6) + 1e-3};
   }
-  gd_status s;
-  if ((s = topo_upload(ctx, t, lbsph, &t->d_lb_sph)) != GD_OK) {
-    for (void *p : t->allocs) cudaFree(p);
-    ctx->in_use -= std::min<uint64_t>(ctx->in_use, t->bytes);
-    delete t;
-    return s;
-  }
-  if ((s = topo_upload(ctx, t, rx, &t->d_rx)) != GD_OK || (s = topo_upload(ctx, t, ry, &t->d_ry)) != GD_OK ||
-      (s = topo_upload(ctx, t, rz, &t->d_rz)) != GD_OK || (s = topo_upload(ctx, t, lx, &t->d_lx)) != GD_OK ||
-      (s = topo_upload(ctx, t, ly, &t->d_ly)) != GD_OK || (s = topo_upload(ctx, t, lz, &t->d_lz)) != GD_OK ||
-      (s = topo_upload(ctx, t, t->rg_off, &t->d_rg_off)) != GD_OK ||
-      (s = topo_upload(ctx, t, t->lg_off, &t->d_lg_off)) != GD_OK || (s = topo_upload(ctx, t, rsph, &t->d_rg_sph)) != GD_OK ||
-      (s = topo_upload(ctx, t, lsph, &t->d_lg_sph)) != GD_OK || (s = topo_upload(ctx, t, rch, &t->d_rg_chain)) != GD_OK ||
-      (s = topo_upload(ctx, t, lch, &t->d_lg_chain)) != GD_OK || (s = topo_upload(ctx, t, r32, &t->d_r32)) != GD_OK) {
-    for (void *p : t->allocs) cudaFree(p);
+  // one allocation and one copy for every array of the topology
+  TopoPack pack;
+  pack.add(lbsph, &t->d_lb_sph);
+  pack.add(rx, &t->d_rx);
+  pack.add(ry, &t->d_ry);
+  pack.add(rz, &t->d_rz);
+  pack.add(lx, &t->d_lx);
+  pack.add(ly, &t->d_ly);
+  pack.add(lz, &t->d_lz);
+  pack.add(t->rg_off, &t->d_rg_off);
+  pack.add(t->lg_off, &t->d_lg_off);
+  pack.add(rsph, &t->d_rg_sph);
+  pack.add(lsph, &t->d_lg_sph);
+  pack.add(rch, &t->d_rg_chain);
+  pack.add(lch, &t->d_lg_chain);
+  pack.add(r32, &t->d_r32);
+  const gd_status s = pack.commit(ctx, t);
+  if (s != GD_OK) {
+    for (void *q : t->allocs) cudaFree(q);
     ctx->in_use -= std::min<uint64_t>(ctx->in_use, t->bytes);
     delete t;
     return s;

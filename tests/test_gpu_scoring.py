@@ -374,3 +374,38 @@ def test_clamped_lj_variant(oracle):
         check(cx.score_poses(genes, gd.GD_PREC_F64), ref, F64_TOL)
         check(cx.score_poses(genes, gd.GD_PREC_F32), ref, F32_TOL)
         assert np.any(np.abs(ref[:, 1]) > 100.0)  # the clamp is reached
+
+
+def _first_atoms(mol, n):
+    """The molecule's first n atoms (every per-atom field sliced)."""
+    import dataclasses
+    return dataclasses.replace(mol, **{f.name: getattr(mol, f.name)[:n] for f in dataclasses.fields(mol)})
+
+
+@pytest.mark.parametrize("nr,nl", [(1, 1), (7, 33), (64, 32), (65, 129), (129, 128), (200, 257), (513, 95)])
+def test_exact_atom_counts_around_runs_slots_and_chunks(oracle, nr, nl):
+    """Receptors cut at, or one past, the 8-atom runs and 64-atom segments of
+    the FP32 kernel, ligands at, or one past, its 32-atom slots and 128-atom
+    chunks: FP64 and FP32 (whole poses and split items, bit-identical to each
+    other) against the oracle."""
+    from gdock_gb300 import _lib
+    c = synth.make_complex(80, 40, 0, seed=nr + 3 * nl)
+    rec = _first_atoms(c.receptor, nr)
+    lig = gd.position_ligand(rec, _first_atoms(c.ligand, nl))
+    assert (len(rec), len(lig)) == (nr, nl)
+    genes = synth.quaternion_genes(np.random.default_rng(nr * 7 + nl), 24, half_box=6.0)
+    ref = oracle.score_poses(rec, lig, [], genes)
+    ctx = gd.Context(0)
+    try:
+        cx = gd.Complex(rec, lig, [], ctx=ctx)
+        check(cx.score_poses(genes, gd.GD_PREC_F64), ref, F64_TOL)
+        out = {}
+        for mode in (1, 2):
+            ctx.set_tuning(_lib.GD_TUNE_SPLIT, mode)
+            out[mode] = cx.score_poses(genes, gd.GD_PREC_F32)
+            check(out[mode], ref, F32_TOL)
+        for name in FIELDS:
+            assert np.array_equal(out[1][name], out[2][name]), name
+        cx.close()
+    finally:
+        ctx.close()

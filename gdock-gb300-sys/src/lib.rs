@@ -49,6 +49,7 @@ pub const GD_TUNE_SPLIT: i32 = 1;
 pub const GD_TUNE_FAULT: i32 = 2;
 pub const GD_TUNE_FCC: i32 = 3;
 pub const GD_TUNE_CONTACTS: i32 = 4;
+pub const GD_TUNE_RPARTS: i32 = 5;
 /// Read-only values of `gd_context_get_tuning`.
 pub const GD_INFO_LAST_FCC: i32 = 16;
 pub const GD_INFO_LAST_CONTACTS: i32 = 17;

@@ -40,6 +40,7 @@ GD_TUNE_SPLIT = 1
 GD_TUNE_FAULT = 2
 GD_TUNE_FCC = 3
 GD_TUNE_CONTACTS = 4
+GD_TUNE_RPARTS = 5
 GD_INFO_LAST_FCC = 16
 GD_INFO_LAST_CONTACTS = 17
 

@@ -112,6 +112,9 @@ gd_status check_device_error(gd_context *ctx) {
   cudaMemset(ctx->d_err, 0, sizeof(int));
   if (h == kDevTimeout) return fail(ctx, GD_ERR_TIMEOUT, "a device-side wait exceeded its spin limit");
   if (h == kDevCapacity) return fail(ctx, GD_ERR_CAPACITY, "a device-side buffer was too small");
+  if (h == kDevRange)
+    return fail(ctx, GD_ERR_INVALID_ARG,
+                "an FP32 energy partial left the fixed-point range (2^24 kcal/mol per segment): use the FP64 form");
   if (h > kDevBoundsBase)
     return fail(ctx, GD_ERR_CUDA, "device index check failed at site " + std::to_string(h - kDevBoundsBase) +
                                       " (debug library)");
@@ -516,6 +519,12 @@ gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value) {
     ctx->tune_contacts = value;
     return GD_OK;
   }
+  if (knob == GD_TUNE_RPARTS) {
+    if (value < 0 || value > 8)
+      return fail(ctx, GD_ERR_INVALID_ARG, "receptor-parts tuning: 0 (automatic) or 1..8 parts per ligand chunk");
+    ctx->tune_rparts = value;
+    return GD_OK;
+  }
   if (knob == GD_INFO_LAST_FCC || knob == GD_INFO_LAST_CONTACTS)
     return fail(ctx, GD_ERR_INVALID_ARG, "read-only knob");
   return fail(ctx, GD_ERR_INVALID_ARG, "unknown tuning knob");
@@ -528,6 +537,7 @@ int32_t gd_context_get_tuning(const gd_context *ctx, int32_t knob) {
   if (knob == GD_TUNE_FAULT) return ctx->tune_fault;
   if (knob == GD_TUNE_FCC) return ctx->tune_fcc;
   if (knob == GD_TUNE_CONTACTS) return ctx->tune_contacts;
+  if (knob == GD_TUNE_RPARTS) return ctx->tune_rparts;
   if (knob == GD_INFO_LAST_FCC) return ctx->last_fcc;
   if (knob == GD_INFO_LAST_CONTACTS) return ctx->last_contacts;
   return -1;

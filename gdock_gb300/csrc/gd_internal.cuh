@@ -34,7 +34,7 @@ constexpr int kMaxTypes = 64;
 constexpr int kDefaultF32Tune = 256 + 64 + 4;
 
 // device error codes written to the context's error word
-enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2, kDevBoundsBase = 1000 };
+enum : int { kDevOk = 0, kDevTimeout = 1, kDevCapacity = 2, kDevRange = 3, kDevBoundsBase = 1000 };
 // Index checks of the library's debug variant (built with -DGD_DEBUG_CHECKS:
 // libgdock_gb300_debug.so).  A failed check records kDevBoundsBase + site in
 // the context's error word (the first failure stays) and the caller skips or
@@ -137,6 +137,7 @@ struct gd_context {
   int tune_fault = 0;      // GD_TUNE_FAULT: 1 = drop one stage copy (failure-detection tests)
   int tune_fcc = 0;        // GD_TUNE_FCC: 0 automatic, 1 bitsets, 2 contact postings
   int tune_contacts = 0;   // GD_TUNE_CONTACTS: 0 automatic (bitmaps where possible), 1 per-residue lists
+  int tune_rparts = 0;     // GD_TUNE_RPARTS: 0 automatic, 1..8 receptor parts per ligand chunk (split mode)
   int last_fcc = 0;        // GD_INFO_LAST_FCC: pair counts of the last device clustering (1 bitsets, 2 postings)
   int last_contacts = 0;   // GD_INFO_LAST_CONTACTS: kernel of the last contact pass (1 lists, 2 bitmaps)
 };

@@ -2,7 +2,8 @@
 // work items taken from a global queue, so that poses of many complexes of
 // uneven sizes share one launch and no warp ever waits for another.  A work
 // item is one pose, or (split mode, the default) one 128-atom ligand chunk of
-// a pose.
+// a pose, or for launches with few poses one receptor part of such a chunk
+// (the receptor segments g with g mod R = part).
 //
 // Per work item a warp
 //   1. copies the complex's descriptor and the pose frame to its shared memory;
@@ -29,11 +30,14 @@
 //   6. re-decides in FP64, once per segment, the pairs of flagged steps whose
 //      FP32 d2 lies within the guard band of a cutoff (1, 8, 12, 15 A), so
 //      all decisions equal the FP64 ones;
-//   7. reduces in FP64: per-lane Kahan partials per chunk (split mode: the
-//      chunk that completes a pose adds the chunks' partials in order), warp
-//      sums, desolvation from the exact burial counts, AIR in restraint order
+//   7. reduces exactly: each segment's FP32 vdW and Coulomb partials become
+//      2^-32 fixed-point integers summed per lane (integer sums do not depend
+//      on their order, so neither do the energies on how segments, chunks and
+//      receptor parts are grouped into work items), desolvation from the
+//      exact burial counts in FP64 in a fixed order, AIR in restraint order
 //      (bit-identical), and writes the six-field record
-//      (src/chromosome.rs:110-127).
+//      (src/chromosome.rs:110-127).  Split mode: the item that completes a
+//      pose adds the items' partials.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -73,10 +77,13 @@ struct BatchParams {
   // finishes a pose last reduces its per-chunk partials
   int split;
   const long long *pose_start;    // first batch-wide pose index of each complex
-  int max_chunks;
-  double *part;                   // [pose][chunk][vdw, elec, ligand desolvation][32 lanes]
+  int max_chunks;                 // partial slots per pose (chunks x rparts)
+  double *part;                   // [pose][chunk * rparts + part][vdw, elec (fixed point), ligand desolvation][32 lanes]
   unsigned *pcount;               // [pose][max_nr] receptor burial counts
-  int *pdone;                     // [pose] chunks finished
+  int *pdone;                     // [pose] items finished
+  int rparts;                     // receptor parts per chunk (split mode; 1: whole receptor)
+  unsigned *lcount;               // [pose][max_nl] ligand burial counts (rparts > 1)
+  int max_nl;
   // failure-detection test (GD_TUNE_FAULT): the warp that takes work item 0
   // issues no copy for its first ring stage, so its bounded wait runs out
   int drop_copy;
@@ -268,12 +275,36 @@ __device__ __forceinline__ FixOut fix_pair(const ScoreParams &p, double X, doubl
   return o;
 }
 
+// A segment's FP32 energy partial as a 2^-32 fixed-point integer.  Integer
+// sums are exact, so the energies do not depend on how the segments are
+// grouped into work items (whole poses, chunks, receptor parts) nor on the
+// order the partials arrive in.  A segment's partial covers at most 256 pairs
+// (64 receptor atoms x 4 lanes' slots) whose soft-core LJ terms are bounded
+// by their well depths and Coulomb terms by 332 q q; a partial of 2^24
+// kcal/mol or more (or not a number) is reported instead of wrapped.
+__device__ __forceinline__ long long fx_energy(float x, int *err) {
+  if (!(fabsf(x) < 16777216.0f)) {
+    atomicCAS(err, 0, kDevRange);
+    return 0;
+  }
+  return __float2ll_rn(x * 4294967296.0f);
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
 __device__ __forceinline__ void bump_count(uint8_t *cnt, int i, int delta) {
   const int c = static_cast<int>(cnt[i]) + delta;
   cnt[i] = static_cast<uint8_t>(c > 255 ? 255 : (c < 0 ? 0 : c));
 }
 
-template <int S, int kAtoms, int MINB, bool SERIAL, bool CLAMP, bool SPLIT>
+// SPLIT: 0 whole poses, 1 ligand chunks, 2 ligand chunks in receptor parts
+// (bp.rparts; a separate instantiation keeps the single-part kernel's loops
+// free of the part arithmetic)
+template <int S, int kAtoms, int MINB, bool SERIAL, bool CLAMP, int SPLIT>
 __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchParams bp) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -337,11 +368,15 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     __syncwarp();
     const ScoreParams &p = *s_desc;
     if (p.skip && *p.skip) continue;  // this complex is finished (e.g. a converged GA job)
-    // split mode: item = (pose, chunk), at least one chunk per pose (an
-    // empty ligand's single chunk holds no atom); otherwise item = pose
+    // split mode: item = (pose, chunk, receptor part), at least one chunk per
+    // pose (an empty ligand's single chunk holds no atom); otherwise item =
+    // pose
+    const int R = SPLIT == 2 ? bp.rparts : 1;
     const int nchunks = SPLIT ? max(1, (p.nl + kChunk - 1) / kChunk) : (p.nl + kChunk - 1) / kChunk;
-    const int pose = static_cast<int>(SPLIT ? kk / nchunks : kk);
-    const int ch0 = SPLIT ? static_cast<int>(kk % nchunks) : 0;
+    const int per_pose = nchunks * R;
+    const int pose = static_cast<int>(SPLIT ? kk / per_pose : kk);
+    const int rem = SPLIT ? static_cast<int>(kk % per_pose) : 0;
+    const int ch0 = rem / R, rpart = rem % R;
     const int ch1 = SPLIT ? ch0 + 1 : nchunks;
     const int gp = SPLIT ? static_cast<int>(bp.pose_start[lo]) + pose : 0;  // poses of a launch fit an int
     if (!p.models && lane < 16)
@@ -360,7 +395,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
     const float reach_v = sqrtf(144.01f + 2.0f * gv) + 0.01f;
     const float reach2 = reach * reach, reach_v2 = reach_v * reach_v;
     const float2 *tab = reinterpret_cast<const float2 *>(p.tab32);
-    double vdw_t = 0.0, elec_t = 0.0, desolv_t = 0.0;
+    long long vdw_i = 0, elec_i = 0;  // 2^-32 fixed point
+    double desolv_t = 0.0;
     bool failed = false;
 
     for (int ch = ch0; ch < ch1 && !failed; ++ch) {
@@ -383,14 +419,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         s_ssph[lane] = v;
       }
       __syncwarp();
-      int nk = nseg;
+      // this item's segments: those of its receptor part (g mod R = part),
+      // culled for a rigid pose
+      const int nseg_part = (nseg - rpart + R - 1) / R;
+      int nk = nseg_part;
       bool listed = false;
       if (cull) {
         nk = 0;
         for (int g0 = 0; g0 < nseg; g0 += 32) {
           const int g = g0 + lane;
           bool keep = false;
-          if (g < nseg) {
+          if (g < nseg && g % R == rpart) {
             const float4 sg = __ldg(&p.rec_seg[g]);
 #pragma unroll
             for (int s2 = 0; s2 < S; ++s2) {
@@ -406,13 +445,14 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           nk += __popc(m);
         }
         listed = nk <= kSegListMax;
-        if (!listed) nk = nseg;  // too many to list: every segment
+        if (!listed) nk = nseg_part;  // too many to list: every segment of the part
         __syncwarp();
       }
+      auto seg_at = [&](int k) { return listed ? static_cast<int>(s_segl[k]) : rpart + k * R; };
       if (lane == 0)
         for (int k = 0; k < nk && k < kWS; ++k)
           if (!(bp.drop_copy && item == 0 && ch == ch0 && k == 0))
-            issue_seg(q + k, listed ? s_segl[k] : k, p, s_pos, s_meta, s_bar);
+            issue_seg(q + k, seg_at(k), p, s_pos, s_meta, s_bar);
       q_issued = q + min(nk, kWS);
       float lx[S], ly[S], lz[S], lq[S];
       int lt[S], lser[S], lcnt[S];
@@ -493,11 +533,11 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       const float mlim = myb.w + reach;
       const float mlim2 = (myb.w >= 0.0f) ? mlim * mlim : -1.0f;  // empty slot: no row kept
       const float mnear = myb.w + reach_v, mnear2 = mnear * mnear;
-      float sv = 0.0f, cv = 0.0f, se = 0.0f, ce = 0.0f;
+      long long fv = 0, fe = 0;  // this item's vdW and Coulomb sums, 2^-32 fixed point
       // per segment: flagged steps (high 16 bits) and recorded near rows (low 16)
       int seg_cnt = 0;
       for (int kk = 0; kk < nk; ++kk, ++q) {
-        const int g = listed ? s_segl[kk] : kk;
+        const int g = seg_at(kk);
         const int st = static_cast<int>(q % kWS);
         const bool ok = __all_sync(kFull, mbar_wait(&s_bar[st], static_cast<uint32_t>((q / kWS) & 1)));
         if (!ok) {
@@ -656,8 +696,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           if (bm) atomicAdd(&s_rc[s_cidx[t] - sbase], __popc(bm));
         }
         seg_cnt = 0;
-        kahan_add(sv, cv, av);
-        kahan_add(se, ce, ae);
+        fv += fx_energy(av, bp.err);
+        fe += fx_energy(ae, bp.err);
         __syncwarp();
         // receptor burial counts of this segment into the per-item counters
         for (int i = lane; i < na; i += 32) {
@@ -673,7 +713,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         }
         __syncwarp();
         if (lane == 0 && kk + kWS < nk) {
-          issue_seg(q + kWS, listed ? s_segl[kk + kWS] : kk + kWS, p, s_pos, s_meta, s_bar);
+          issue_seg(q + kWS, seg_at(kk + kWS), p, s_pos, s_meta, s_bar);
           q_issued = q + kWS + 1;
         }
       }
@@ -681,25 +721,30 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       __syncwarp();
       // the chunk's per-lane partials; both modes add them in chunk order,
       // so split and whole-pose items give bit-identical energies
+      // ligand desolvation from this chunk's burial counts; with receptor
+      // parts the counts are only partial here and go to the pose's counters
       double dch = 0.0;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         lcnt[s] += s_lfix[s * 32 + lane];  // burial corrections of FP64 re-decisions
         s_lfix[s * 32 + lane] = 0;
         const int j = ch * kChunk + s * 32 + lane;
-        if (j < p.nl) dch += p.lig_desolv[static_cast<size_t>(j) * 11 + min(lcnt[s], 10)];
+        if (R == 1) {
+          if (j < p.nl) dch += p.lig_desolv[static_cast<size_t>(j) * 11 + min(lcnt[s], 10)];
+        } else if (j < p.nl && lcnt[s] != 0 && GD_DCHECK(bp.err, j < bp.max_nl, 11)) {
+          atomicAdd(&bp.lcount[static_cast<size_t>(gp) * bp.max_nl + j], static_cast<unsigned>(lcnt[s]));
+        }
       }
-      const double vch = static_cast<double>(sv) - static_cast<double>(cv);
-      const double ech = static_cast<double>(se) - static_cast<double>(ce);
       if (SPLIT) {
-        if (!GD_DCHECK(bp.err, ch < bp.max_chunks, 9)) break;
-        double *pt = bp.part + (static_cast<size_t>(gp) * bp.max_chunks + ch) * 96;
-        pt[lane] = vch;
-        pt[32 + lane] = ech;
+        const int slot = ch * R + rpart;
+        if (!GD_DCHECK(bp.err, slot < bp.max_chunks, 9)) break;
+        double *pt = bp.part + (static_cast<size_t>(gp) * bp.max_chunks + slot) * 96;
+        reinterpret_cast<long long *>(pt)[lane] = fv;
+        reinterpret_cast<long long *>(pt)[32 + lane] = fe;
         pt[64 + lane] = dch;
       } else {
-        vdw_t += vch;
-        elec_t += ech;
+        vdw_i += fv;
+        elec_i += fe;
         desolv_t += dch;
       }
     }
@@ -720,13 +765,30 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       int done = 0;
       if (lane == 0) done = atomicAdd(&bp.pdone[gp], 1);
       done = __shfl_sync(kFull, done, 0);
-      if (done != nchunks - 1) continue;
+      if (done != per_pose - 1) continue;
       __threadfence();
+      for (int c = 0; c < per_pose; ++c) {
+        const long long *pi =
+            reinterpret_cast<const long long *>(bp.part + (static_cast<size_t>(gp) * bp.max_chunks + c) * 96);
+        vdw_i += __ldcg(pi + lane);
+        elec_i += __ldcg(pi + 32 + lane);
+      }
+      // ligand desolvation chunk by chunk, in the same order and arithmetic
+      // as whole-pose items
       for (int c = 0; c < nchunks; ++c) {
-        const double *pt = bp.part + (static_cast<size_t>(gp) * bp.max_chunks + c) * 96;
-        vdw_t += __ldcg(pt + lane);
-        elec_t += __ldcg(pt + 32 + lane);
-        desolv_t += __ldcg(pt + 64 + lane);
+        if (R == 1) {
+          desolv_t += __ldcg(bp.part + (static_cast<size_t>(gp) * bp.max_chunks + c) * 96 + 64 + lane);
+        } else {
+          double dc = 0.0;
+          for (int s = 0; s < S; ++s) {
+            const int j = c * kChunk + s * 32 + lane;
+            if (j < p.nl) {
+              const unsigned n = __ldcg(&bp.lcount[static_cast<size_t>(gp) * bp.max_nl + j]);
+              dc += p.lig_desolv[static_cast<size_t>(j) * 11 + (n < 10u ? n : 10u)];
+            }
+          }
+          desolv_t += dc;
+        }
       }
       for (int i = lane; i < p.nr; i += 32) {
         const unsigned c = __ldcg(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + i]);
@@ -740,8 +802,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         cnt[i] = 0;
       }
     }
-    vdw_t = warp_sum(vdw_t);
-    elec_t = warp_sum(elec_t);
+    const double vdw_t = static_cast<double>(warp_sum_ll(vdw_i)) * 0x1p-32;
+    const double elec_t = static_cast<double>(warp_sum_ll(elec_i)) * 0x1p-32;
     desolv_t = warp_sum(desolv_t);
     // AIR: one restraint per lane, summed in restraint order
     double air = 0.0;
@@ -787,6 +849,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
 // 4 slots and 4 rows per step, five CTAs per SM, used for launches with few
 // poses per warp.
 constexpr int kSplitTune = -1;
+constexpr int kSplitPartsTune = -2;  // the split kernel with receptor parts
 
 // Kernel variants.  The common case (no equal receptor/ligand serials, no
 // clamp needed) has a tuning grid of slots per lane S, receptor atoms per
@@ -795,19 +858,20 @@ constexpr int kSplitTune = -1;
 // + 256 for the register cap of five resident CTAs per SM.
 template <typename F>
 cudaError_t with_variant(int tune, bool serial, bool clamp, F f) {
-  if (tune == kSplitTune) return f(k_score_f32w<4, 4, 5, false, false, true>);
+  if (tune == kSplitTune) return f(k_score_f32w<4, 4, 5, false, false, 1>);
+  if (tune == kSplitPartsTune) return f(k_score_f32w<4, 4, 5, false, false, 2>);
   if (serial || clamp) {
-    if (serial && clamp) return f(k_score_f32w<4, 1, 4, true, true, false>);
-    if (serial) return f(k_score_f32w<4, 1, 4, true, false, false>);
-    return f(k_score_f32w<4, 1, 4, false, true, false>);
+    if (serial && clamp) return f(k_score_f32w<4, 1, 4, true, true, 0>);
+    if (serial) return f(k_score_f32w<4, 1, 4, true, false, 0>);
+    return f(k_score_f32w<4, 1, 4, false, true, 0>);
   }
   switch (tune) {
-    case 4: return f(k_score_f32w<4, 1, 4, false, false, false>);
-    case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false, false>);
-    case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false, false>);
-    case 256 + 64 + 2: return f(k_score_f32w<2, 4, 5, false, false, false>);
-    case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false, false>);
-    default: return f(k_score_f32w<4, 4, 5, false, false, false>);  // 256 + 64 + 4 = kDefaultF32Tune
+    case 4: return f(k_score_f32w<4, 1, 4, false, false, 0>);
+    case 64 + 2: return f(k_score_f32w<2, 4, 4, false, false, 0>);
+    case 64 + 4: return f(k_score_f32w<4, 4, 4, false, false, 0>);
+    case 256 + 64 + 2: return f(k_score_f32w<2, 4, 5, false, false, 0>);
+    case 16 + 4: return f(k_score_f32w<4, 2, 4, false, false, 0>);
+    default: return f(k_score_f32w<4, 4, 5, false, false, 0>);  // 256 + 64 + 4 = kDefaultF32Tune
   }
 }
 
@@ -853,10 +917,12 @@ struct BatchPlan {
   std::vector<long long> start;       // work-item prefix per complex
   std::vector<long long> pose_start;  // pose prefix per complex
   int split = 0, max_chunks = 1;
-  size_t part_b = 0, cnt_b = 0, done_b = 0;  // split-mode scratch
+  int rparts = 1, max_nl = 0;  // receptor parts per chunk (split mode), longest ligand
+  size_t part_b = 0, cnt_b = 0, done_b = 0, lcnt_b = 0;  // split-mode scratch
 };
 
 constexpr size_t kSplitScratchMax = size_t(4) << 30;  // split scratch beyond this: whole poses
+constexpr int kMaxRparts = 8;  // receptor parts per chunk, at most (GD_TUNE_RPARTS accepts 1..8)
 
 static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
 
@@ -873,11 +939,18 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   pl->start.assign(ncx + 1, 0);
   pl->pose_start.assign(ncx + 1, 0);
   pl->max_nr = 0;
+  pl->max_nl = 0;
   pl->max_chunks = 1;
+  long long chunk_items = 0;  // (pose, chunk) items of a split launch
+  int max_nseg = 1;
   for (int c = 0; c < ncx; ++c) {
     pl->pose_start[c + 1] = pl->pose_start[c] + descs[c].n_poses;
     pl->max_nr = std::max(pl->max_nr, descs[c].nr);
-    pl->max_chunks = std::max(pl->max_chunks, (descs[c].nl + chunk_split - 1) / chunk_split);
+    pl->max_nl = std::max(pl->max_nl, descs[c].nl);
+    const int nch = std::max(1, (descs[c].nl + chunk_split - 1) / chunk_split);
+    pl->max_chunks = std::max(pl->max_chunks, nch);
+    chunk_items += static_cast<long long>(descs[c].n_poses) * nch;
+    max_nseg = std::max(max_nseg, (descs[c].nr + kSeg - 1) / kSeg);
   }
   const long long poses = pl->pose_start[ncx];
   pl->tune = slots;
@@ -891,25 +964,63 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   int per_sm = 0;
   cudaError_t e = fit(pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0, &per_sm);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
-  const size_t part_b = static_cast<size_t>(poses) * pl->max_chunks * 96 * sizeof(double);
-  const size_t cnt_b = static_cast<size_t>(poses) * pl->max_nr * sizeof(unsigned);
-  const size_t split_b = al256(part_b) + al256(cnt_b) + al256(static_cast<size_t>(poses) * sizeof(int));
-  const bool fits = split_b <= kSplitScratchMax && (ctx->budget == 0 || ctx->in_use + split_b <= ctx->budget);
+  // receptor parts: a launch with fewer (pose, chunk) items than about two
+  // rounds of the split kernel's resident warps splits each chunk's receptor
+  // into R interleaved segment sets, so that the SMs fill, keeping at least
+  // two segments per part.  A part's item also pays the chunk's set-up, so
+  // for receptors of fewer than 16 segments the target shrinks in
+  // proportion (measured on receptors of 6, 40 and 107 segments at 150 to
+  // 1,200 poses).  GD_TUNE_RPARTS forces R.  The energies do not depend on R
+  // (fixed-point sums).
+  int split_per_sm = 0;
+  {
+    const int keep_tune = pl->tune;
+    pl->tune = kSplitTune;
+    e = fit(0, &split_per_sm);
+    pl->tune = keep_tune;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
+    e = fit(pl->max_nr <= kCntSmemMax ? ((pl->max_nr + 15) / 16) * 16 : 0, &per_sm);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
+  }
+  const long long target = static_cast<long long>(std::min(2.0, max_nseg / 8.0) * split_per_sm * kWarps *
+                                                  ctx->sm_count);
+  int R = ctx->tune_rparts > 0 ? ctx->tune_rparts
+                               : static_cast<int>(std::min<long long>(
+                                     kMaxRparts, std::max<long long>(1, (target + std::max(chunk_items, 1LL) - 1) /
+                                                                            std::max(chunk_items, 1LL))));
+  if (ctx->tune_rparts <= 0) R = std::max(1, std::min(R, max_nseg / 2));
+  auto split_bytes = [&](int r, size_t *part_b, size_t *cnt_b, size_t *lcnt_b) {
+    *part_b = static_cast<size_t>(poses) * pl->max_chunks * r * 96 * sizeof(double);
+    *cnt_b = static_cast<size_t>(poses) * pl->max_nr * sizeof(unsigned);
+    *lcnt_b = r > 1 ? static_cast<size_t>(poses) * std::max(pl->max_nl, 1) * sizeof(unsigned) : 0;
+    const size_t b = al256(*part_b) + al256(*cnt_b) + al256(static_cast<size_t>(poses) * sizeof(int)) + al256(*lcnt_b);
+    return b <= kSplitScratchMax && (ctx->budget == 0 || ctx->in_use + b <= ctx->budget);
+  };
+  size_t part_b = 0, cnt_b = 0, lcnt_b = 0;
+  bool fits = split_bytes(R, &part_b, &cnt_b, &lcnt_b);
+  if (!fits && R > 1 && ctx->tune_rparts <= 0) {
+    R = 1;
+    fits = split_bytes(R, &part_b, &cnt_b, &lcnt_b);
+  }
   pl->split = 0;
-  if (allow_split && fits && poses > 0 && pl->max_chunks > 1 && !serial && !clamp)
+  if (allow_split && fits && poses > 0 && (pl->max_chunks > 1 || R > 1) && !serial && !clamp)
     pl->split = ctx->tune_split != 1;
   if (pl->split) {
+    pl->rparts = R;
     pl->part_b = part_b;
     pl->cnt_b = cnt_b;
+    pl->lcnt_b = lcnt_b;
     pl->done_b = static_cast<size_t>(poses) * sizeof(int);
-    pl->tune = kSplitTune;
+    pl->tune = R > 1 ? kSplitPartsTune : kSplitTune;
     e = fit(0, &per_sm);  // burial counters live in the split scratch
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring occupancy");
   } else {
-    pl->part_b = pl->cnt_b = pl->done_b = 0;
+    pl->rparts = 1;
+    pl->part_b = pl->cnt_b = pl->done_b = pl->lcnt_b = 0;
   }
   for (int c = 0; c < ncx; ++c) {
-    const long long per_pose = pl->split ? std::max(1, (descs[c].nl + chunk_split - 1) / chunk_split) : 1;
+    const long long per_pose =
+        pl->split ? static_cast<long long>(std::max(1, (descs[c].nl + chunk_split - 1) / chunk_split)) * pl->rparts : 1;
     pl->start[c + 1] = pl->start[c] + static_cast<long long>(descs[c].n_poses) * per_pose;
   }
   const long long items = pl->start[ncx];
@@ -922,7 +1033,7 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
 // prefix, per-warp global burial counters (large receptors, whole-pose
 // items), split-mode partials, burial counts and chunk counters.
 struct ArgLayout {
-  size_t desc, start, queue, pstart, gcounts, part, pcount, pdone, total;
+  size_t desc, start, queue, pstart, gcounts, part, pcount, pdone, lcount, total;
 };
 
 static ArgLayout arg_layout(int ncx, const BatchPlan &pl, size_t gcount_bytes) {
@@ -944,6 +1055,8 @@ static ArgLayout arg_layout(int ncx, const BatchPlan &pl, size_t gcount_bytes) {
   o += al256(pl.cnt_b);
   L.pdone = o;
   o += al256(pl.done_b);
+  L.lcount = o;
+  o += al256(pl.lcnt_b);
   L.total = o;
   return L;
 }
@@ -989,10 +1102,13 @@ static gd_status launch_args(gd_context *ctx, int ncx, const BatchPlan &pl, cons
   bp.split = pl.split;
   bp.drop_copy = ctx->tune_fault == 1;
   bp.pose_start = reinterpret_cast<const long long *>(arg + L.pstart);
-  bp.max_chunks = pl.max_chunks;
+  bp.max_chunks = pl.max_chunks * pl.rparts;
   bp.part = pl.split ? reinterpret_cast<double *>(arg + L.part) : nullptr;
   bp.pcount = pl.split ? reinterpret_cast<unsigned *>(arg + L.pcount) : nullptr;
   bp.pdone = pl.split ? reinterpret_cast<int *>(arg + L.pdone) : nullptr;
+  bp.rparts = pl.split ? pl.rparts : 1;
+  bp.lcount = pl.split && pl.rparts > 1 ? reinterpret_cast<unsigned *>(arg + L.lcount) : nullptr;
+  bp.max_nl = pl.max_nl;
   e = launch_var(pl.tune, bp, serial, clamp, pl.smem, pl.grid, stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched scoring launch");
   return GD_OK;

@@ -131,12 +131,18 @@ gd_status gd_context_destroy(gd_context *ctx);
  *                      share no residue, else per-residue contact lists),
  *                      1 = per-residue contact lists always.  Both decide
  *                      every atom pair exactly; the keys are identical.
+ *   GD_TUNE_RPARTS:    receptor parts per ligand chunk of a split FP32
+ *                      launch: 0 = automatic (more than one only when the
+ *                      launch has too few (pose, chunk) items to fill the
+ *                      GPU), 1..8 = that many.  The energies do not depend
+ *                      on it (per-segment fixed-point sums).
  * Read-only (gd_context_get_tuning; set_tuning refuses them):
  *   GD_INFO_LAST_FCC:      pair counts of the context's last device
  *                          clustering: 1 bitsets, 2 postings, 0 none yet.
  *   GD_INFO_LAST_CONTACTS: contact pass of the last gd_pose_contacts or
  *                          gd_cluster: 1 lists, 2 bitmaps, 0 none yet. */
 enum { GD_TUNE_F32_SLOTS = 0, GD_TUNE_SPLIT = 1, GD_TUNE_FAULT = 2, GD_TUNE_FCC = 3, GD_TUNE_CONTACTS = 4,
+       GD_TUNE_RPARTS = 5,
        GD_INFO_LAST_FCC = 16, GD_INFO_LAST_CONTACTS = 17 };
 gd_status gd_context_set_tuning(gd_context *ctx, int32_t knob, int32_t value);
 /* The FP32 scoring autotuner: times every candidate (GD_TUNE_F32_SLOTS,

@@ -409,3 +409,65 @@ def test_exact_atom_counts_around_runs_slots_and_chunks(oracle, nr, nl):
         cx.close()
     finally:
         ctx.close()
+
+
+def test_receptor_parts_do_not_change_the_energies(oracle):
+    """Split launches may cut each ligand chunk's receptor into R interleaved
+    segment sets (GD_TUNE_RPARTS; automatically for launches with few poses).
+    The vdW and Coulomb sums are per-segment fixed-point integers, so R = 1,
+    2, 3 and 8, and whole-pose items, give bit-identical energies, all within
+    the FP32 tolerance of the oracle."""
+    from gdock_gb300 import _lib
+    cases = [synth.make_complex(50, 76, 6, seed=11), synth.make_complex(300, 150, 12, seed=2),
+             synth.make_complex(12, 40, 2, seed=4)]
+    ctx = gd.Context(0)
+    try:
+        for c in cases:
+            lig = gd.position_ligand(c.receptor, c.ligand)
+            cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
+            genes = synth.quaternion_genes(np.random.default_rng(len(c.receptor)), 30, half_box=10.0)
+            ref = oracle.score_poses(c.receptor, lig, c.restraint_pairs, genes)
+            ctx.set_tuning(_lib.GD_TUNE_SPLIT, 1)
+            whole = cx.score_poses(genes, gd.GD_PREC_F32)
+            check(whole, ref, F32_TOL)
+            ctx.set_tuning(_lib.GD_TUNE_SPLIT, 2)
+            for r in (0, 1, 2, 3, 8):
+                ctx.set_tuning(_lib.GD_TUNE_RPARTS, r)
+                assert ctx.get_tuning(_lib.GD_TUNE_RPARTS) == r
+                got = cx.score_poses(genes, gd.GD_PREC_F32)
+                for name in FIELDS:
+                    assert np.array_equal(got[name], whole[name]), (len(c.receptor), r, name)
+            ctx.set_tuning(_lib.GD_TUNE_RPARTS, 0)
+            ctx.set_tuning(_lib.GD_TUNE_SPLIT, 0)
+            cx.close()
+        with pytest.raises(gd.GdError):
+            ctx.set_tuning(_lib.GD_TUNE_RPARTS, 9)
+    finally:
+        ctx.close()
+
+
+def test_fp32_sum_range_is_reported(oracle):
+    """Charges so large that one segment's FP32 Coulomb partial leaves the
+    fixed-point range (2^24 kcal/mol) make the FP32 call fail with a status
+    instead of wrapping; the FP64 form still scores them, and the context
+    keeps working."""
+    rec = make_mol([tatom(0.0, 0.0, 0.0, "C", charge=3000.0, resseq=1, serial=1, chain="A"),
+                    tatom(1.5, 0.0, 0.0, "C", charge=3000.0, resseq=2, serial=2, chain="A")])
+    lig = make_mol([tatom(0.0, 2.0, 0.0, "C", charge=3000.0, resseq=1, serial=11, chain="B"),
+                    tatom(0.0, -2.0, 0.0, "C", charge=-3000.0, resseq=2, serial=12, chain="B")])
+    genes = np.zeros((2, 6))
+    ctx = gd.Context(0)
+    try:
+        cx = gd.Complex(rec, lig, [], ctx=ctx)
+        with pytest.raises(gd.GdError):
+            cx.score_poses(genes, gd.GD_PREC_F32)
+        check(cx.score_poses(genes, gd.GD_PREC_F64), oracle.score_poses(rec, lig, [], genes), F64_TOL)
+        cx.close()
+        c = synth.make_complex(20, 10, 0, seed=3)
+        lig2 = gd.position_ligand(c.receptor, c.ligand)
+        cx2 = gd.Complex(c.receptor, lig2, [], ctx=ctx)
+        g2 = synth.random_genes(np.random.default_rng(2), 4, max_displacement=5.0)
+        check(cx2.score_poses(g2, gd.GD_PREC_F32), oracle.score_poses(c.receptor, lig2, [], g2), F32_TOL)
+        cx2.close()
+    finally:
+        ctx.close()

@@ -103,13 +103,6 @@ static __device__ __forceinline__ double exact_d2(double ax, double ay, double a
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
-static __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
-  const float y = __fsub_rn(x, c);
-  const float t = __fadd_rn(s, y);
-  c = __fsub_rn(__fsub_rn(t, s), y);
-  s = t;
-}
-
 static __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
@@ -174,6 +167,5 @@ static __device__ void write_pose(const ScoreParams &p, int pose, double vdw, do
                         __dmul_rn(p.wa, air));
   p.out[pose] = o;
 }
-
 
 }  // namespace gd

@@ -38,8 +38,8 @@ N_REC_RES, N_LIG_RES, N_RESTRAINTS, N_POSES, SEED = 300, 150, 12, 65536, 2026
 FLOP_PER_PAIR = 37  # convention: d2 8, LJ 18, Coulomb 4, cutoff tests 5, burial 2
 # DRAM bytes per pose of the FP32 scoring kernel: dram__bytes_read.sum +
 # dram__bytes_write.sum of one ncu capture of the split-mode kernel on 4,096
-# poses of this workload, 43.13 MB + 8.00 MB (profiles/k_score_f32w_single_complex.md)
-TRAFFIC_PER_POSE = (43.131392e6 + 8.000512e6) / 4096
+# poses of this workload, 22.40 MB + 0.71 MB (profiles/k_score_f32w_single_complex.md)
+TRAFFIC_PER_POSE = (22.403840e6 + 0.710656e6) / 4096
 METRIC = "poses/s (batched FP32 scoring, single complex)"
 
 

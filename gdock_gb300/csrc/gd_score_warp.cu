@@ -79,7 +79,7 @@ struct BatchParams {
   const long long *pose_start;    // first batch-wide pose index of each complex
   int max_chunks;                 // partial slots per pose (chunks x rparts)
   double *part;                   // [pose][chunk * rparts + part][vdw, elec (fixed point), ligand desolvation][32 lanes]
-  unsigned *pcount;               // [pose][max_nr] receptor burial counts
+  unsigned *pcount;               // [pose][(max_nr + 1) / 2] receptor burial counts, two 16-bit counts a word
   int *pdone;                     // [pose] items finished
   int rparts;                     // receptor parts per chunk (split mode; 1: whole receptor)
   unsigned *lcount;               // [pose][max_nl] ligand burial counts (rparts > 1)
@@ -704,8 +704,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
           const int c = s_rc[i];
           if (c) {
             if (SPLIT) {
-              if (GD_DCHECK(bp.err, gbase + i < bp.max_nr, 10))
-                atomicAdd(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + gbase + i], static_cast<unsigned>(c));
+              // a count never exceeds the ligand's atoms (< 65,536 in split
+              // launches), so the two halves of a word never carry into each other
+              const int a = gbase + i;
+              if (GD_DCHECK(bp.err, a < bp.max_nr, 10))
+                atomicAdd(&bp.pcount[static_cast<size_t>(gp) * ((bp.max_nr + 1) >> 1) + (a >> 1)],
+                          static_cast<unsigned>(c) << ((a & 1) * 16));
             }
             else bump_count(cnt, gbase + i, c);
             s_rc[i] = 0;
@@ -791,7 +795,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
         }
       }
       for (int i = lane; i < p.nr; i += 32) {
-        const unsigned c = __ldcg(&bp.pcount[static_cast<size_t>(gp) * bp.max_nr + i]);
+        const unsigned w = __ldcg(&bp.pcount[static_cast<size_t>(gp) * ((bp.max_nr + 1) >> 1) + (i >> 1)]);
+        const unsigned c = (w >> ((i & 1) * 16)) & 0xffffu;
         desolv_t += p.rec_desolv[static_cast<size_t>(i) * 11 + (c < 10u ? c : 10u)];
       }
     } else {
@@ -991,7 +996,7 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
   if (ctx->tune_rparts <= 0) R = std::max(1, std::min(R, max_nseg / 2));
   auto split_bytes = [&](int r, size_t *part_b, size_t *cnt_b, size_t *lcnt_b) {
     *part_b = static_cast<size_t>(poses) * pl->max_chunks * r * 96 * sizeof(double);
-    *cnt_b = static_cast<size_t>(poses) * pl->max_nr * sizeof(unsigned);
+    *cnt_b = static_cast<size_t>(poses) * ((pl->max_nr + 1) / 2) * sizeof(unsigned);
     *lcnt_b = r > 1 ? static_cast<size_t>(poses) * std::max(pl->max_nl, 1) * sizeof(unsigned) : 0;
     const size_t b = al256(*part_b) + al256(*cnt_b) + al256(static_cast<size_t>(poses) * sizeof(int)) + al256(*lcnt_b);
     return b <= kSplitScratchMax && (ctx->budget == 0 || ctx->in_use + b <= ctx->budget);
@@ -1003,7 +1008,8 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
     fits = split_bytes(R, &part_b, &cnt_b, &lcnt_b);
   }
   pl->split = 0;
-  if (allow_split && fits && poses > 0 && (pl->max_chunks > 1 || R > 1) && !serial && !clamp)
+  // split launches keep receptor burial counts in 16 bits: ligands up to 65,535 atoms
+  if (allow_split && fits && poses > 0 && (pl->max_chunks > 1 || R > 1) && !serial && !clamp && pl->max_nl < 65536)
     pl->split = ctx->tune_split != 1;
   if (pl->split) {
     pl->rparts = R;

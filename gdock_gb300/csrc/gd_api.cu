@@ -770,27 +770,34 @@ gd_status gd_complex_set_weights(gd_complex *cx, const gd_weights *w) {
   return GD_OK;
 }
 
-gd_status gd_make_frames(const double *genes, int32_t n, gd_pose_frame *frames) {
-  if (n < 0 || (n > 0 && (!genes || !frames))) return GD_ERR_INVALID_ARG;
-  const int nth = n >= 4096 ? std::max(1u, std::min(16u, std::thread::hardware_concurrency())) : 1;
+// Frames of n poses on up to 16 host threads (from 4,096 poses), and the
+// largest |displacement| component among them (sizes the FP32 guard bands).
+static void frames_and_max_disp(const double *genes, int n, gd_pose_frame *frames, double *max_disp) {
+  const int nth = n >= 4096 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) : 1;
+  std::vector<double> m(nth, 0.0);
+  auto work = [&](int t) {
+    double mt = 0.0;
+    for (int i = t; i < n; i += nth) {
+      const double *g = genes + 6 * static_cast<size_t>(i);
+      make_frame(g, frames + i);
+      mt = std::max({mt, std::fabs(g[3]), std::fabs(g[4]), std::fabs(g[5])});
+    }
+    m[t] = mt;
+  };
   if (nth <= 1) {
-    for (int i = 0; i < n; ++i) make_frame(genes + 6 * static_cast<size_t>(i), frames + i);
-    return GD_OK;
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
   }
-  std::vector<std::thread> th;
-  for (int t = 0; t < nth; ++t)
-    th.emplace_back([=]() {
-      for (int i = t; i < n; i += nth) make_frame(genes + 6 * static_cast<size_t>(i), frames + i);
-    });
-  for (auto &x : th) x.join();
-  return GD_OK;
+  if (max_disp) *max_disp = *std::max_element(m.begin(), m.end());
 }
 
-static double max_abs_disp(const double *genes, int n) {
-  double m = 0.0;
-  for (int i = 0; i < n; ++i)
-    for (int k = 3; k < 6; ++k) m = std::max(m, std::fabs(genes[6 * static_cast<size_t>(i) + k]));
-  return m;
+gd_status gd_make_frames(const double *genes, int32_t n, gd_pose_frame *frames) {
+  if (n < 0 || (n > 0 && (!genes || !frames))) return GD_ERR_INVALID_ARG;
+  frames_and_max_disp(genes, n, frames, nullptr);
+  return GD_OK;
 }
 
 gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_precision prec, gd_pose_energy *out) {
@@ -808,10 +815,11 @@ gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_prec
   gd_pose_energy *h_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->h_pinned) + ((fb + 255) / 256) * 256);
   gd_pose_frame *d_frames = static_cast<gd_pose_frame *>(ctx->d_scratch);
   gd_pose_energy *d_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->d_scratch) + ((fb + 255) / 256) * 256);
-  gd_make_frames(genes, n, h_frames);
+  double maxd = 0.0;
+  frames_and_max_disp(genes, n, h_frames, &maxd);
   cudaError_t e = cudaMemcpyAsync(d_frames, h_frames, fb, cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "H2D frames");
-  s = launch_score(cx, d_frames, nullptr, n, prec, d_out, ctx->stream, max_abs_disp(genes, n));
+  s = launch_score(cx, d_frames, nullptr, n, prec, d_out, ctx->stream, maxd);
   if (s != GD_OK) return s;
   e = cudaMemcpyAsync(h_out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "D2H energies");

@@ -723,10 +723,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) k_score_f32w(const BatchPar
       }
       if (failed) break;
       __syncwarp();
-      // the chunk's per-lane partials; both modes add them in chunk order,
-      // so split and whole-pose items give bit-identical energies
-      // ligand desolvation from this chunk's burial counts; with receptor
-      // parts the counts are only partial here and go to the pose's counters
+      // the chunk's per-lane partials (split and whole-pose items add them
+      // alike, so both give bit-identical energies): ligand desolvation from
+      // this chunk's burial counts; with receptor parts the counts are only
+      // partial here and go to the pose's counters
       double dch = 0.0;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
@@ -1037,7 +1037,8 @@ static gd_status plan_batch(gd_context *ctx, const std::vector<ScoreParams> &des
 
 // Layout of the argument block: descriptors, item prefix, work counter, pose
 // prefix, per-warp global burial counters (large receptors, whole-pose
-// items), split-mode partials, burial counts and chunk counters.
+// items), split-mode partials, receptor burial counts, item counters and
+// (receptor parts) ligand burial counts.
 struct ArgLayout {
   size_t desc, start, queue, pstart, gcounts, part, pcount, pdone, lcount, total;
 };

@@ -5,13 +5,17 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <chrono>
 #include <functional>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
+#include <condition_variable>
+#include <mutex>
 #include <thread>
+#include <unistd.h>
 #include <cstdint>
 #include <utility>
 
@@ -770,26 +774,102 @@ gd_status gd_complex_set_weights(gd_complex *cx, const gd_weights *w) {
   return GD_OK;
 }
 
-// Frames of n poses on up to 16 host threads (from 4,096 poses), and the
-// largest |displacement| component among them (sizes the FP32 guard bands).
+// Host worker threads kept across calls: starting 16 threads costs more than
+// building a large batch's frames on them, and gdock builds frames every
+// generation.  run(k, f) calls f(0..k-1) on the workers and the calling
+// thread and returns when all are done; callers are serialised.  The pool is
+// never destroyed (its threads end with the process), and a process forked
+// after it was made builds its own (a child has none of the parent's
+// threads).
+class HostPool {
+ public:
+  static HostPool &get() {
+    static std::mutex mu;
+    static HostPool *pool = nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pool || pool->pid_ != getpid()) pool = new HostPool();  // a forked child's pool replaces the parent's
+    return *pool;
+  }
+  int size() const { return static_cast<int>(workers_.size()) + 1; }
+  void run(int k, const std::function<void(int)> &f) {
+    std::lock_guard<std::mutex> caller(run_mu_);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &f;
+      tasks_ = k;
+      next_ = 0;
+      done_ = 0;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return done_ == tasks_; });
+    fn_ = nullptr;
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    const int n = static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) - 1;
+    for (int i = 0; i < n; ++i)
+      workers_.emplace_back([this] {
+        long long seen = 0;
+        for (;;) {
+          {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [&] { return gen_ != seen; });
+            seen = gen_;
+          }
+          work();
+        }
+      });
+    for (auto &w : workers_) w.detach();
+  }
+  // take tasks until none is left
+  void work() {
+    for (;;) {
+      int t;
+      const std::function<void(int)> *f;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!fn_ || next_ >= tasks_) return;
+        t = next_++;
+        f = fn_;
+      }
+      (*f)(t);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (++done_ == tasks_) done_cv_.notify_all();
+    }
+  }
+  pid_t pid_;
+  std::vector<std::thread> workers_;
+  std::mutex mu_, run_mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)> *fn_ = nullptr;
+  int tasks_ = 0, next_ = 0, done_ = 0;
+  long long gen_ = 0;
+};
+
+// Frames of n poses, on the host pool from 4,096 poses, and the largest
+// |displacement| component among them (sizes the FP32 guard bands).
 static void frames_and_max_disp(const double *genes, int n, gd_pose_frame *frames, double *max_disp) {
-  const int nth = n >= 4096 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) : 1;
-  std::vector<double> m(nth, 0.0);
+  const int nt = n >= 4096 ? 64 : 1;  // contiguous ranges of poses
+  std::vector<double> m(nt, 0.0);
   auto work = [&](int t) {
+    const int i0 = static_cast<int>(static_cast<long long>(n) * t / nt),
+              i1 = static_cast<int>(static_cast<long long>(n) * (t + 1) / nt);
     double mt = 0.0;
-    for (int i = t; i < n; i += nth) {
+    for (int i = i0; i < i1; ++i) {
       const double *g = genes + 6 * static_cast<size_t>(i);
       make_frame(g, frames + i);
       mt = std::max({mt, std::fabs(g[3]), std::fabs(g[4]), std::fabs(g[5])});
     }
     m[t] = mt;
   };
-  if (nth <= 1) {
+  if (nt == 1) {
     work(0);
   } else {
-    std::vector<std::thread> th;
-    for (int t = 0; t < nth; ++t) th.emplace_back(work, t);
-    for (auto &x : th) x.join();
+    HostPool::get().run(nt, work);
   }
   if (max_disp) *max_disp = *std::max_element(m.begin(), m.end());
 }
@@ -815,19 +895,33 @@ gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_prec
   gd_pose_energy *h_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->h_pinned) + ((fb + 255) / 256) * 256);
   gd_pose_frame *d_frames = static_cast<gd_pose_frame *>(ctx->d_scratch);
   gd_pose_energy *d_out = reinterpret_cast<gd_pose_energy *>(static_cast<char *>(ctx->d_scratch) + ((fb + 255) / 256) * 256);
+  // phase times on stderr with GD_TRACE (host frames, launch set-up, device
+  // work and copies, result copy)
+  const bool tr = trace_on();
+  auto t = std::chrono::steady_clock::now();
+  auto lap = [&](const char *name) {
+    if (!tr) return;
+    const auto now = std::chrono::steady_clock::now();
+    trace(name, std::chrono::duration<double>(now - t).count());
+    t = now;
+  };
   double maxd = 0.0;
   frames_and_max_disp(genes, n, h_frames, &maxd);
+  lap("score_poses: frames (host)");
   cudaError_t e = cudaMemcpyAsync(d_frames, h_frames, fb, cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "H2D frames");
   s = launch_score(cx, d_frames, nullptr, n, prec, d_out, ctx->stream, maxd);
   if (s != GD_OK) return s;
   e = cudaMemcpyAsync(h_out, d_out, ob, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "D2H energies");
+  lap("score_poses: copies and launch issued");
   e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "score kernel");
+  lap("score_poses: wait for the device");
   s = check_device_error(ctx);
   if (s != GD_OK) return s;
   std::memcpy(out, h_out, ob);
+  lap("score_poses: error word and result copy");
   return GD_OK;
 }
 

@@ -93,3 +93,45 @@ def test_header_is_plain_c_and_links(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
     assert out.stdout.split() == [str(len(names)), "128"]
+
+
+def test_frames_on_the_host_pool():
+    """Large batches build their frames on a pool of host threads kept across
+    calls: the frames equal the one-pose calls', repeated calls and
+    concurrent callers agree, and a process forked after the pool exists
+    builds its own (the child has none of the parent's threads) instead of
+    waiting on them."""
+    import os
+    import threading
+    import time
+    import warnings
+    import numpy as np
+    from gdock_gb300 import synth
+    g = synth.random_genes(np.random.default_rng(1), 20000)
+    a = _lib.make_frames(g)
+    assert np.array_equal(a[::997], np.stack([_lib.make_frames(g[i:i + 1])[0] for i in range(0, 20000, 997)]))
+    for _ in range(3):
+        assert np.array_equal(_lib.make_frames(g), a)
+    ok = []
+    ts = [threading.Thread(target=lambda: ok.append(np.array_equal(_lib.make_frames(g), a))) for _ in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert ok == [True] * 4
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", DeprecationWarning)
+        pid = os.fork()
+    if pid == 0:
+        os._exit(0 if np.array_equal(_lib.make_frames(g), a) else 3)
+    t_end = time.time() + 60
+    while True:
+        done, status = os.waitpid(pid, os.WNOHANG)
+        if done:
+            break
+        if time.time() > t_end:
+            os.kill(pid, 9)
+            os.waitpid(pid, 0)
+            raise AssertionError("the forked child did not finish building frames")
+        time.sleep(0.05)
+    assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0

@@ -874,6 +874,20 @@ static void frames_and_max_disp(const double *genes, int n, gd_pose_frame *frame
   if (max_disp) *max_disp = *std::max_element(m.begin(), m.end());
 }
 
+// memcpy on the host pool for copies of 1 MiB or more (a large scoring
+// call's results out of the pinned staging buffer)
+static void copy_out(void *dst, const void *src, size_t bytes) {
+  if (bytes < (size_t(1) << 20)) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  const int nt = 16;
+  HostPool::get().run(nt, [&](int t) {
+    const size_t b0 = bytes * t / nt, b1 = bytes * (t + 1) / nt;
+    std::memcpy(static_cast<char *>(dst) + b0, static_cast<const char *>(src) + b0, b1 - b0);
+  });
+}
+
 gd_status gd_make_frames(const double *genes, int32_t n, gd_pose_frame *frames) {
   if (n < 0 || (n > 0 && (!genes || !frames))) return GD_ERR_INVALID_ARG;
   frames_and_max_disp(genes, n, frames, nullptr);
@@ -920,7 +934,7 @@ gd_status gd_score_poses(gd_complex *cx, const double *genes, int32_t n, gd_prec
   lap("score_poses: wait for the device");
   s = check_device_error(ctx);
   if (s != GD_OK) return s;
-  std::memcpy(out, h_out, ob);
+  copy_out(out, h_out, ob);
   lap("score_poses: error word and result copy");
   return GD_OK;
 }
@@ -1024,7 +1038,7 @@ gd_status gd_score_models(gd_complex *cx, const double *lig_xyz, int32_t n_model
   if (e != cudaSuccess) return cuda_fail(ctx, e, "score kernel");
   s = check_device_error(ctx);
   if (s != GD_OK) return s;
-  std::memcpy(out, h_out, ob);
+  copy_out(out, h_out, ob);
   return GD_OK;
 }
 

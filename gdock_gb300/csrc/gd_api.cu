@@ -331,13 +331,13 @@ static std::vector<int> segment_order(const double *x, const double *y, const do
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
   struct Span { int lo, hi, unit; };
-  std::vector<Span> todo{{0, n, kRecSeg}};
-  while (!todo.empty()) {
-    const Span sp = todo.back();
-    todo.pop_back();
+  std::vector<Span> pending{{0, n, kRecSeg}};
+  while (!pending.empty()) {
+    const Span sp = pending.back();
+    pending.pop_back();
     const int m = sp.hi - sp.lo;
     if (m <= sp.unit) {
-      if (sp.unit > 8 && m > 8) todo.push_back({sp.lo, sp.hi, 8});
+      if (sp.unit > 8 && m > 8) pending.push_back({sp.lo, sp.hi, 8});
       continue;
     }
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -352,8 +352,8 @@ static std::vector<int> segment_order(const double *x, const double *y, const do
     std::stable_sort(order.begin() + sp.lo, order.begin() + sp.hi, [c](int a, int b) { return c[a] < c[b]; });
     const int nseg = (m + sp.unit - 1) / sp.unit;
     const int mid = sp.lo + (nseg / 2) * sp.unit;
-    todo.push_back({mid, sp.hi, sp.unit});
-    todo.push_back({sp.lo, mid, sp.unit});
+    pending.push_back({mid, sp.hi, sp.unit});
+    pending.push_back({sp.lo, mid, sp.unit});
   }
   return order;
 }

@@ -267,26 +267,32 @@ def autotune_ga(gd, _lib, ctx, cxs, pop, split_mode, generations=3):
             "runs_per_s_by_variant": {variant_name(*k): v for k, v in rates.items()}}
 
 
-def run_c1(args):
+C1_WORKLOAD = ("synthetic receptor 50 residues x ligand 76 residues, 6 restraints, GA pop 150 x 50 generations "
+               "(fixed) with the Hall of Fame (500 entries, top 10 per generation), FCC clustering of the Hall of Fame")
+
+
+def measure_c1(split: str = "auto", steps: int = 1, warmup: int = 1) -> dict:
     """The small plain-method config: receptor 50 x ligand 76 residues, 6
     restraints, GA pop 150 x 50 generations in FP64 with the Hall of Fame, then
     FCC clustering of the Hall of Fame (src/commands/run.rs:666-686); one dock
-    per step.  The CPU leg runs the oracle's GA and Hall of Fame on the same
-    draws (gdock's own loop, threaded per pose) on the host cores."""
+    per step, and the same dock in the FP32 graph form.  The CPU leg runs the
+    oracle's GA and Hall of Fame on the same draws (gdock's own loop, threaded
+    per pose) on the host cores."""
     import gdock_gb300 as gd
     from gdock_gb300 import _lib, position_ligand, synth
     ctx = gd.Context(0)
-    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[args.split])
+    ctx.set_tuning(_lib.GD_TUNE_SPLIT, {"auto": 0, "never": 1, "always": 2}[split])
     c = synth.make_complex(50, 76, 6, seed=SEED)
     lig = position_ligand(c.receptor, c.ligand)
     cx = gd.Complex(c.receptor, lig, c.restraint_pairs, ctx=ctx)
     G, pop = 50, 150
     cfg = _lib.ga_default_cfg(pop_size=pop, max_generations=G, early_stopping=0, seed=7)
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx, hall_of_fame=True)
+        gd.run_ga([cx], cfg, gd.GD_PREC_F32, use_graph=True, ctx=ctx, hall_of_fame=True)
     times, times32 = [], []
-    res = None
-    for _ in range(max(1, args.steps)):
+    res = clusters = None
+    for _ in range(max(1, steps)):
         t0 = time.perf_counter()
         res = gd.run_ga([cx], cfg, gd.GD_PREC_F64, use_graph=False, ctx=ctx, hall_of_fame=True)
         clusters = cx.cluster(res.hall_of_fame[0]["genes"])
@@ -297,7 +303,9 @@ def run_c1(args):
         times32.append(time.perf_counter() - t0)
     t, t32 = float(np.median(times)), float(np.median(times32))
     # CPU leg: the oracle's generation loop on the same draws, all host cores
-    from oracle import oracle as orc
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+    orc.build()
     draws = _lib.ga_draw(cfg, cfg.seed, G)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
@@ -311,26 +319,36 @@ def run_c1(args):
     close = []
     orc.run_ga(c.receptor, lig, c.restraint_pairs, cfg, draws, nthreads=threads, close_out=close)
     same_hof = bool(np.array_equal(np.array([g for g, _, _ in hof.entries]), res.hall_of_fame[0]["genes"]))
+    m = {"docks_per_s": 1.0 / t, "seconds_per_dock": t, "steps": len(times), "workload": C1_WORKLOAD,
+         "receptor_atoms": len(c.receptor), "ligand_atoms": len(lig),
+         "clusters": len(clusters), "hall_of_fame_entries": int(len(res.hall_of_fame[0])),
+         "hall_of_fame_equals_oracle": same_hof,
+         "f32_graph_docks_per_s": 1.0 / t32,
+         "final_population_equals_oracle": same,
+         "ga_comparisons": {"total": int(sum(t for t, _, _ in close)), "ties": int(sum(k for _, k, _ in close)),
+                            "margin_below_1e-9": int(sum(k for _, _, k in close)),
+                            "note": "fitness comparisons of bookkeeping, elitism, tournaments and the offspring "
+                                    "sort over the 50 generations; ties are equal values (identical poses), "
+                                    "margin_below_1e-9 the unequal ones decided by less than 1e-9 relative"},
+         "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "docks/s", "cores": threads, "kind": "port",
+                          "sample": "one full dock: the oracle's GA and Hall of Fame on the same draws, then "
+                                    "its FCC clustering"}}
+    cx.close()
+    ctx.close()
+    return m
+
+
+def run_c1(args):
+    m = measure_c1(args.split, args.steps, args.warmup)
     line = {"metric": "docks/s (plain FP64 GA, pop 150 x 50 generations, then FCC clustering)",
-            "value": 1.0 / t, "unit": "docks/s", "n_gpus": 1, "steps": len(times), "warmup": max(1, args.warmup),
-            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "synthetic receptor 50 residues x ligand 76 residues, 6 restraints, GA pop 150 "
-                                   "x 50 generations (fixed) with the Hall of Fame (500 entries, top 10 per "
-                                   "generation), FCC clustering of the Hall of Fame",
-                       "receptor_atoms": len(c.receptor), "ligand_atoms": len(lig)},
-            "clusters": len(clusters), "hall_of_fame_entries": int(len(res.hall_of_fame[0])),
-            "hall_of_fame_equals_oracle": same_hof,
-            "f32_graph_docks_per_s": 1.0 / t32,
-            "final_population_equals_oracle": same,
-            "ga_comparisons": {"total": int(sum(t for t, _, _ in close)), "ties": int(sum(k for _, k, _ in close)),
-                               "margin_below_1e-9": int(sum(k for _, _, k in close)),
-                               "note": "fitness comparisons of bookkeeping, elitism, tournaments and the offspring "
-                                       "sort over the 50 generations; ties are equal values (identical poses), "
-                                       "margin_below_1e-9 the unequal ones decided by less than 1e-9 relative"},
-            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "docks/s", "cores": threads, "kind": "port",
-                             "sample": "one full dock: the oracle's GA and Hall of Fame on the same draws, then "
-                                       "its FCC clustering"}}
+            "value": m["docks_per_s"], "unit": "docks/s", "n_gpus": 1, "steps": m["steps"],
+            "warmup": max(1, args.warmup), "ms_per_step": m["seconds_per_dock"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": C1_WORKLOAD, "receptor_atoms": m["receptor_atoms"],
+                       "ligand_atoms": m["ligand_atoms"]},
+            **{k: m[k] for k in ("clusters", "hall_of_fame_entries", "hall_of_fame_equals_oracle",
+                                 "f32_graph_docks_per_s", "final_population_equals_oracle", "ga_comparisons",
+                                 "cpu_baseline")}}
     print(json.dumps(line), flush=True)
 
 
@@ -832,7 +850,9 @@ def main():
     ctx.close()
     if rank == 0 and world == 1 and args.extras == "all":
         # the other half of the headline metric, measured in the same run:
-        # docks/s of the batched GA and served jobs/s with p50/p99 latency
+        # docks/s of one plain-method dock (FP64 and the FP32 graph form), of
+        # the batched GA, and served jobs/s with p50/p99 latency
+        line["single_dock"] = measure_c1(args.split, 1, 1)
         line["batched_ga"] = measure_c3(args.split, 1)
         line["served"] = measure_c4(args.split, rates=(32.0, 200.0), per_rate=32, fp64_jobs=2)
     if rank == 0:
